@@ -1,0 +1,363 @@
+"""ctypes binding of libgst.so (include/gst.h, include/gst_gen.h).
+
+The library is the product: every solve runs the CUDA kernels in libgst.so.
+There is no Python or CPU fallback; if the library is missing this module
+raises instead of degrading.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import enum
+from dataclasses import dataclass, field
+from pathlib import Path
+
+import numpy as np
+
+LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libgst.so"
+
+I32P = C.POINTER(C.c_int32)
+I64P = C.POINTER(C.c_int64)
+F64P = C.POINTER(C.c_double)
+
+MAX_K = 16
+COST_LIMIT = 1073741823
+
+
+class Status(enum.IntEnum):
+    OK = 0
+    INFEASIBLE = 1
+    BAD_INPUT = 2
+    OOM = 3
+    TIMEOUT = 4
+    CUDA_ERROR = 5
+    OVERFLOW = 6
+    INTERNAL = 7
+
+
+class GSTError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{Status(status).name}: {message}")
+        self.status = Status(status)
+
+
+class Opts(C.Structure):
+    _fields_ = [
+        ("struct_size", C.c_int32),
+        ("upper_bound", C.c_int32),
+        ("max_rounds", C.c_int32),
+        ("use_graph", C.c_int32),
+        ("collect_stats", C.c_int32),
+        ("reserved", C.c_int32 * 11),
+    ]
+
+
+# name -> (restype, argtypes); every symbol include/*.h declares
+SIGNATURES = {
+    "gst_graph_upload": (C.c_int, [I32P, I32P, I32P, C.c_int32, C.c_int64, C.POINTER(C.c_void_p)]),
+    "gst_graph_free": (None, [C.c_void_p]),
+    "gst_graph_num_vertices": (C.c_int32, [C.c_void_p]),
+    "gst_graph_num_entries": (C.c_int64, [C.c_void_p]),
+    "gst_solve": (C.c_int, [C.c_void_p, I32P, I32P, C.c_int32, C.POINTER(Opts), C.POINTER(C.c_void_p)]),
+    "gst_solve_batch": (
+        C.c_int,
+        [C.c_void_p, C.c_int32, I32P, I32P, I32P, C.POINTER(Opts), C.POINTER(C.c_void_p)],
+    ),
+    "gst_result_free": (None, [C.c_void_p]),
+    "gst_result_status": (C.c_int, [C.c_void_p]),
+    "gst_result_cost": (C.c_int32, [C.c_void_p]),
+    "gst_result_root": (C.c_int32, [C.c_void_p]),
+    "gst_result_num_vertices": (C.c_int32, [C.c_void_p]),
+    "gst_result_num_edges": (C.c_int32, [C.c_void_p]),
+    "gst_result_vertices": (None, [C.c_void_p, I32P]),
+    "gst_result_edges": (None, [C.c_void_p, I32P]),
+    "gst_result_states": (C.c_int64, [C.c_void_p]),
+    "gst_result_launches": (C.c_int64, [C.c_void_p]),
+    "gst_result_times": (None, [C.c_void_p, F64P]),
+    "gst_result_stats": (None, [C.c_void_p, I64P]),
+    "gst_graph_debug_table": (C.c_int, [C.c_void_p, C.c_int32, I32P]),
+    "gst_last_error": (C.c_char_p, []),
+    "gst_version": (C.c_char_p, []),
+    # generators (include/gst_gen.h)
+    "gst_gen_random_connected": (C.c_void_p, [C.c_int32, C.c_int64, C.c_int32, C.c_int32, C.c_uint64]),
+    "gst_gen_barabasi_albert": (C.c_void_p, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_uint64]),
+    "gst_host_graph_num_vertices": (C.c_int32, [C.c_void_p]),
+    "gst_host_graph_num_entries": (C.c_int64, [C.c_void_p]),
+    "gst_host_graph_copy": (None, [C.c_void_p, I32P, I32P, I32P]),
+    "gst_host_graph_free": (None, [C.c_void_p]),
+    "gst_gen_groups_uniform": (C.c_void_p, [C.c_int32, C.c_int32, C.c_int32, C.c_uint64]),
+    "gst_gen_groups_zipf_degree": (
+        C.c_void_p,
+        [I32P, I32P, C.c_int32, C.c_int64, C.c_int32, C.c_double, C.c_int32, C.c_int32, C.c_uint64],
+    ),
+    "gst_host_groups_k": (C.c_int32, [C.c_void_p]),
+    "gst_host_groups_num_members": (C.c_int64, [C.c_void_p]),
+    "gst_host_groups_copy": (None, [C.c_void_p, I32P, I32P]),
+    "gst_host_groups_free": (None, [C.c_void_p]),
+}
+
+_LIB = None
+
+
+def lib() -> C.CDLL:
+    """Loads libgst.so (building it first if the CUDA toolkit is present)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    from . import build
+
+    if build.toolkit_available():
+        build.build_library()  # no-op when up to date
+    if not LIB_PATH.exists():
+        raise RuntimeError(f"libgst.so not found at {LIB_PATH}; run gpu4gst_code_gb300.build")
+    dll = C.CDLL(str(LIB_PATH))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(dll, name)
+        fn.restype = res
+        fn.argtypes = args
+    _LIB = dll
+    return dll
+
+
+def _i32(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def _ptr(a: np.ndarray, t=I32P):
+    return a.ctypes.data_as(t)
+
+
+def last_error() -> str:
+    return lib().gst_last_error().decode()
+
+
+def version() -> str:
+    return lib().gst_version().decode()
+
+
+@dataclass
+class Result:
+    """One query's answer (gst_result)."""
+
+    status: Status
+    cost: int
+    root: int
+    vertices: np.ndarray
+    edges: np.ndarray  # (n, 3) int32: u < v, w
+    states: int
+    launches: int = 0
+    times_ms: tuple = (0.0, 0.0, 0.0, 0.0)
+    stats: dict = field(default_factory=dict)
+
+    @property
+    def feasible(self) -> bool:
+        return self.status == Status.OK
+
+
+STAT_NAMES = ("rounds", "vertices", "entries", "rows", "gathered", "improved", "splits", "bytes")
+
+
+def _read_result(r) -> Result:
+    L = lib()
+    st = Status(L.gst_result_status(r))
+    nv = L.gst_result_num_vertices(r)
+    ne = L.gst_result_num_edges(r)
+    v = np.zeros(nv, np.int32)
+    e = np.zeros((ne, 3), np.int32)
+    if nv:
+        L.gst_result_vertices(r, _ptr(v))
+    if ne:
+        L.gst_result_edges(r, _ptr(e))
+    t = (C.c_double * 4)()
+    L.gst_result_times(r, t)
+    s = (C.c_int64 * 8)()
+    L.gst_result_stats(r, s)
+    return Result(
+        status=st,
+        cost=int(L.gst_result_cost(r)),
+        root=int(L.gst_result_root(r)),
+        vertices=v,
+        edges=e,
+        states=int(L.gst_result_states(r)),
+        launches=int(L.gst_result_launches(r)),
+        times_ms=tuple(t),
+        stats=dict(zip(STAT_NAMES, list(s))),
+    )
+
+
+def make_opts(upper_bound: int = 0, max_rounds: int = 0, use_graph: bool = False, collect_stats: bool = False) -> Opts:
+    o = Opts()
+    o.struct_size = C.sizeof(Opts)
+    o.upper_bound = int(upper_bound)
+    o.max_rounds = int(max_rounds)
+    o.use_graph = int(bool(use_graph))
+    o.collect_stats = int(bool(collect_stats))
+    return o
+
+
+def groups_to_csr(groups) -> tuple[np.ndarray, np.ndarray]:
+    """[[members of group 0], [members of group 1], ...] -> (group_ptr, members)."""
+    ptr = [0]
+    mem: list[int] = []
+    for g in groups:
+        mem.extend(int(x) for x in g)
+        ptr.append(len(mem))
+    return _i32(ptr), _i32(mem)
+
+
+class Graph:
+    """A graph resident on the current GPU (gst_graph)."""
+
+    def __init__(self, row_ptr, col, w):
+        L = lib()
+        self.row_ptr = _i32(row_ptr)
+        self.col = _i32(col)
+        self.w = _i32(w)
+        V = len(self.row_ptr) - 1
+        h = C.c_void_p()
+        st = L.gst_graph_upload(_ptr(self.row_ptr), _ptr(self.col), _ptr(self.w), V, len(self.col), C.byref(h))
+        if st != Status.OK:
+            raise GSTError(st, last_error())
+        self._h = h
+        self.V = V
+        self.nnz = len(self.col)
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().gst_graph_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def solve(self, group_ptr, members=None, *, upper_bound=0, max_rounds=0, use_graph=False,
+              collect_stats=False, raise_on_error=True) -> Result:
+        """Solves one query. `group_ptr` may be a list of member lists."""
+        if members is None:
+            group_ptr, members = groups_to_csr(group_ptr)
+        gp, mem = _i32(group_ptr), _i32(members)
+        k = len(gp) - 1
+        o = make_opts(upper_bound, max_rounds, use_graph, collect_stats)
+        r = C.c_void_p()
+        st = lib().gst_solve(self._h, _ptr(gp), _ptr(mem), k, C.byref(o), C.byref(r))
+        msg = last_error()
+        try:
+            res = _read_result(r) if r.value else None
+        finally:
+            if r.value:
+                lib().gst_result_free(r)
+        if st not in (Status.OK, Status.INFEASIBLE) and raise_on_error:
+            raise GSTError(st, msg)
+        if res is None:
+            res = Result(Status(st), -1, -1, np.zeros(0, np.int32), np.zeros((0, 3), np.int32), 0)
+        return res
+
+    def debug_table(self, k: int) -> np.ndarray:
+        """(V, 2^k) table of the last solve with k groups (gst_graph_debug_table)."""
+        out = np.zeros(self.V * (1 << k), np.int32)
+        st = lib().gst_graph_debug_table(self._h, k, _ptr(out))
+        if st != Status.OK:
+            raise GSTError(st, last_error())
+        return out.reshape(self.V, 1 << k)
+
+    def solve_batch(self, queries, *, upper_bound=0, use_graph=False, collect_stats=False) -> list[Result]:
+        """queries: list of (group_ptr, members) or list of member-list lists."""
+        ks, gptr, mem = [], [0], []
+        for q in queries:
+            gp, m = q if isinstance(q, tuple) else groups_to_csr(q)
+            gp = _i32(gp)
+            ks.append(len(gp) - 1)
+            base = len(mem)
+            mem.extend(int(x) for x in m)
+            gptr.extend(int(base + x) for x in gp[1:])
+        ks_a, gp_a, mem_a = _i32(ks), _i32(gptr), _i32(mem)
+        n = len(ks)
+        outs = (C.c_void_p * n)()
+        o = make_opts(upper_bound, 0, use_graph, collect_stats)
+        st = lib().gst_solve_batch(self._h, n, _ptr(ks_a), _ptr(gp_a), _ptr(mem_a), C.byref(o), outs)
+        msg = last_error()
+        res = []
+        for i in range(n):
+            if outs[i]:
+                res.append(_read_result(outs[i]))
+                lib().gst_result_free(outs[i])
+            else:
+                res.append(None)
+        if st not in (Status.OK, Status.INFEASIBLE):
+            raise GSTError(st, msg)
+        return res
+
+
+# ------------------------------------------------------------- generators --
+@dataclass
+class CSR:
+    row_ptr: np.ndarray
+    col: np.ndarray
+    w: np.ndarray
+
+    @property
+    def V(self) -> int:
+        return len(self.row_ptr) - 1
+
+    @property
+    def nnz(self) -> int:
+        return len(self.col)
+
+
+def _take_graph(h) -> CSR:
+    L = lib()
+    if not h:
+        raise GSTError(Status.BAD_INPUT, "generator rejected its parameters")
+    try:
+        V = L.gst_host_graph_num_vertices(h)
+        n = L.gst_host_graph_num_entries(h)
+        rp = np.zeros(V + 1, np.int32)
+        col = np.zeros(n, np.int32)
+        w = np.zeros(n, np.int32)
+        L.gst_host_graph_copy(h, _ptr(rp), _ptr(col), _ptr(w))
+    finally:
+        L.gst_host_graph_free(h)
+    return CSR(rp, col, w)
+
+
+def _take_groups(h) -> tuple[np.ndarray, np.ndarray]:
+    L = lib()
+    if not h:
+        raise GSTError(Status.BAD_INPUT, "group generator rejected its parameters")
+    try:
+        k = L.gst_host_groups_k(h)
+        n = L.gst_host_groups_num_members(h)
+        gp = np.zeros(k + 1, np.int32)
+        mem = np.zeros(n, np.int32)
+        L.gst_host_groups_copy(h, _ptr(gp), _ptr(mem))
+    finally:
+        L.gst_host_groups_free(h)
+    return gp, mem
+
+
+def gen_random_connected(V: int, E: int, wmin: int, wmax: int, seed: int) -> CSR:
+    return _take_graph(lib().gst_gen_random_connected(V, E, wmin, wmax, seed))
+
+
+def gen_barabasi_albert(V: int, m: int, wmin: int, wmax: int, seed: int) -> CSR:
+    return _take_graph(lib().gst_gen_barabasi_albert(V, m, wmin, wmax, seed))
+
+
+def gen_groups_uniform(V: int, k: int, size: int, seed: int):
+    return _take_groups(lib().gst_gen_groups_uniform(V, k, size, seed))
+
+
+def gen_groups_zipf_degree(g: CSR, k: int, s: float, size_min: int, size_max: int, seed: int):
+    """Zipf(s)-sized groups clipped to [size_min, size_max], members by degree."""
+    rp, col = _i32(g.row_ptr), _i32(g.col)
+    return _take_groups(
+        lib().gst_gen_groups_zipf_degree(_ptr(rp), _ptr(col), g.V, g.nnz, k, s, size_min, size_max, seed)
+    )

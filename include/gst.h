@@ -1,0 +1,150 @@
+/*
+ * gst.h — C ABI of the GB300 exact group Steiner tree (GST) solver.
+ *
+ * One call solves one query exactly with the DPBF dynamic program: a graph
+ * (integer-weighted, undirected, in CSR form) and k vertex groups go in; a
+ * minimum-cost tree touching every group and its cost come out.
+ *
+ * The functions replace the reference's single-GPU entry point
+ *   graph_hash_of_mixed_weighted DPBF_GPU(node **host_tree, node *host_tree_one_d,
+ *       CSR_graph &graph, std::unordered_set<int> &cumpulsory_group_vertices,
+ *       graph_v_of_v_idealID &group_graph, graph_v_of_v_idealID &input_graph,
+ *       int *pointer1, int *real_cost, int *community, int *c_size,
+ *       non_overlapped_group_sets s, double *rt)
+ * declared at rucgraph/DPQ.cuh:57 and defined at src/DPQ.cu:501-768, and the
+ * CSR upload of toCSR (rucgraph/graph_v_of_v_idealID/csr_graph.hpp:29-65).
+ * Plain pointers and sizes only; every call returns a gst_status and never
+ * exits the process (the reference prints and returns an empty tree, or
+ * calls exit(), where these return GST_INFEASIBLE / GST_BAD_INPUT).
+ *
+ * Threading: calls on one gst_graph are serialised internally (the graph
+ * owns one device workspace); distinct graphs may be used from distinct
+ * threads. All device work runs on the device that was current when the
+ * graph was uploaded, on a stream the graph owns; every call returns only
+ * after its device work finished (synchronous, like DPBF_GPU).
+ */
+#ifndef GST_H_
+#define GST_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum gst_status {
+  GST_OK = 0,
+  GST_INFEASIBLE = 1, /* no tree covers every group (reference: src/DPQ.cu:620-624) */
+  GST_BAD_INPUT = 2,  /* malformed CSR, group list, k out of range, negative weight */
+  GST_OOM = 3,        /* a device or host allocation failed */
+  GST_TIMEOUT = 4,    /* a convergence loop hit gst_opts.max_rounds */
+  GST_CUDA_ERROR = 5, /* a CUDA runtime call failed; see gst_last_error() */
+  GST_OVERFLOW = 6,   /* a tree cost reached GST_COST_LIMIT (int32 headroom) */
+  GST_INTERNAL = 7    /* an internal consistency check failed */
+} gst_status;
+
+/* Largest number of groups per query (the state table is V x 2^k). */
+#define GST_MAX_K 16
+/* Every tree cost must stay below this; larger sums report GST_OVERFLOW. */
+#define GST_COST_LIMIT 1073741823
+
+typedef struct gst_graph gst_graph;
+typedef struct gst_result gst_result;
+
+/* Solve options. Zero-initialise, set struct_size = sizeof(gst_opts), then
+ * change what you need; a NULL pointer means all defaults. */
+typedef struct gst_opts {
+  int32_t struct_size;
+  /* Upper bound on the optimal cost known to the caller (the cost of any
+   * feasible tree); states whose cost plus the one-label lower bound
+   * exceeds it are pruned. <= 0: no bound. A bound below the true optimum
+   * makes the solve return GST_INFEASIBLE. */
+  int32_t upper_bound;
+  /* Cap on growth rounds per DP wave; 0 = V + 1 (always enough). */
+  int32_t max_rounds;
+  /* 1 = drive the DP through a captured CUDA graph (one launch per query);
+   * 0 = launch kernels from the host loop. Both give identical results. */
+  int32_t use_graph;
+  /* 1 = fill the per-kernel statistics returned by gst_result_stats. */
+  int32_t collect_stats;
+  int32_t reserved[11];
+} gst_opts;
+
+/* ---------------------------------------------------------------- graph -- */
+
+/* Copies a CSR graph to the current device and keeps it resident.
+ * row_ptr[V+1] (row_ptr[0] = 0, non-decreasing, row_ptr[V] = nnz),
+ * col[nnz] in [0,V), w[nnz] in [0, GST_COST_LIMIT). Undirected graphs list
+ * each edge in both rows, as toCSR does; weights are the reference's int
+ * truncation of its double weights (csr_graph.hpp:46). Parallel entries
+ * are allowed (the lighter one wins).
+ * Replaces toCSR's cudaMallocManaged + cudaMemcpy (csr_graph.hpp:55-61). */
+gst_status gst_graph_upload(const int32_t *row_ptr, const int32_t *col, const int32_t *w, int32_t V,
+                            int64_t nnz, gst_graph **out);
+
+/* Frees the device copy and the workspace (csr_graph: caller frees,
+ * rucgraph/test_gpu.h:281-283). NULL is ignored. */
+void gst_graph_free(gst_graph *g);
+
+int32_t gst_graph_num_vertices(const gst_graph *g);
+int64_t gst_graph_num_entries(const gst_graph *g);
+
+/* ---------------------------------------------------------------- solve -- */
+
+/* Solves one query: group g (0 <= g < k) is members[group_ptr[g] ..
+ * group_ptr[g+1]). Bit g of a group-set mask stands for group g (the
+ * reference uses the iteration order of its unordered_set, DPQ.cu:22-34;
+ * the optimal cost does not depend on the order).
+ * On GST_OK, *out holds the optimal cost, the root vertex and the tree.
+ * On GST_INFEASIBLE, *out holds an empty tree and cost -1.
+ * Replaces DPBF_GPU (src/DPQ.cu:501-768). */
+gst_status gst_solve(gst_graph *g, const int32_t *group_ptr, const int32_t *members, int32_t k,
+                     const gst_opts *opts, gst_result **out);
+
+/* Solves nq independent queries on one resident graph. Query q has ks[q]
+ * groups; the groups of all queries are concatenated: query q owns groups
+ * [b_q, b_q + ks[q]) with b_q = ks[0] + ... + ks[q-1], and group j is
+ * members[group_ptr[j] .. group_ptr[j+1]). out[q] receives each query's
+ * result (also for infeasible queries); the return value is the first
+ * non-OK, non-INFEASIBLE status, else GST_OK. No counterpart in the
+ * reference (it runs one query per DPBF_GPU call). */
+gst_status gst_solve_batch(gst_graph *g, int32_t nq, const int32_t *ks, const int32_t *group_ptr,
+                           const int32_t *members, const gst_opts *opts, gst_result **out);
+
+/* --------------------------------------------------------------- result -- */
+
+void gst_result_free(gst_result *r);
+gst_status gst_result_status(const gst_result *r);
+/* Optimal cost (DPBF_GPU's *real_cost), -1 if infeasible. */
+int32_t gst_result_cost(const gst_result *r);
+/* Vertex whose full-mask state attains the cost (DPQ.cu:712-721). */
+int32_t gst_result_root(const gst_result *r);
+/* Distinct tree vertices / edges. Edges are (u, v, w) triples, u < v. */
+int32_t gst_result_num_vertices(const gst_result *r);
+int32_t gst_result_num_edges(const gst_result *r);
+/* Copy out; buffers must hold num_vertices / 3*num_edges int32. */
+void gst_result_vertices(const gst_result *r, int32_t *vertices);
+void gst_result_edges(const gst_result *r, int32_t *edges);
+/* DP states settled (DPBF_GPU's *pointer1 counter, DPQ.cu:675). */
+int64_t gst_result_states(const gst_result *r);
+/* CUDA kernels the solve launched (no counterpart in the reference). */
+int64_t gst_result_launches(const gst_result *r);
+/* Device milliseconds: [0] whole solve, [1] growth rounds (DPBF_GPU's *rt,
+ * DPQ.cu:707-709), [2] merges, [3] argmin + backtrack. */
+void gst_result_times(const gst_result *r, double *ms4);
+/* Statistics (filled when opts.collect_stats): [0] growth rounds launched,
+ * [1] vertices scanned, [2] CSR entries scanned, [3] neighbour rows
+ * gathered, [4] state entries gathered, [5] states improved, [6] merge
+ * splits evaluated, [7] algorithmic bytes of the growth kernel. */
+void gst_result_stats(const gst_result *r, int64_t *stats8);
+
+/* ---------------------------------------------------------------- misc -- */
+
+/* Message of the last failing call on this thread ("" if none). */
+const char *gst_last_error(void);
+const char *gst_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GST_H_ */

@@ -1,0 +1,187 @@
+"""GPU parity tests: libgst (CUDA, through the C ABI) against the oracle.
+
+Costs must match the reference CPU DPBF bit-exactly (integer arithmetic:
+no tolerance), every returned tree must be a valid group Steiner tree of
+exactly that cost, and on small instances the whole V x 2^k state table
+must equal the oracle's exact fixpoint."""
+import numpy as np
+import pytest
+
+import oracle
+from conftest import load_edge_cases, load_fixture, make_instance
+from gpu4gst_code_gb300 import dpbf, native
+from gpu4gst_code_gb300.native import Status
+
+pytestmark = pytest.mark.gpu
+
+ORACLE_INF = 2**31 - 1
+
+
+def _check(g_rp, g_col, g_w, gp, mem, res, cost):
+    assert res.status == Status.OK
+    assert res.cost == cost
+    err = oracle.check_tree(g_rp, g_col, g_w, gp, mem, res.vertices, res.edges, res.cost)
+    assert err is None, err
+
+
+def test_fixture_simple_iterative():
+    rp, col, w, gp, mem, cost = load_fixture()
+    with native.Graph(rp, col, w) as g:
+        res = g.solve(gp, mem)
+        _check(rp, col, w, gp, mem, res, cost)
+        assert cost == 16
+
+
+def test_golden_costs_bit_exact(golden):
+    graphs = {}
+    for case in golden["cases"]:
+        g, gp, mem = make_instance(case)
+        key = tuple(case["graph"])
+        if key not in graphs:
+            graphs[key] = native.Graph(g.row_ptr, g.col, g.w)
+        res = graphs[key].solve(gp, mem)
+        _check(g.row_ptr, g.col, g.w, gp, mem, res, case["dpbf"])
+    for dg in graphs.values():
+        dg.close()
+
+
+def test_edge_cases():
+    for name, c in load_edge_cases().items():
+        with native.Graph(c["rp"], c["col"], c["w"]) as g:
+            res = g.solve(c["gp"], c["mem"])
+            if int(c["cost"]) < 0:
+                assert res.status == Status.INFEASIBLE, name
+                assert res.cost == -1 and len(res.vertices) == 0
+            else:
+                _check(c["rp"], c["col"], c["w"], c["gp"], c["mem"], res, int(c["cost"]))
+
+
+def test_empty_group_is_infeasible():
+    rp, col, w, gp, mem, _ = load_fixture()
+    gp2 = np.concatenate([gp, [gp[-1]]]).astype(np.int32)  # a 5th group with no members
+    with native.Graph(rp, col, w) as g:
+        assert g.solve(gp2, mem).status == Status.INFEASIBLE
+
+
+@pytest.mark.parametrize("idx", [0, 1, 2, 3, 200, 201, 202, 203, 204])
+def test_full_state_table_matches_oracle(golden, idx):
+    case = golden["cases"][idx]
+    g, gp, mem = make_instance(case)
+    if g.V > 6000:
+        pytest.skip("table check kept to small graphs")
+    k = len(gp) - 1
+    want = oracle.dp_table(g.row_ptr, g.col, g.w, gp, mem)
+    want = np.where(want == ORACLE_INF, native.COST_LIMIT, want)
+    with native.Graph(g.row_ptr, g.col, g.w) as dg:
+        res = dg.solve(gp, mem)
+        assert res.status == Status.OK
+        got = dg.debug_table(k)
+    # the last wave is merged but not grown (growth cannot lower the optimum)
+    full = (1 << k) - 1
+    assert np.array_equal(got[:, 1:full], want[:, 1:full])
+    assert got[:, full].min() == want[:, full].min() == case["dpbf"]
+    assert np.all(got[:, full] >= want[:, full])
+
+
+def test_upper_bound_pruning_is_exact(golden):
+    for case in golden["cases"][::20] + golden["cases"][200:]:
+        g, gp, mem = make_instance(case)
+        opt = case["dpbf"]
+        with native.Graph(g.row_ptr, g.col, g.w) as dg:
+            for ub in (opt, opt + 1, opt + 50, 2 * opt + 1):
+                if ub <= 0:
+                    continue
+                res = dg.solve(gp, mem, upper_bound=ub)
+                _check(g.row_ptr, g.col, g.w, gp, mem, res, opt)
+            if opt > 1:
+                # a bound below the optimum prunes every full tree
+                assert dg.solve(gp, mem, upper_bound=opt - 1).status == Status.INFEASIBLE
+
+
+def test_hub_rows_use_block_path():
+    # star: hub 0 joined to 600 leaves (degree > 64 -> one CTA per row)
+    V = 601
+    edges = [(0, i, 1 + (i * 7) % 13) for i in range(1, V)] + [(i, i + 1, 50) for i in range(1, V - 1)]
+    rows = [[] for _ in range(V)]
+    for a, b, ww in edges:
+        rows[a].append((b, ww))
+        rows[b].append((a, ww))
+    rp, col, w = [0], [], []
+    for r in rows:
+        r.sort()
+        col += [x for x, _ in r]
+        w += [y for _, y in r]
+        rp.append(len(col))
+    groups = [[5, 300], [77], [450, 12], [599], [3, 4]]
+    gp, mem = native.groups_to_csr(groups)
+    want = oracle.dpbf(rp, col, w, gp, mem)
+    with native.Graph(rp, col, w) as g:
+        res = g.solve(gp, mem)
+        _check(rp, col, w, gp, mem, res, want.cost)
+
+
+@pytest.mark.parametrize("k", [1, 2, 5, 8, 10])
+def test_many_group_counts(k):
+    g = native.gen_random_connected(700, 2500, 1, 60, 40 + k)
+    gp, mem = native.gen_groups_uniform(700, k, 3, 50 + k)
+    want = oracle.dpbf(g.row_ptr, g.col, g.w, gp, mem)
+    with native.Graph(g.row_ptr, g.col, g.w) as dg:
+        res = dg.solve(gp, mem)
+        _check(g.row_ptr, g.col, g.w, gp, mem, res, want.cost)
+
+
+def test_workspace_reuse_across_k_and_repeat():
+    g = native.gen_barabasi_albert(4000, 4, 1, 100, 3)
+    with native.Graph(g.row_ptr, g.col, g.w) as dg:
+        for k, seed in [(3, 1), (6, 2), (4, 3), (6, 2), (2, 5)]:
+            gp, mem = native.gen_groups_zipf_degree(g, k, 1.2, 5, 500, seed)
+            want = oracle.dpbf(g.row_ptr, g.col, g.w, gp, mem)
+            res = dg.solve(gp, mem)
+            _check(g.row_ptr, g.col, g.w, gp, mem, res, want.cost)
+
+
+def test_batch_matches_single(golden):
+    g = native.gen_barabasi_albert(3000, 4, 1, 100, 17)
+    queries = [native.gen_groups_zipf_degree(g, 3 + (i % 5), 1.2, 5, 500, 900 + i) for i in range(12)]
+    with native.Graph(g.row_ptr, g.col, g.w) as dg:
+        batch = dg.solve_batch(queries)
+        for (gp, mem), res in zip(queries, batch):
+            want = oracle.dpbf(g.row_ptr, g.col, g.w, gp, mem)
+            _check(g.row_ptr, g.col, g.w, gp, mem, res, want.cost)
+
+
+def test_reference_call_surface_on_fixture():
+    # the reference's harness flow (rucgraph/test_gpu.h:116-223) through the mirror
+    rp, col, w, gp, mem, cost = load_fixture()
+    input_graph = dpbf.csr_to_graph_v_of_v(rp, col, w)
+    groups = [list(mem[gp[i]:gp[i + 1]]) for i in range(len(gp) - 1)]
+    group_graph, group_vertices = dpbf.group_graph_from_groups(len(input_graph), groups)
+    csr = dpbf.toCSR(input_graph)
+    counter = [0]
+    tree, real_cost, processed, rt = dpbf.DPBF_GPU(csr, group_vertices, group_graph, input_graph, pointer1=counter)
+    assert real_cost == cost == 16
+    assert dpbf.graph_hash_of_mixed_weighted_sum_of_ec(tree) == real_cost
+    assert dpbf.this_is_a_feasible_solution_gpu(tree, group_graph, group_vertices)
+    assert processed > 0 and counter[0] == processed and rt >= 0
+    csr.free()
+
+
+def test_bad_member_is_rejected():
+    rp, col, w, gp, mem, _ = load_fixture()
+    bad = mem.copy()
+    bad[0] = 10**6
+    with native.Graph(rp, col, w) as g:
+        with pytest.raises(native.GSTError) as e:
+            g.solve(gp, bad)
+        assert e.value.status == Status.BAD_INPUT
+
+
+def test_timeout_status_is_reported():
+    g = native.gen_random_connected(2000, 4000, 1, 100, 8)
+    gp, mem = native.gen_groups_uniform(2000, 3, 2, 9)
+    with native.Graph(g.row_ptr, g.col, g.w) as dg:
+        res = dg.solve(gp, mem, max_rounds=1, raise_on_error=False)
+        assert res.status == Status.TIMEOUT
+        # the graph stays usable after the error
+        want = oracle.dpbf(g.row_ptr, g.col, g.w, gp, mem)
+        _check(g.row_ptr, g.col, g.w, gp, mem, dg.solve(gp, mem), want.cost)

@@ -1,0 +1,124 @@
+"""CPU-only checks of libgst: it loads, exports every symbol the headers
+declare, and rejects bad input before touching the device. No call here
+launches GPU work."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from gpu4gst_code_gb300 import dpbf, native
+from gpu4gst_code_gb300.native import Status
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def declared_functions():
+    names = set()
+    for h in (ROOT / "include").glob("*.h"):
+        text = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
+        for m in re.finditer(r"\b(gst_[a-z0-9_]+)\s*\(", text):
+            names.add(m.group(1))
+    return sorted(names)
+
+
+def test_library_exports_every_declared_symbol():
+    lib = native.lib()
+    names = declared_functions()
+    assert "gst_solve" in names and "gst_graph_upload" in names
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_binding_covers_every_declared_symbol():
+    assert set(declared_functions()) <= set(native.SIGNATURES)
+
+
+def test_version_string():
+    assert "sm_103a" in native.version()
+
+
+def _upload(rp, col, w, V=None, nnz=None):
+    rp, col, w = (np.ascontiguousarray(x, np.int32) for x in (rp, col, w))
+    h = C.c_void_p()
+    st = native.lib().gst_graph_upload(rp.ctypes.data_as(native.I32P), col.ctypes.data_as(native.I32P),
+                                       w.ctypes.data_as(native.I32P), len(rp) - 1 if V is None else V,
+                                       len(col) if nnz is None else nnz, C.byref(h))
+    return st, h
+
+
+@pytest.mark.parametrize(
+    "rp,col,w,why",
+    [
+        ([1, 2], [0], [1], "row_ptr[0] != 0"),
+        ([0, 2, 1], [1, 0], [1, 1], "decreasing row_ptr"),
+        ([0, 1, 2], [1, 5], [1, 1], "col out of range"),
+        ([0, 1, 2], [1, 0], [1, -3], "negative weight"),
+        ([0, 1, 2], [1, 0], [1, native.COST_LIMIT], "weight at the cost limit"),
+    ],
+)
+def test_upload_rejects_bad_csr(rp, col, w, why):
+    st, h = _upload(rp, col, w)
+    assert st == Status.BAD_INPUT, why
+    assert not h.value
+    assert native.last_error()
+
+
+def test_upload_rejects_nnz_mismatch():
+    st, _ = _upload([0, 1, 2], [1, 0], [1, 1], nnz=1)
+    assert st == Status.BAD_INPUT
+
+
+def test_solve_rejects_null_graph():
+    gp = np.array([0, 1], np.int32)
+    mem = np.array([0], np.int32)
+    r = C.c_void_p()
+    st = native.lib().gst_solve(None, gp.ctypes.data_as(native.I32P), mem.ctypes.data_as(native.I32P), 1, None,
+                                C.byref(r))
+    assert st == Status.BAD_INPUT and not r.value
+
+
+def test_generators_are_deterministic():
+    a = native.gen_barabasi_albert(2000, 4, 1, 100, 9)
+    b = native.gen_barabasi_albert(2000, 4, 1, 100, 9)
+    assert np.array_equal(a.col, b.col) and np.array_equal(a.w, b.w)
+    assert a.nnz == 2 * (10 + (2000 - 5) * 4)
+    # symmetric, sorted rows, no self loops
+    for v in range(0, 2000, 97):
+        row = a.col[a.row_ptr[v]:a.row_ptr[v + 1]]
+        assert np.all(np.diff(row) > 0) and v not in row
+        for u in row:
+            assert v in a.col[a.row_ptr[u]:a.row_ptr[u + 1]]
+    gp, mem = native.gen_groups_zipf_degree(a, 6, 1.2, 5, 500, 4)
+    sizes = np.diff(gp)
+    assert len(sizes) == 6 and sizes.min() >= 5 and sizes.max() <= 500
+    for g in range(6):
+        assert len(set(mem[gp[g]:gp[g + 1]])) == sizes[g]
+
+
+def test_random_connected_shape():
+    g = native.gen_random_connected(1000, 5000, 1, 100, 0)
+    assert g.nnz == 10000 and g.w.min() >= 1 and g.w.max() <= 100
+
+
+def test_reference_mirror_helpers():
+    # toCSR truncates double weights like csr_graph.hpp:46
+    gv = [[(1, 2.9)], [(0, 2.9), (2, 1.5)], [(1, 1.5)]]
+    csr = dpbf.toCSR(gv)
+    assert list(csr.all_pointer) == [0, 1, 3, 4]
+    assert list(csr.all_edge_weight) == [2, 2, 1, 1]
+    s = dpbf.graph_v_of_v_idealID_DPBF_non_overlapped_group_sets_gpu(7)
+    # sum over masks i of (2^(k-|i|) - 1) = 3^k - 2^(k+1) + 1 for k=3
+    assert s.length == 27 - 16 + 1
+    tree = dpbf.graph_hash_of_mixed_weighted()
+    for v in (0, 1, 2):
+        tree.add_vertex(v)
+    tree.add_edge(0, 1, 2)
+    tree.add_edge(1, 2, 1)
+    assert dpbf.graph_hash_of_mixed_weighted_sum_of_ec(tree) == 3
+    gg, gids = dpbf.group_graph_from_groups(3, [[0], [2]])
+    assert dpbf.this_is_a_feasible_solution_gpu(tree, gg, gids)
+    lone = dpbf.graph_hash_of_mixed_weighted()
+    lone.add_vertex(0)
+    assert not dpbf.this_is_a_feasible_solution_gpu(lone, gg, gids)
