@@ -139,7 +139,11 @@ __global__ void __launch_bounds__(kGrowThreads) k_merge(GraphDev g, LevelArgs a)
 // per vertex (blocks [0, nbig)), partial minima combined in shared memory.
 template <int G, int MPL>
 __global__ void __launch_bounds__(kGrowThreads) k_grow(GraphDev g, LevelArgs a) {
-  if (*a.prev_changed == 0) return;  // the previous round changed nothing
+  if (*a.prev_changed == 0) {
+    // converged: keep the rotation consistent so later rounds also see 0
+    if (blockIdx.x == 0 && threadIdx.x == 0) *a.zero_changed = 0;
+    return;
+  }
   const int tid = threadIdx.x;
   const int lane = tid & 31;
   const int glane = lane & (G - 1);

@@ -1,0 +1,110 @@
+/*
+ * gst_dpbf_dropin.hpp — the reference's DPBF_GPU entry point, implemented on
+ * libgst.
+ *
+ * For a codebase built on the reference's headers: compile exactly one .cpp
+ * that includes the reference's "DPQ.cuh" first and this header second, in
+ * place of src/DPQ.cu, and link libgst.so. Every existing caller of
+ *
+ *   graph_hash_of_mixed_weighted DPBF_GPU(node **host_tree, node *host_tree_one_d,
+ *       CSR_graph &graph, std::unordered_set<int> &cumpulsory_group_vertices,
+ *       graph_v_of_v_idealID &group_graph, graph_v_of_v_idealID &input_graph,
+ *       int *pointer1, int *real_cost, int *community, int *c_size,
+ *       non_overlapped_group_sets s, double *rt);      (rucgraph/DPQ.cuh:57)
+ *
+ * (e.g. rucgraph/test_gpu.h:208) then runs the exact GB300 solver.
+ *
+ * Semantics kept from src/DPQ.cu:501-768:
+ *   - groups: for each g in cumpulsory_group_vertices, in iteration order,
+ *     the members are the first elements of group_graph[g] (DPQ.cu:22-34);
+ *   - the CSR arrays of toCSR (managed memory, host-readable) are the graph;
+ *     they are uploaded once per CSR_graph (keyed by all_edge) and kept;
+ *   - returns the tree (vertices with weight 0, edges with the CSR's int
+ *     weights, as the backtrack adds them at DPQ.cu:744-750), sets
+ *     *real_cost, adds the states written to *pointer1 and stores the
+ *     growth-phase seconds in *rt;
+ *   - no feasible tree: prints the reference's message and returns an empty
+ *     tree, leaving *real_cost untouched (DPQ.cu:620-624).
+ * Differences: host_tree / host_tree_one_d are not written (the state table
+ * stays on the device), `s` is not needed (splits are enumerated on the
+ * device), costs are exact beyond the reference's inf = 10000 cap
+ * (DPQ.cuh:48), and a CUDA or input error prints gst_last_error() and
+ * returns an empty tree instead of continuing silently.
+ * community and c_size are unused, as in the reference.
+ */
+#ifndef GST_DPBF_DROPIN_HPP_
+#define GST_DPBF_DROPIN_HPP_
+
+#include <cstdint>
+#include <iostream>
+#include <mutex>
+#include <unordered_map>
+#include <unordered_set>
+#include <vector>
+
+#include "gst.h"
+
+namespace gst_dropin {
+
+inline gst_graph *resident_graph(CSR_graph &graph) {
+  static std::mutex mu;
+  static std::unordered_map<const int *, gst_graph *> cache;
+  std::lock_guard<std::mutex> lock(mu);
+  auto it = cache.find(graph.all_edge);
+  if (it != cache.end()) return it->second;
+  gst_graph *g = nullptr;
+  if (gst_graph_upload(graph.all_pointer, graph.all_edge, graph.all_edge_weight, graph.V, graph.E_all, &g) !=
+      GST_OK) {
+    std::cout << "DPBF_GPU: graph upload failed: " << gst_last_error() << std::endl;
+    return nullptr;
+  }
+  cache[graph.all_edge] = g;
+  return g;
+}
+
+}  // namespace gst_dropin
+
+graph_hash_of_mixed_weighted DPBF_GPU(node **host_tree, node *host_tree_one_d, CSR_graph &graph,
+                                      std::unordered_set<int> &cumpulsory_group_vertices,
+                                      graph_v_of_v_idealID &group_graph, graph_v_of_v_idealID &input_graph,
+                                      int *pointer1, int *real_cost, int *community, int *c_size,
+                                      non_overlapped_group_sets s, double *rt) {
+  (void)host_tree;
+  (void)host_tree_one_d;
+  (void)input_graph;
+  (void)community;
+  (void)c_size;
+  (void)s;
+  graph_hash_of_mixed_weighted solution_tree;
+  gst_graph *g = gst_dropin::resident_graph(graph);
+  if (!g) return solution_tree;
+  std::vector<int32_t> group_ptr{0}, members;
+  for (int gid : cumpulsory_group_vertices) {
+    for (auto &e : group_graph[gid]) members.push_back(e.first);
+    group_ptr.push_back((int32_t)members.size());
+  }
+  gst_result *r = nullptr;
+  const gst_status st = gst_solve(g, group_ptr.data(), members.data(), (int32_t)cumpulsory_group_vertices.size(),
+                                  nullptr, &r);
+  if (st == GST_OK) {
+    std::vector<int32_t> vs((size_t)gst_result_num_vertices(r)), es(3 * (size_t)gst_result_num_edges(r));
+    gst_result_vertices(r, vs.data());
+    gst_result_edges(r, es.data());
+    for (int32_t v : vs) graph_hash_of_mixed_weighted_add_vertex(solution_tree, v, 0);
+    for (size_t i = 0; i < es.size(); i += 3)
+      graph_hash_of_mixed_weighted_add_edge(solution_tree, es[i], es[i + 1], es[i + 2]);
+    *real_cost = gst_result_cost(r);
+    if (pointer1) *pointer1 += (int)gst_result_states(r);
+    double ms[4];
+    gst_result_times(r, ms);
+    if (rt) *rt = ms[1] / 1e3;
+  } else if (st == GST_INFEASIBLE) {
+    std::cout << "can not find a solution" << std::endl;
+  } else {
+    std::cout << "DPBF_GPU: " << gst_last_error() << std::endl;
+  }
+  gst_result_free(r);
+  return solution_tree;
+}
+
+#endif /* GST_DPBF_DROPIN_HPP_ */

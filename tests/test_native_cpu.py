@@ -122,3 +122,25 @@ def test_reference_mirror_helpers():
     lone = dpbf.graph_hash_of_mixed_weighted()
     lone.add_vertex(0)
     assert not dpbf.this_is_a_feasible_solution_gpu(lone, gg, gids)
+
+
+def test_dropin_adapter_compiles_against_reference_headers(tmp_path):
+    """include/gst_dpbf_dropin.hpp defines the reference's DPBF_GPU
+    (rucgraph/DPQ.cuh:57) on libgst: compile it with the reference's own
+    headers and link it against libgst.so (no GPU needed to link)."""
+    import shutil
+    import subprocess
+
+    ref = Path("/root/reference/rucgraph")
+    if not (ref / "DPQ.cuh").exists() or not shutil.which("g++"):
+        pytest.skip("reference headers not present")
+    native.lib()
+    tu = tmp_path / "dropin.cpp"
+    tu.write_text('#include "DPQ.cuh"\n#include "gst_dpbf_dropin.hpp"\n'
+                  "int main(){ return &DPBF_GPU != nullptr ? 0 : 1; }\n")
+    cuda_inc = "/usr/local/cuda/include"
+    out = tmp_path / "dropin"
+    proc = subprocess.run(["g++", "-std=c++17", "-w", "-I", str(ref), "-I", cuda_inc, "-I", str(ROOT / "include"),
+                           str(tu), str(native.LIB_PATH), "-o", str(out), "-lpthread"],
+                          capture_output=True, text=True)
+    assert proc.returncode == 0, proc.stderr[-2000:]
