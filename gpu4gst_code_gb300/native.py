@@ -21,6 +21,7 @@ F64P = C.POINTER(C.c_double)
 
 MAX_K = 16
 COST_LIMIT = 1073741823
+NOALLOC_MAX_VERTICES = 1 << 20
 
 
 class Status(enum.IntEnum):
@@ -32,6 +33,7 @@ class Status(enum.IntEnum):
     CUDA_ERROR = 5
     OVERFLOW = 6
     INTERNAL = 7
+    TOO_LARGE = 8
 
 
 class GSTError(RuntimeError):
@@ -75,6 +77,11 @@ SIGNATURES = {
     "gst_result_times": (None, [C.c_void_p, F64P]),
     "gst_result_stats": (None, [C.c_void_p, I64P]),
     "gst_graph_debug_table": (C.c_int, [C.c_void_p, C.c_int32, I32P]),
+    "gst_group_distances_noalloc": (
+        C.c_int,
+        [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int64, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p,
+         C.c_void_p],
+    ),
     "gst_last_error": (C.c_char_p, []),
     "gst_version": (C.c_char_p, []),
     # generators (include/gst_gen.h)

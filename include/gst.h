@@ -40,7 +40,8 @@ typedef enum gst_status {
   GST_TIMEOUT = 4,    /* a convergence loop hit gst_opts.max_rounds */
   GST_CUDA_ERROR = 5, /* a CUDA runtime call failed; see gst_last_error() */
   GST_OVERFLOW = 6,   /* a tree cost reached GST_COST_LIMIT (int32 headroom) */
-  GST_INTERNAL = 7    /* an internal consistency check failed */
+  GST_INTERNAL = 7,   /* an internal consistency check failed */
+  GST_TOO_LARGE = 8   /* input beyond the fixed capacity of gst_group_distances_noalloc */
 } gst_status;
 
 /* Largest number of groups per query (the state table is V x 2^k). */
@@ -137,6 +138,45 @@ void gst_result_times(const gst_result *r, double *ms4);
  * gathered, [4] state entries gathered, [5] states improved, [6] merge
  * splits evaluated, [7] algorithmic bytes of the growth kernel. */
 void gst_result_stats(const gst_result *r, int64_t *stats8);
+
+/* ------------------------------------------------- allocation-free call -- */
+
+/* Largest graph gst_group_distances_noalloc accepts. */
+#define GST_NOALLOC_MAX_VERTICES (1 << 20)
+
+/* Distance from every vertex to the nearest of `sources` (one group), for
+ * callers that cannot allocate device memory: code inside a host
+ * application or serving stack that owns all device memory through its own
+ * pool (cudaMalloc/cudaFree would bypass its accounting), latency-critical
+ * paths that cannot take cudaMalloc's implicit device synchronisation, and
+ * plugins loaded after such a process has fixed its memory budget. This
+ * call allocates nothing: no cudaMalloc, cudaFree, stream, event or host
+ * heap memory.
+ *
+ * All pointers are DEVICE pointers owned by the caller: the CSR graph
+ * (row_ptr[V+1], col[nnz], w[nnz], same rules as gst_graph_upload; rows
+ * outside [0, nnz] and out-of-range entries give GST_BAD_INPUT),
+ * sources[num_sources] (vertex IDs), and the outputs dist[V] (GST_COST_LIMIT
+ * where unreachable) and pred[V] (the CSR entry e of u's row with col[e] the
+ * next vertex towards the sources and dist[u] = dist[col[e]] + w[e]; -1 for
+ * sources and unreachable vertices). `stream` is a cudaStream_t (NULL: the
+ * default stream); the call returns after its work on that stream is done.
+ *
+ * Limit: V <= GST_NOALLOC_MAX_VERTICES, else GST_TOO_LARGE and nothing runs.
+ * The frontier scratch (3 MiB + 256 B) is a fixed array in the library's
+ * device image, held on every GPU that loads the library until the process
+ * exits. The first call on a device looks up that array's address (once per
+ * device, with the device current); make that first call before capturing
+ * any stream. Every call shares the array and leaves its contents behind;
+ * each call clears what it uses first, but calls whose work overlaps on one
+ * GPU (other streams, other host threads) race and corrupt each other.
+ * Errors are returned as the status only (gst_last_error() is not set):
+ * GST_BAD_INPUT for NULL pointers, V < 1 or a source / CSR entry out of
+ * range, GST_OVERFLOW, GST_TIMEOUT, GST_CUDA_ERROR.
+ * No counterpart in the reference. */
+gst_status gst_group_distances_noalloc(const int32_t *row_ptr, const int32_t *col, const int32_t *w, int32_t V,
+                                       int64_t nnz, const int32_t *sources, int32_t num_sources, int32_t *dist,
+                                       int32_t *pred, void *stream);
 
 /* ---------------------------------------------------------------- misc -- */
 
