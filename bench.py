@@ -45,6 +45,9 @@ WORKLOADS = {
     "ba1m_k6": dict(V=1_000_000, m=4, wmin=1, wmax=100, k=6, zipf=(1.2, 5, 500), graph_seed=2,
                     desc="plain GPU DPBF, single query: BA m=4, |V|=1,000,000, w U[1,100], k=6, "
                          "Zipf(1.2) sizes in [5,500], degree-proportional members"),
+    "ba400k_k6": dict(V=400_000, m=4, wmin=1, wmax=100, k=6, zipf=(1.2, 5, 500), graph_seed=2,
+                      desc="profiling size of ba1m_k6: BA m=4, |V|=400,000, w U[1,100], k=6, Zipf(1.2) "
+                           "sizes in [5,500], degree-proportional members"),
     "ba2m_k8": dict(V=2_000_000, m=8, wmin=1, wmax=1000, k=8, uniform=50, graph_seed=3,
                     desc="plain GPU DPBF, large mask: BA m=8, |V|=2,000,000, w U[1,1000], k=8 x 50 uniform"),
     "rc1k_k3": dict(V=1000, E=5000, wmin=1, wmax=100, k=3, uniform=20, graph_seed=0,

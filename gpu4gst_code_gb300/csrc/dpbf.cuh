@@ -3,16 +3,18 @@
 //
 // State table layout in HBM ("level-major, vertex-major within a level"):
 // the 2^k - 1 non-empty group-set masks are ordered by popcount (the DP
-// wave, or level), then by value. Level l holds m_l = C(k,l) masks; its
-// slice starts at entry base_l * V with base_l = sum_{l'<l} m_l', and the
-// m_l entries of vertex v are contiguous at base_l*V + v*m_l + rank(S).
-// Growth at level l therefore gathers one contiguous m_l-entry row per
-// neighbour, and a merge reads the lower-level rows of its own vertex.
-// cost[] holds int32 tree costs (GST_INF = no tree); par[] holds how the
-// state was last improved:
-//   par >= 0        grown over CSR entry par of this vertex (col = child),
-//   par <  0        merged from S1 = -par and S ^ S1,
-//   par == GST_LEAF the vertex itself (S inside its groups, cost 0).
+// wave, or level), then by value. Level l holds m_l = C(k,l) masks in a row
+// of stride s_l = m_l rounded up to a multiple of 4 (padding entries hold
+// kInf), so every row starts on a 16-byte boundary and can be moved with
+// int4 loads. Level l's slice starts at entry base_l * V with
+// base_l = sum_{l'<l} s_l', and vertex v's row is at base_l*V + v*s_l.
+// Growth at level l gathers one contiguous row per neighbour; a merge reads
+// the lower-level rows of its own vertex.
+// cost[] holds int32 tree costs (kInf = no tree); par[] holds how the state
+// was last improved:
+//   par >= 0      grown over CSR entry par of this vertex (col = child),
+//   par <  0      merged from S1 = -par and S ^ S1,
+//   par == kLeaf  the vertex itself (S inside its groups, cost 0).
 #pragma once
 #include <cstdint>
 
@@ -24,13 +26,16 @@ constexpr int32_t kInf = 0x3FFFFFFF;  // == GST_COST_LIMIT; finite costs stay be
 constexpr int32_t kLeaf = INT32_MIN;
 constexpr int kDegBig = 64;        // rows longer than this go to a CTA of their own
 constexpr int kGrowThreads = 256;  // block size of growth / merge kernels
+constexpr int kMaxThreadMasks = 24;  // waves with stride <= this: a thread per vertex
+
+__host__ __device__ constexpr int32_t row_stride(int32_t m) { return (m + 3) & ~3; }
 
 // Per-mask position in the table (device copy built on the host for each k).
 struct MaskInfo {
-  int32_t base;   // base_l of the mask's level
-  int32_t m;      // masks in that level
-  int32_t rank;   // index within the level
-  int32_t level;  // popcount
+  int32_t base;    // base_l of the mask's level
+  int32_t stride;  // row stride s_l of that level
+  int32_t rank;    // index within the level
+  int32_t level;   // popcount
 };
 
 // Statistic slots (int64) accumulated by kernels when stats are on.
@@ -46,13 +51,42 @@ enum StatSlot {
   kNumStats = 8
 };
 
-// Device-side counters of one solve (a small int32 block).
+// Per-query scalars read by the kernels from device memory, so one
+// captured CUDA graph serves every query with the same k.
+struct SolveParams {
+  int32_t ub;          // upper bound for pruning (<= 0: none)
+  int32_t max_rounds;  // growth rounds allowed per wave
+  int32_t stats_on;    // accumulate StatSlot counters
+  int32_t k;
+  // Stored costs stay below kInf - (largest edge weight): then adding any
+  // weight to a finite cost stays below kInf, so relaxations need no
+  // overflow test. A cost that reaches the limit is reported (GST_OVERFLOW).
+  int32_t ovf_limit;
+  int32_t pad[3];
+};
+
+// Growth-loop control of the current wave (reset before each wave).
+// Round r uses change-count slot r%3 and reads slot (r+2)%3 (the previous
+// round; the merge acts as round -1 and fills slot 2); the last block to
+// finish a round publishes its total and advances `round`.
+struct GrowCtl {
+  int32_t round;
+  uint32_t done;        // blocks finished in the current round
+  int32_t changed[3];   // rotating per-round change counts
+  int32_t dense[3];     // round ran dense (all vertices, no candidate marks)
+  int32_t last_changed; // changes of the last completed round
+  int32_t timeout;      // stopped by max_rounds with changes pending
+};
+
+// Device-side counters of one solve.
 struct Counters {
-  int32_t changed[3];  // rotating per-round change counts
-  int32_t overflow;    // a candidate reached kInf
-  int32_t bt_overflow; // backtrack ran out of capacity
+  int32_t overflow;     // a candidate reached kInf
+  int32_t bt_overflow;  // backtrack ran out of capacity / found a bad record
   int32_t bt_nv, bt_ne, bt_states;
-  unsigned long long best;  // (cost << 32) | root, argmin of the full mask
+  int32_t rounds_total; // growth rounds that did work, all waves
+  int32_t timeout;
+  int32_t pad;
+  unsigned long long best;    // (cost << 32) | root, argmin of the full mask
   unsigned long long states;  // states written by merges + growth
 };
 
@@ -62,36 +96,41 @@ struct GraphDev {
   const int2* adj;         // (col, w) per CSR entry
   const int32_t* big;      // vertices with degree > kDegBig
   int32_t nbig;
+  const int32_t* order;    // the other vertices by decreasing degree
+  int32_t nsmall;          // V - nbig
+  const int2* hub_chunk;   // (hub index, first CSR entry) per 32-entry chunk
+  int64_t nchunks;
+  unsigned long long* hub_min;  // per hub: hub_stride packed (cost, entry) minima
+  int32_t* hub_cnt;             // per hub: chunks finished this round
+  int32_t hub_stride;
 };
 
 struct LevelArgs {
-  int32_t level, m, k;
+  int32_t level, m, stride, k;
   int64_t base;                // base_l * V
+  int32_t stride1;             // row stride of wave 1 (pruning bound)
   const int32_t* lmasks;       // masks of this level, by rank
   const MaskInfo* minfo;       // indexed by mask
   int32_t* cost;
   int32_t* par;
   const uint32_t* gmask;       // groups(v) bit mask
-  const uint8_t* cur_flag;     // changed in the previous round
-  uint8_t* next_flag;          // changed in this round
-  uint8_t* clear_flag;         // cleared for the round after next
-  const int32_t* prev_changed;
-  int32_t* cur_changed;
-  int32_t* zero_changed;
+  uint8_t* flags;              // changed flags F[0..2] (V bytes each)
+  uint8_t* cand;               // candidate flags C[0..2] (V bytes each)
+  GrowCtl* ctl;
   Counters* ctr;
-  long long* stats;            // nullptr when off
-  // pruning (upper_bound > 0): drop a state when cost + LB(v, full^S) > ub,
-  // LB = max over groups g outside S of cost(v,{g}) (level-1 slice).
-  int32_t ub;
-  int64_t base1;               // level-1 slice (== 0)
+  long long* stats;
+  const SolveParams* params;
+  cudaGraphConditionalHandle cond;  // while-loop handle when captured
+  int32_t use_cond;
 };
 
 // Launchers (dpbf_kernels.cu). All asynchronous on `stream`.
-cudaError_t launch_group_masks(const int32_t* group_ptr, const int32_t* members, int32_t k, int32_t nmembers,
-                               uint32_t* gmask, cudaStream_t stream);
+cudaError_t launch_group_masks(const int32_t* group_ptr, const int32_t* members, int32_t k, uint32_t* gmask,
+                               cudaStream_t stream);
 cudaError_t launch_merge(const GraphDev& g, const LevelArgs& a, cudaStream_t stream);
 cudaError_t launch_grow_round(const GraphDev& g, const LevelArgs& a, int num_sms, cudaStream_t stream);
-cudaError_t launch_argmin(const GraphDev& g, const int32_t* full_slice, Counters* ctr, cudaStream_t stream);
+cudaError_t launch_argmin(const GraphDev& g, const int32_t* full_slice, int32_t stride, Counters* ctr,
+                          cudaStream_t stream);
 cudaError_t launch_backtrack(const GraphDev& g, int64_t nnz, const int32_t* par, const MaskInfo* minfo,
                              int32_t full, Counters* ctr, int2* qa, int2* qb, int32_t* out_v, int3* out_e,
                              int32_t cap, cudaStream_t stream);

@@ -1,14 +1,14 @@
 // DPBF kernels for sm_103a: group masks, merge, growth round, argmin and
 // backtrack. Plain SIMT integer code: the DP is min-plus over int32 costs
-// and is bound by HBM traffic (growth) and the INT32 pipe (merge); nothing
-// here is a contraction, so no tensor-core path applies.
+// and is bound by memory traffic and latency (growth) and the INT32 pipe
+// (merge); nothing here is a contraction, so no tensor-core path applies.
 //
 // What each kernel replaces in the reference (src/DPQ.cu):
 //   k_group_masks   set_max_ID / get_max (:22-47) — groups(v) as a bit mask
 //   k_merge         the merge half of Relax (:286-314) and the seeding of
 //                   T(v,p)=0 for p inside groups(v) (:638-659), done as one
 //                   pass per DP wave over every vertex's submask splits
-//   k_grow          dis0_init (:404-433) and the grow half of Relax
+//   k_grow_*        dis0_init (:404-433) and the grow half of Relax
 //                   (:259-282): one label-correcting round, pull form
 //   k_argmin        host min scan over T(v,full) (:712-721)
 //   k_backtrack     host BFS over parent records (:729-758)
@@ -26,27 +26,40 @@ __device__ __forceinline__ long long warp_sum_ll(long long x) {
   return x;
 }
 
-__device__ __forceinline__ void flush_stat(long long* stats, int slot, long long x) {
-  x = warp_sum_ll(x);
-  if ((threadIdx.x & 31) == 0 && x != 0) atomicAdd(reinterpret_cast<unsigned long long*>(stats + slot),
-                                                   static_cast<unsigned long long>(x));
+// Sums N per-thread counters over the block; the totals land in thread 0.
+// Every thread of the block must call it.
+template <int N>
+__device__ __forceinline__ void block_sum(long long (&v)[N]) {
+  __shared__ long long part[kGrowThreads / 32][N];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int i = 0; i < N; ++i) v[i] = warp_sum_ll(v[i]);
+  if (lane == 0) {
+#pragma unroll
+    for (int i = 0; i < N; ++i) part[warp][i] = v[i];
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
+#pragma unroll
+      for (int i = 0; i < N; ++i) v[i] += part[w][i];
+    }
+  }
 }
 
-__device__ __forceinline__ void flush_count(int32_t* dst, int x) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-  if ((threadIdx.x & 31) == 0 && x != 0) atomicAdd(dst, x);
+__device__ __forceinline__ void add_stat(long long* stats, int slot, long long x) {
+  if (x) atomicAdd(reinterpret_cast<unsigned long long*>(stats + slot), static_cast<unsigned long long>(x));
 }
 
 // Largest cost allowed for state (v,S) under the bound: ub - LB(v, full^S)
 // with LB = max over groups g outside S of T(v,{g}) (one-label bound,
 // src/DPQ.cu:361-403, applied per remaining group set). -1 = state dead.
-__device__ __forceinline__ int32_t prune_cap(const LevelArgs& a, int32_t v, uint32_t S) {
-  const int32_t* d = a.cost + a.base1 + (int64_t)v * a.k;
+__device__ __forceinline__ int32_t prune_cap(const LevelArgs& a, int32_t ub, int32_t v, uint32_t S) {
+  const int32_t* d = a.cost + (int64_t)v * a.stride1;  // wave 1 slice starts at 0; rank({g}) = g
   int32_t lb = 0;
   for (int g = 0; g < a.k; ++g)
     if (!((S >> g) & 1u)) lb = max(lb, __ldg(d + g));
-  const int32_t cap = a.ub - lb;
+  const int32_t cap = ub - lb;
   return cap < 0 ? -1 : cap;
 }
 
@@ -54,55 +67,58 @@ __device__ __forceinline__ int32_t prune_cap(const LevelArgs& a, int32_t v, uint
 
 // ------------------------------------------------------------ group masks --
 __global__ void k_group_masks(const int32_t* __restrict__ group_ptr, const int32_t* __restrict__ members,
-                              int32_t k, int32_t n, uint32_t* __restrict__ gmask) {
-  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  int32_t g = 0;
-  while (g + 1 < k && group_ptr[g + 1] <= i) ++g;
-  atomicOr(gmask + members[i], 1u << g);
+                              int32_t k, uint32_t* __restrict__ gmask) {
+  const int32_t n = group_ptr[k];
+  for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    int32_t g = 0;
+    while (g + 1 < k && group_ptr[g + 1] <= i) ++g;
+    atomicOr(gmask + members[i], 1u << g);
+  }
 }
 
 // ------------------------------------------------------------------ merge --
-// One thread per (v, S) of the level: T(v,S) = 0 when S is inside groups(v),
-// else the best split T(v,S1) + T(v,S^S1) over S1 holding the lowest bit of
-// S (each unordered split once). Writes every entry of the level slice and
-// marks vertices with a finite entry as the first growth frontier.
+// One thread per (v, slot) of the level's rows: T(v,S) = 0 when S is inside
+// groups(v), else the best split T(v,S1) + T(v,S^S1) over S1 holding the
+// lowest bit of S (each unordered split once); padding slots get kInf.
+// Writes every entry of the level slice, marks vertices with a finite entry
+// as changed in "round -1" (flag array 2, count slot 2) and makes round 0 a
+// full sweep.
 __global__ void __launch_bounds__(kGrowThreads) k_merge(GraphDev g, LevelArgs a) {
-  const int64_t total = (int64_t)g.V * a.m;
+  const int64_t total = (int64_t)g.V * a.stride;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  int finite = 0, overflow = 0;
-  long long splits = 0;
+  const int32_t ub = (a.level >= 2) ? a.params->ub : 0;
+  const int32_t ovf_limit = a.params->ovf_limit;
+  uint8_t* flag2 = a.flags + 2 * (int64_t)g.V;
+  long long acc[3] = {0, 0, 0};  // finite states, splits, overflow
   for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += stride) {
-    const int32_t v = (int32_t)(idx / a.m);
-    const int32_t j = (int32_t)(idx - (int64_t)v * a.m);
-    const uint32_t S = (uint32_t)__ldg(a.lmasks + j);
-    int32_t best = ((__ldg(a.gmask + v) & S) == S) ? 0 : kInf;
+    const int32_t v = (int32_t)(idx / a.stride);
+    const int32_t j = (int32_t)(idx - (int64_t)v * a.stride);
+    int32_t best = kInf;
     int32_t code = kLeaf;
-    if (a.level >= 2 && best != 0) {
-      const uint32_t low = S & (0u - S), rest = S ^ low;
-      for (uint32_t sub = (rest - 1u) & rest;; sub = (sub - 1u) & rest) {
-        const uint32_t s1 = sub | low, s2 = S ^ s1;
-        const MaskInfo i1 = a.minfo[s1], i2 = a.minfo[s2];
-        const int32_t c1 = a.cost[(int64_t)i1.base * g.V + (int64_t)v * i1.m + i1.rank];
-        const int32_t c2 = a.cost[(int64_t)i2.base * g.V + (int64_t)v * i2.m + i2.rank];
-        const int32_t c = c1 + c2;  // both <= kInf < 2^30: no wrap
-        if (c < best) {
-          if (c >= kInf) {
-            overflow = 1;
-          } else {
-            best = c;
-            code = -(int32_t)s1;
+    if (j < a.m) {
+      const uint32_t S = (uint32_t)__ldg(a.lmasks + j);
+      if ((__ldg(a.gmask + v) & S) == S) best = 0;
+      if (a.level >= 2 && best != 0) {
+        const uint32_t low = S & (0u - S), rest = S ^ low;
+        for (uint32_t sub = (rest - 1u) & rest;; sub = (sub - 1u) & rest) {
+          const uint32_t s1 = sub | low, s2 = S ^ s1;
+          const MaskInfo i1 = a.minfo[s1], i2 = a.minfo[s2];
+          const int32_t c1 = a.cost[(int64_t)i1.base * g.V + (int64_t)v * i1.stride + i1.rank];
+          const int32_t c2 = a.cost[(int64_t)i2.base * g.V + (int64_t)v * i2.stride + i2.rank];
+          const int32_t c = c1 + c2;  // both <= kInf < 2^30: no wrap
+          if (c1 < kInf && c2 < kInf) {
+            if (c >= ovf_limit)
+              acc[2] = 1;
+            else if (c < best) {
+              best = c;
+              code = -(int32_t)s1;
+            }
           }
-        } else if (c >= kInf && c1 < kInf && c2 < kInf) {
-          overflow = 1;
+          ++acc[1];
+          if (sub == 0u) break;
         }
-        ++splits;
-        if (sub == 0u) break;
       }
-    }
-    if (a.ub > 0 && best < kInf && a.level >= 2) {
-      const int32_t cap = prune_cap(a, v, S);
-      if (best > cap) {
+      if (ub > 0 && best < kInf && a.level >= 2 && best > prune_cap(a, ub, v, S)) {
         best = kInf;
         code = kLeaf;
       }
@@ -110,261 +126,539 @@ __global__ void __launch_bounds__(kGrowThreads) k_merge(GraphDev g, LevelArgs a)
     a.cost[a.base + idx] = best;
     a.par[a.base + idx] = code;
     if (best < kInf) {
-      a.next_flag[v] = 1;
-      ++finite;
+      flag2[v] = 1;
+      ++acc[0];
     }
   }
-  flush_count(a.cur_changed, finite);
-  if (a.stats) {
-    flush_stat(a.stats, kStatSplits, splits);
-  }
-  if (overflow) atomicExch(&a.ctr->overflow, 1);
-  {
-    long long f = warp_sum_ll(finite);
-    if ((threadIdx.x & 31) == 0 && f) atomicAdd(&a.ctr->states, (unsigned long long)f);
+  block_sum(acc);
+  if (threadIdx.x == 0) {
+    if (acc[0]) {
+      atomicAdd(&a.ctl->changed[2], (int32_t)acc[0]);
+      atomicAdd(&a.ctr->states, (unsigned long long)acc[0]);
+    }
+    if (a.params->stats_on) add_stat(a.stats, kStatSplits, acc[1]);
+    if (acc[2]) atomicExch(&a.ctr->overflow, 1);
+    if (blockIdx.x == 0) a.ctl->dense[2] = 1;  // round 0 sweeps every vertex
   }
 }
 
 // ------------------------------------------------------------------- grow --
 // One label-correcting round for every mask of the level, pull form: each
-// vertex u takes min over neighbours v changed in the previous round of
-// T(v,S) + w(u,v), for all masks S of the level at once (the m entries of a
-// row are contiguous). Only u writes u's entries, so a state's cost and its
-// parent are always written together by one thread (the reference writes
-// the parent after a separate atomicMin, DPQ.cu:269-272).
+// candidate vertex u takes min over neighbours v changed in the previous
+// round of T(v,S) + w(u,v), for all masks S of the level at once (a row is
+// contiguous). Only u's thread(s) write u's row, so a state's cost and its
+// parent are always written together (the reference writes the parent after
+// a separate atomicMin, DPQ.cu:269-272).
 //
-// Rows with degree <= kDegBig: a group of G lanes per vertex; lanes load G
-// CSR entries at once, then broadcast each changed neighbour and gather its
-// row (lane j holds masks j, j+G, ...). Rows with degree > kDegBig: one CTA
-// per vertex (blocks [0, nbig)), partial minima combined in shared memory.
-template <int G, int MPL>
-__global__ void __launch_bounds__(kGrowThreads) k_grow(GraphDev g, LevelArgs a) {
-  if (*a.prev_changed == 0) {
-    // converged: keep the rotation consistent so later rounds also see 0
-    if (blockIdx.x == 0 && threadIdx.x == 0) *a.zero_changed = 0;
-    return;
-  }
-  const int tid = threadIdx.x;
-  const int lane = tid & 31;
-  const int glane = lane & (G - 1);
-  const int gbase = lane & ~(G - 1);
-  const unsigned gmask_lanes = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << gbase);
-  const unsigned gbits = (G == 32) ? 0xffffffffu : ((1u << G) - 1u);
-  const int m = a.m;
-  constexpr int CH = G * MPL;  // masks per pass
-  const bool prune = a.ub > 0;
-  const bool stats = a.stats != nullptr;
-  long long st_vert = 0, st_ent = 0, st_rows = 0, st_imp = 0;
-  int changed = 0, overflow = 0;
+// Sparse rounds: an improved vertex marks its neighbours as the next round's
+// candidates and only candidates are processed. Dense rounds (the previous
+// round changed more than V/8 vertices): every vertex is processed, every
+// neighbour row is gathered without consulting the change flags, and no
+// candidates are marked (the next round then sweeps every vertex).
+//
+// Mappings:
+//   k_grow_thread<MP>  waves with row stride MP <= 24: one thread per
+//                      vertex holds its whole row in registers and gathers
+//                      U neighbour rows at a time with int4 loads;
+//   k_grow_group<G,L>  wider waves: G lanes per vertex, lane j holding masks
+//                      j, j+G, ... (L per lane), neighbour rows gathered four
+//                      at a time;
+//   hubs (degree > kDegBig) in both: 32-entry chunks of hub rows taken by
+//                      any warp, minima folded into a per-hub scratch row,
+//                      applied by the warp that finishes the hub's last chunk.
+// The last block to finish publishes the round's change count, advances
+// the round and, inside a captured CUDA graph, sets the while condition.
+namespace {
 
-  if ((int)blockIdx.x < g.nbig) {
-    // ---------------------------------------------- one CTA, one big row --
-    __shared__ unsigned long long red[CH];
-    __shared__ int32_t cap_s[CH];
-    __shared__ int any_imp;
-    constexpr int NG = kGrowThreads / G;
-    const int gi = tid / G;
-    const int32_t u = g.big[blockIdx.x];
-    const int32_t beg = g.row_ptr[u], end = g.row_ptr[u + 1];
-    const int64_t rowu = a.base + (int64_t)u * m;
-    if (tid == 0) any_imp = 0;
-    for (int jc = 0; jc < m; jc += CH) {
-      __syncthreads();
-      if (tid < CH) {
-        const int j = jc + tid;
-        const int32_t own = (j < m) ? a.cost[rowu + j] : -1;
-        red[tid] = ((unsigned long long)(uint32_t)own << 32) | 0xffffffffull;
-        int32_t cap = kInf - 1;
-        if (j < m && prune) cap = prune_cap(a, u, (uint32_t)__ldg(a.lmasks + j));
-        cap_s[tid] = (j < m) ? cap : -1;
-      }
-      __syncthreads();
-      int32_t best[MPL], code[MPL], capl[MPL];
+constexpr int kGatherUnroll = 4;
+
+struct RoundState {
+  int32_t r;
+  bool dense, all_cand, stats;
+  int32_t ub;
+  int32_t ovf_limit;  // stored costs must stay below this (kInf - largest weight)
+  const uint8_t* cur_flag;
+  uint8_t* next_flag;
+  uint8_t* clear_flag;
+  const uint8_t* cand_cur;
+  uint8_t* cand_next;
+  uint8_t* cand_clear;
+};
+
+// Per-thread counters: changed rows, improved entries, vertices, CSR
+// entries, rows gathered, candidate marks, overflow.
+enum { kAccChanged, kAccImproved, kAccVert, kAccEnt, kAccRows, kAccMarks, kAccOverflow, kAccN };
+
+__device__ __forceinline__ bool round_begin(const GraphDev& g, const LevelArgs& a, RoundState& rs) {
+  const GrowCtl* ctl = a.ctl;
+  rs.r = ctl->round;
+  const int32_t prev = ctl->changed[(rs.r + 2) % 3];
+  if (prev == 0) {  // nothing changed in the previous round: converged
+    if (a.use_cond && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(a.cond, 0);
+    return false;
+  }
+  rs.dense = prev > (g.V >> 1);
+  rs.all_cand = rs.dense || ctl->dense[(rs.r + 2) % 3] != 0;
+  rs.stats = a.params->stats_on != 0;
+  rs.ub = a.level >= 2 ? a.params->ub : 0;  // wave 1 is the bound's own input: never pruned
+  rs.ovf_limit = a.params->ovf_limit;
+  const int64_t V = g.V;
+  rs.cur_flag = a.flags + (int64_t)((rs.r + 2) % 3) * V;
+  rs.next_flag = a.flags + (int64_t)(rs.r % 3) * V;
+  rs.clear_flag = a.flags + (int64_t)((rs.r + 1) % 3) * V;
+  rs.cand_cur = a.cand + (int64_t)(rs.r % 3) * V;
+  rs.cand_next = a.cand + (int64_t)((rs.r + 1) % 3) * V;
+  rs.cand_clear = a.cand + (int64_t)((rs.r + 2) % 3) * V;
+  return true;
+}
+
+// Block-level accumulators of a growth round: every warp folds its counters
+// in and the last warp of the block to arrive publishes them, so no warp of
+// the block waits at a barrier for the slowest one.
+struct BlockAcc {
+  unsigned long long v[kAccN];
+  unsigned int warps_done;
+};
+
+__device__ __forceinline__ void block_acc_init(BlockAcc& ba) {
+  if (threadIdx.x < kAccN) ba.v[threadIdx.x] = 0ull;
+  if (threadIdx.x == 0) ba.warps_done = 0u;
+  __syncthreads();
+}
+
+__device__ __forceinline__ void round_end(const LevelArgs& a, const RoundState& rs, long long (&acc)[kAccN],
+                                          BlockAcc& ba) {
+  const int lane = threadIdx.x & 31;
 #pragma unroll
-      for (int t = 0; t < MPL; ++t) {
+  for (int i = 0; i < kAccN; ++i) acc[i] = warp_sum_ll(acc[i]);
+  int last = 0;
+  if (lane == 0) {
+#pragma unroll
+    for (int i = 0; i < kAccN; ++i)
+      if (acc[i]) atomicAdd(&ba.v[i], (unsigned long long)acc[i]);
+    __threadfence_block();
+    last = atomicAdd(&ba.warps_done, 1u) == (blockDim.x >> 5) - 1;
+  }
+  if (!last) return;
+  __threadfence_block();
+#pragma unroll
+  for (int i = 0; i < kAccN; ++i) acc[i] = (long long)atomicAdd(&ba.v[i], 0ull);
+  GrowCtl* ctl = a.ctl;
+  if (acc[kAccChanged]) atomicAdd(&ctl->changed[rs.r % 3], (int32_t)acc[kAccChanged]);
+  if (acc[kAccImproved]) atomicAdd(&a.ctr->states, (unsigned long long)acc[kAccImproved]);
+  if (acc[kAccOverflow]) atomicExch(&a.ctr->overflow, 1);
+  if (rs.stats) {
+    const long long m = a.m, s = a.stride;
+    add_stat(a.stats, kStatVertices, acc[kAccVert]);
+    add_stat(a.stats, kStatEntries, acc[kAccEnt]);
+    add_stat(a.stats, kStatRows, acc[kAccRows]);
+    add_stat(a.stats, kStatGathered, acc[kAccRows] * m);
+    add_stat(a.stats, kStatImproved, acc[kAccImproved]);
+    // algorithmic bytes: per processed vertex the row_ptr pair, its own row
+    // and its candidate byte; per CSR entry scanned (col,w) and, in sparse
+    // rounds, the change flag; one neighbour row per gather; the parent per
+    // improved entry, the row rewritten and a change flag per changed row;
+    // (col,w) + a candidate byte per mark
+    const long long flag_bytes = rs.dense ? 0 : 1;
+    add_stat(a.stats, kStatBytes,
+             acc[kAccVert] * (9 + 4 * s) + acc[kAccEnt] * (8 + flag_bytes) + acc[kAccRows] * 4 * s +
+                 acc[kAccImproved] * 4 + acc[kAccChanged] * (4 * s + 1) + acc[kAccMarks] * 9);
+  }
+  __threadfence();
+  const uint32_t t = atomicAdd(&ctl->done, 1u);
+  if (t != gridDim.x - 1) return;
+  // last block of the round
+  __threadfence();
+  const int32_t total = atomicAdd(&ctl->changed[rs.r % 3], 0);
+  ctl->dense[rs.r % 3] = rs.dense ? 1 : 0;
+  ctl->last_changed = total;
+  ctl->changed[(rs.r + 1) % 3] = 0;
+  ctl->done = 0u;
+  ctl->round = rs.r + 1;
+  atomicAdd(&a.ctr->rounds_total, 1);
+  if (rs.stats) add_stat(a.stats, kStatRounds, 1);
+  const bool more = total > 0 && rs.r + 1 < a.params->max_rounds;
+  if (total > 0 && !more) {
+    ctl->timeout = 1;
+    a.ctr->timeout = 1;
+  }
+  if (a.use_cond) cudaGraphSetConditional(a.cond, more ? 1u : 0u);
+}
+
+// Relaxes a group's running minima against CSR entries [e0, e0 + G) of the
+// current row (mask chunk jc).
+template <int G, int L>
+__device__ __forceinline__ void group_relax(const GraphDev& g, const LevelArgs& a, const RoundState& rs, int32_t e0,
+                                            int32_t end, int jc, int glane, int gbase, unsigned gmask_lanes,
+                                            unsigned gbits, int32_t (&best)[L], int32_t (&code)[L],
+                                            long long (&acc)[kAccN]) {
+  const int32_t e = e0 + glane;
+  int32_t nv = 0, nw = 0;
+  bool act = false;
+  if (e < end) {
+    const int2 x = g.adj[e];
+    nv = x.x;
+    nw = x.y;
+    act = rs.dense || rs.cur_flag[nv] != 0;
+  }
+  unsigned bal = (__ballot_sync(gmask_lanes, act) >> gbase) & gbits;
+  if (glane == 0) acc[kAccRows] += __popc(bal);
+  const int32_t s = a.stride;
+  while (bal) {
+    int src[kGatherUnroll];
+#pragma unroll
+    for (int i = 0; i < kGatherUnroll; ++i) {
+      src[i] = bal ? __ffs(bal) - 1 : -1;
+      bal &= bal - 1u;
+    }
+    int32_t vv[kGatherUnroll], ww[kGatherUnroll];
+#pragma unroll
+    for (int i = 0; i < kGatherUnroll; ++i) {
+      const int sl = src[i] < 0 ? 0 : src[i];
+      vv[i] = __shfl_sync(gmask_lanes, nv, sl, G);
+      ww[i] = __shfl_sync(gmask_lanes, nw, sl, G);
+    }
+    int32_t c[kGatherUnroll][L];
+#pragma unroll
+    for (int i = 0; i < kGatherUnroll; ++i) {
+      const int64_t rowv = a.base + (int64_t)vv[i] * s + jc;
+#pragma unroll
+      for (int t = 0; t < L; ++t) {
+        const int j = glane + t * G;
+        c[i][t] = (src[i] >= 0 && jc + j < s) ? a.cost[rowv + j] : kInf;
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < kGatherUnroll; ++i) {
+#pragma unroll
+      for (int t = 0; t < L; ++t) {
+        int32_t x = c[i][t];
+        if (x < kInf) {
+          x += ww[i];  // both < 2^30: no wrap
+          if (x >= rs.ovf_limit)
+            acc[kAccOverflow] = 1;
+          else if (x < best[t]) {
+            best[t] = x;
+            code[t] = e0 + src[i];
+          }
+        }
+      }
+    }
+  }
+}
+
+// Hub rows (degree > kDegBig) are cut into 32-entry chunks that any warp
+// may take. A warp relaxes its chunk for every mask (lane j holds masks
+// j, j+32, ...), folds each lane's minimum into the hub's scratch row with
+// a 64-bit atomicMin of (cost << 32 | CSR entry), and counts the chunk as
+// done; the warp that finishes a hub's last chunk applies the scratch row
+// to the hub's state row (its single writer), clears the scratch row and
+// the counter for the next round, and marks the hub's neighbours. No warp
+// ever waits for another.
+template <int L>
+__device__ __forceinline__ void hub_chunks(const GraphDev& g, const LevelArgs& a, const RoundState& rs,
+                                           long long (&acc)[kAccN]) {
+  constexpr int G = 32;
+  constexpr int CH = G * L;
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int32_t s = a.stride;
+  for (int64_t c = warp; c < g.nchunks; c += nwarps) {
+    const int2 hc = g.hub_chunk[c];  // (hub index, first CSR entry of the chunk)
+    const int32_t u = g.big[hc.x];
+    if (!rs.all_cand && !rs.cand_cur[u]) continue;
+    const int32_t beg = g.row_ptr[u], end = g.row_ptr[u + 1];
+    const int32_t cend = min(end, hc.y + G);
+    unsigned long long* hm = g.hub_min + (int64_t)hc.x * g.hub_stride;
+    for (int jc = 0; jc < s; jc += CH) {
+      int32_t best[L], code[L];
+#pragma unroll
+      for (int t = 0; t < L; ++t) {
         best[t] = kInf;
         code[t] = -1;
-        capl[t] = cap_s[glane + t * G];
       }
-      for (int32_t e0 = beg + gi * G; e0 < end; e0 += NG * G) {
-        const int32_t e = e0 + glane;
-        int32_t nv = 0, nw = 0;
-        bool act = false;
-        if (e < end) {
-          const int2 x = g.adj[e];
-          nv = x.x;
-          nw = x.y;
-          act = a.cur_flag[nv] != 0;
-        }
-        unsigned bal = (__ballot_sync(gmask_lanes, act) >> gbase) & gbits;
-        if (stats && glane == 0) st_rows += __popc(bal);
-        while (bal) {
-          const int src = __ffs(bal) - 1;
-          bal &= bal - 1u;
-          const int32_t v = __shfl_sync(gmask_lanes, nv, src, G);
-          const int32_t w = __shfl_sync(gmask_lanes, nw, src, G);
-          const int64_t rowv = a.base + (int64_t)v * m + jc;
+      group_relax<G, L>(g, a, rs, hc.y, cend, jc, lane, 0, 0xffffffffu, 0xffffffffu, best, code, acc);
 #pragma unroll
-          for (int t = 0; t < MPL; ++t) {
-            const int j = glane + t * G;
-            if (jc + j < m) {
-              int32_t c = a.cost[rowv + j];
-              if (c < kInf) {
-                c += w;
-                if (c >= kInf) overflow = 1;
-                if (c < best[t] && c <= capl[t]) {
-                  best[t] = c;
-                  code[t] = e0 + src;
-                }
-              }
-            }
-          }
-        }
-      }
-#pragma unroll
-      for (int t = 0; t < MPL; ++t) {
-        const int j = glane + t * G;
-        if (jc + j < m && best[t] < kInf)
-          atomicMin(&red[j], ((unsigned long long)(uint32_t)best[t] << 32) | (uint32_t)code[t]);
-      }
-      __syncthreads();
-      if (tid < CH && jc + tid < m) {
-        const unsigned long long r = red[tid];
-        const int32_t c = (int32_t)(r >> 32);
-        const int32_t own = a.cost[rowu + jc + tid];
-        if (c < own) {
-          a.cost[rowu + jc + tid] = c;
-          a.par[rowu + jc + tid] = (int32_t)(uint32_t)(r & 0xffffffffull);
-          any_imp = 1;
-          ++st_imp;
-        }
+      for (int t = 0; t < L; ++t) {
+        const int j = jc + lane + t * G;
+        if (j < s && best[t] < kInf)
+          atomicMin(hm + j, ((unsigned long long)(uint32_t)best[t] << 32) | (uint32_t)code[t]);
       }
     }
-    __syncthreads();
-    if (tid == 0) {
-      st_vert = 1;
-      st_ent = end - beg;
-      if (any_imp) {
-        a.next_flag[u] = 1;
-        changed = 1;
-      }
+    if (lane == 0) acc[kAccEnt] += cend - hc.y;
+    __threadfence();
+    int last = 0;
+    if (lane == 0) last = atomicAdd(g.hub_cnt + hc.x, 1) == (end - beg + G - 1) / G - 1;
+    last = __shfl_sync(0xffffffffu, last, 0);
+    if (!last) continue;
+    __threadfence();
+    const int64_t rowu = a.base + (int64_t)u * s;
+    bool imp = false;
+    for (int j = lane; j < s; j += G) {
+      const unsigned long long r = atomicExch(hm + j, ~0ull);  // read and clear
+      if (j >= a.m || r == ~0ull) continue;
+      const int32_t c2 = (int32_t)(r >> 32);
+      const int32_t own = a.cost[rowu + j];
+      if (c2 >= own) continue;
+      if (rs.ub > 0 && c2 > prune_cap(a, rs.ub, u, (uint32_t)__ldg(a.lmasks + j))) continue;
+      a.cost[rowu + j] = c2;
+      a.par[rowu + j] = (int32_t)(uint32_t)(r & 0xffffffffull);
+      imp = true;
+      ++acc[kAccImproved];
     }
-  } else {
-    // ------------------------------------------- groups over small rows --
-    const int32_t sblock = blockIdx.x - g.nbig;
-    const int32_t nsblocks = gridDim.x - g.nbig;
-    const int64_t sthread = (int64_t)sblock * blockDim.x + tid;
-    const int64_t nsthreads = (int64_t)nsblocks * blockDim.x;
-    for (int64_t i = sthread; i < g.V; i += nsthreads) a.clear_flag[i] = 0;
-    if (sthread == 0) {
-      *a.zero_changed = 0;
-      if (stats) atomicAdd(reinterpret_cast<unsigned long long*>(a.stats + kStatRounds), 1ull);
+    if (lane == 0) {
+      atomicExch(g.hub_cnt + hc.x, 0);
+      ++acc[kAccVert];
     }
-    const int64_t ngroups = nsthreads / G;
-    for (int64_t uu = sthread / G; uu < g.V; uu += ngroups) {
-      const int32_t u = (int32_t)uu;
-      const int32_t beg = g.row_ptr[u], end = g.row_ptr[u + 1];
-      if (end - beg > kDegBig) continue;
-      const int64_t rowu = a.base + (int64_t)u * m;
-      bool imp_any = false;
-      for (int jc = 0; jc < m; jc += CH) {
-        int32_t own[MPL], best[MPL], code[MPL], capl[MPL];
-        bool live = false;
-#pragma unroll
-        for (int t = 0; t < MPL; ++t) {
-          const int j = jc + glane + t * G;
-          own[t] = (j < m) ? a.cost[rowu + j] : -1;
-          best[t] = own[t];
-          code[t] = -1;
-          capl[t] = (j < m) ? kInf - 1 : -1;
-          if (j < m && prune) capl[t] = prune_cap(a, u, (uint32_t)__ldg(a.lmasks + j));
-          live |= capl[t] >= 0 && own[t] != 0;
+    if (__ballot_sync(0xffffffffu, imp)) {
+      if (!rs.dense) {
+        for (int32_t e = beg + lane; e < end; e += G) {
+          rs.cand_next[g.adj[e].x] = 1;
+          ++acc[kAccMarks];
         }
-        // no lane can improve: skip the row scan
-        if (!(__ballot_sync(gmask_lanes, live) & gmask_lanes)) continue;
-        for (int32_t e0 = beg; e0 < end; e0 += G) {
-          const int32_t e = e0 + glane;
-          int32_t nv = 0, nw = 0;
-          bool act = false;
-          if (e < end) {
-            const int2 x = g.adj[e];
-            nv = x.x;
-            nw = x.y;
-            act = a.cur_flag[nv] != 0;
-          }
-          unsigned bal = (__ballot_sync(gmask_lanes, act) >> gbase) & gbits;
-          if (stats && glane == 0) st_rows += __popc(bal);
-          while (bal) {
-            const int src = __ffs(bal) - 1;
-            bal &= bal - 1u;
-            const int32_t v = __shfl_sync(gmask_lanes, nv, src, G);
-            const int32_t w = __shfl_sync(gmask_lanes, nw, src, G);
-            const int64_t rowv = a.base + (int64_t)v * m + jc;
-#pragma unroll
-            for (int t = 0; t < MPL; ++t) {
-              const int j = glane + t * G;
-              if (jc + j < m) {
-                int32_t c = a.cost[rowv + j];
-                if (c < kInf) {
-                  c += w;
-                  if (c >= kInf) overflow = 1;
-                  if (c < best[t] && c <= capl[t]) {
-                    best[t] = c;
-                    code[t] = e0 + src;
-                  }
-                }
-              }
-            }
-          }
-        }
-        bool imp = false;
-#pragma unroll
-        for (int t = 0; t < MPL; ++t) {
-          const int j = jc + glane + t * G;
-          if (j < m && best[t] < own[t]) {
-            a.cost[rowu + j] = best[t];
-            a.par[rowu + j] = code[t];
-            imp = true;
-            ++st_imp;
-          }
-        }
-        imp_any |= (__ballot_sync(gmask_lanes, imp) & gmask_lanes) != 0;
       }
-      if (glane == 0) {
-        st_vert += 1;
-        st_ent += end - beg;
-        if (imp_any) {
-          a.next_flag[u] = 1;
-          ++changed;
-        }
+      if (lane == 0) {
+        rs.next_flag[u] = 1;
+        ++acc[kAccChanged];
       }
     }
   }
-  flush_count(a.cur_changed, changed);
-  if (stats) {
-    flush_stat(a.stats, kStatVertices, st_vert);
-    flush_stat(a.stats, kStatEntries, st_ent);
-    flush_stat(a.stats, kStatRows, st_rows);
-    flush_stat(a.stats, kStatGathered, st_rows * m);
-    flush_stat(a.stats, kStatImproved, st_imp);
-    // algorithmic bytes: row_ptr pair + own row per scanned vertex, (col,w)
-    // + frontier byte per scanned entry, one m-entry row per changed
-    // neighbour, cost + parent per improved entry, one flag per changed row
-    flush_stat(a.stats, kStatBytes,
-               st_vert * (8 + 4LL * m) + st_ent * 9 + st_rows * 4LL * m + st_imp * 8 + changed);
+}
+
+}  // namespace
+
+// Thread per vertex: the vertex's MP-entry row lives in registers.
+template <int MP>
+__global__ void __launch_bounds__(kGrowThreads, (MP <= 16 ? 3 : 2)) k_grow_thread(GraphDev g, LevelArgs a) {
+  RoundState rs;
+  if (!round_begin(g, a, rs)) return;
+  __shared__ BlockAcc ba;
+  block_acc_init(ba);
+  long long acc[kAccN] = {0, 0, 0, 0, 0, 0, 0};
+  constexpr int U = MP <= 8 ? 4 : 2;
+  constexpr int Q = MP / 4;
+  const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = t0; i < g.V; i += nthreads) {
+    rs.clear_flag[i] = 0;
+    rs.cand_clear[i] = 0;
   }
+  hub_chunks<(MP + 31) / 32>(g, a, rs, acc);
   {
-    long long imp = warp_sum_ll(st_imp);
-    if (lane == 0 && imp) atomicAdd(&a.ctr->states, (unsigned long long)imp);
+    // vertices by decreasing degree: a warp's lanes walk rows of similar
+    // length, and the longest rows start first
+    // odd rounds sweep backwards: in-place updates then also carry along
+    // the order in the other direction within one round
+    for (int64_t i = t0; i < g.nsmall; i += nthreads) {
+      const int32_t u = g.order[(rs.r & 1) ? g.nsmall - 1 - i : i];
+      if (!rs.all_cand && !rs.cand_cur[u]) continue;
+      const int32_t beg = g.row_ptr[u], end = g.row_ptr[u + 1];
+      int4* rowc = reinterpret_cast<int4*>(a.cost + a.base + (int64_t)u * MP);
+      int32_t best[MP];
+      // parent of entry j as (CSR entry - beg), one byte each (rows are at
+      // most kDegBig long); 0xff = unchanged
+      uint32_t code[Q];
+#pragma unroll
+      for (int q = 0; q < Q; ++q) {
+        const int4 x = rowc[q];
+        best[4 * q] = x.x;
+        best[4 * q + 1] = x.y;
+        best[4 * q + 2] = x.z;
+        best[4 * q + 3] = x.w;
+        code[q] = 0xffffffffu;
+      }
+      bool live = false;
+#pragma unroll
+      for (int j = 0; j < MP; ++j) live |= j < a.m && best[j] != 0;  // cost-0 states cannot improve
+      ++acc[kAccVert];
+      acc[kAccEnt] += end - beg;
+      if (!live) continue;
+      for (int32_t e0 = beg; e0 < end; e0 += U) {
+        int32_t nv[U], nw[U];
+        bool act[U];
+#pragma unroll
+        for (int i = 0; i < U; ++i) {
+          act[i] = e0 + i < end;
+          nv[i] = 0;
+          nw[i] = 0;
+          if (act[i]) {
+            const int2 x = g.adj[e0 + i];
+            nv[i] = x.x;
+            nw[i] = x.y;
+          }
+        }
+        if (!rs.dense) {
+#pragma unroll
+          for (int i = 0; i < U; ++i) act[i] = act[i] && rs.cur_flag[nv[i]] != 0;
+        }
+        int32_t rows[U][MP];
+#pragma unroll
+        for (int i = 0; i < U; ++i) {
+          if (act[i]) {
+            ++acc[kAccRows];
+            const int4* rv = reinterpret_cast<const int4*>(a.cost + a.base + (int64_t)nv[i] * MP);
+#pragma unroll
+            for (int q = 0; q < Q; ++q) {
+              const int4 x = rv[q];
+              rows[i][4 * q] = x.x;
+              rows[i][4 * q + 1] = x.y;
+              rows[i][4 * q + 2] = x.z;
+              rows[i][4 * q + 3] = x.w;
+            }
+          } else {
+#pragma unroll
+            for (int j = 0; j < MP; ++j) rows[i][j] = kInf;
+          }
+        }
+        // a kInf row entry gives c >= kInf and never wins; rows hold values
+        // below ovf_limit (checked when stored), so c cannot wrap or reach
+        // kInf from a finite entry
+#pragma unroll
+        for (int i = 0; i < U; ++i) {
+          const uint32_t rel = (uint32_t)(e0 + i - beg);
+#pragma unroll
+          for (int j = 0; j < MP; ++j) {
+            const int32_t c = rows[i][j] + nw[i];
+            const bool lt = c < best[j];
+            best[j] = lt ? c : best[j];
+            const int sh = 8 * (j & 3);
+            code[j >> 2] = lt ? ((code[j >> 2] & ~(0xffu << sh)) | (rel << sh)) : code[j >> 2];
+          }
+        }
+      }
+      bool any = false;
+#pragma unroll
+      for (int j = 0; j < MP; ++j) {
+        const int sh = 8 * (j & 3);
+        const bool imp = ((code[j >> 2] >> sh) & 0xffu) != 0xffu;
+        if (imp && best[j] >= rs.ovf_limit) acc[kAccOverflow] = 1;
+        if (imp && rs.ub > 0 && best[j] > prune_cap(a, rs.ub, u, (uint32_t)__ldg(a.lmasks + j))) {
+          best[j] = a.cost[a.base + (int64_t)u * MP + j];  // keep the stored value
+          code[j >> 2] |= 0xffu << sh;
+        }
+        any |= ((code[j >> 2] >> sh) & 0xffu) != 0xffu;
+      }
+      if (!any) continue;
+#pragma unroll
+      for (int q = 0; q < Q; ++q) rowc[q] = make_int4(best[4 * q], best[4 * q + 1], best[4 * q + 2], best[4 * q + 3]);
+      int32_t* rowp = a.par + a.base + (int64_t)u * MP;
+#pragma unroll
+      for (int j = 0; j < MP; ++j) {
+        const uint32_t rel = (code[j >> 2] >> (8 * (j & 3))) & 0xffu;
+        if (rel != 0xffu) {
+          rowp[j] = beg + (int32_t)rel;
+          ++acc[kAccImproved];
+        }
+      }
+      rs.next_flag[u] = 1;
+      ++acc[kAccChanged];
+      if (!rs.dense) {
+        for (int32_t e = beg; e < end; ++e) {
+          rs.cand_next[g.adj[e].x] = 1;
+          ++acc[kAccMarks];
+        }
+      }
+    }
   }
-  if (overflow) atomicExch(&a.ctr->overflow, 1);
+  round_end(a, rs, acc, ba);
+}
+
+// G lanes per vertex for waves wider than kMaxThreadMasks. Each warp takes
+// 32 consecutive vertices at a time, finds the candidates among them with
+// one ballot, and its 32/G groups take the candidates in turn.
+template <int G, int L>
+__global__ void __launch_bounds__(kGrowThreads, (L >= 3 ? 3 : 4)) k_grow_group(GraphDev g, LevelArgs a) {
+  RoundState rs;
+  if (!round_begin(g, a, rs)) return;
+  __shared__ BlockAcc ba;
+  block_acc_init(ba);
+  long long acc[kAccN] = {0, 0, 0, 0, 0, 0, 0};
+  {
+    const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = t0; i < g.V; i += nthreads) {
+      rs.clear_flag[i] = 0;
+      rs.cand_clear[i] = 0;
+    }
+  }
+  hub_chunks<((G * L + 31) / 32 < 4 ? (G * L + 31) / 32 : 4)>(g, a, rs, acc);
+  {
+    const int tid = threadIdx.x, lane = tid & 31;
+    const int glane = lane & (G - 1), gbase = lane & ~(G - 1);
+    const unsigned gmask_lanes = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << gbase);
+    const unsigned gbits = (G == 32) ? 0xffffffffu : ((1u << G) - 1u);
+    constexpr int CH = G * L;
+    constexpr int NGW = 32 / G;
+    const int gw = lane / G;
+    const int32_t s = a.stride;
+    const int64_t wid = ((int64_t)blockIdx.x * blockDim.x + tid) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t vbase = wid * 32; vbase < g.V; vbase += nwarps * 32) {
+      const int64_t vl = vbase + lane;
+      const bool cnd = vl < g.V && (rs.all_cand || rs.cand_cur[vl] != 0);
+      unsigned cm = __ballot_sync(0xffffffffu, cnd);
+      for (int i = 0; i < gw && cm; ++i) cm &= cm - 1u;
+      while (cm) {
+        const int32_t u = (int32_t)(vbase + __ffs(cm) - 1);
+        for (int i = 0; i < NGW && cm; ++i) cm &= cm - 1u;
+        const int32_t beg = g.row_ptr[u], end = g.row_ptr[u + 1];
+        if (end - beg > kDegBig) continue;  // handled in 32-entry chunks
+        const int64_t rowu = a.base + (int64_t)u * s;
+        bool imp_any = false;
+        for (int jc = 0; jc < s; jc += CH) {
+          int32_t own[L], best[L], code[L];
+          bool live = false;
+#pragma unroll
+          for (int t = 0; t < L; ++t) {
+            const int j = jc + glane + t * G;
+            own[t] = (j < s) ? a.cost[rowu + j] : kInf;
+            best[t] = own[t];
+            code[t] = -1;
+            live |= j < a.m && own[t] != 0;
+          }
+          if (!(__ballot_sync(gmask_lanes, live) & gmask_lanes)) continue;
+          for (int32_t e0 = beg; e0 < end; e0 += G)
+            group_relax<G, L>(g, a, rs, e0, end, jc, glane, gbase, gmask_lanes, gbits, best, code, acc);
+          bool imp = false;
+#pragma unroll
+          for (int t = 0; t < L; ++t) {
+            const int j = jc + glane + t * G;
+            if (j < a.m && best[t] < own[t]) {
+              if (rs.ub > 0 && best[t] > prune_cap(a, rs.ub, u, (uint32_t)__ldg(a.lmasks + j))) continue;
+              a.cost[rowu + j] = best[t];
+              a.par[rowu + j] = code[t];
+              imp = true;
+              ++acc[kAccImproved];
+            }
+          }
+          imp_any |= (__ballot_sync(gmask_lanes, imp) & gmask_lanes) != 0;
+        }
+        if (imp_any && !rs.dense) {
+          for (int32_t e = beg + glane; e < end; e += G) {
+            rs.cand_next[g.adj[e].x] = 1;
+            ++acc[kAccMarks];
+          }
+        }
+        if (glane == 0) {
+          ++acc[kAccVert];
+          acc[kAccEnt] += end - beg;
+          if (imp_any) {
+            rs.next_flag[u] = 1;
+            ++acc[kAccChanged];
+          }
+        }
+      }
+    }
+  }
+  round_end(a, rs, acc, ba);
 }
 
 // ----------------------------------------------------------------- argmin --
-__global__ void k_argmin(int32_t V, const int32_t* __restrict__ full_slice, Counters* ctr) {
+__global__ void k_argmin(int32_t V, const int32_t* __restrict__ full_slice, int32_t stride, Counters* ctr) {
   unsigned long long best = ~0ull;
   for (int32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
-    const int32_t c = full_slice[v];
+    const int32_t c = full_slice[(int64_t)v * stride];
     if (c < kInf) {
       const unsigned long long p = ((unsigned long long)(uint32_t)c << 32) | (uint32_t)v;
       best = p < best ? p : best;
@@ -416,7 +710,7 @@ __global__ void __launch_bounds__(256) k_backtrack(GraphDev g, int64_t nnz, cons
       const int32_t vi = atomicAdd(&ctr->bt_nv, 1);
       if (vi < cap) out_v[vi] = v;
       const MaskInfo mi = minfo[S];
-      const int32_t c = par[(int64_t)mi.base * g.V + (int64_t)v * mi.m + mi.rank];
+      const int32_t c = par[(int64_t)mi.base * g.V + (int64_t)v * mi.stride + mi.rank];
       if (c == kLeaf) continue;
       if (c >= 0) {
         if ((int64_t)c >= nnz || c < g.row_ptr[v] || c >= g.row_ptr[v + 1]) {
@@ -461,15 +755,14 @@ __global__ void __launch_bounds__(256) k_backtrack(GraphDev g, int64_t nnz, cons
 }
 
 // ---------------------------------------------------------------- launchers --
-cudaError_t launch_group_masks(const int32_t* group_ptr, const int32_t* members, int32_t k, int32_t nmembers,
-                               uint32_t* gmask, cudaStream_t stream) {
-  if (nmembers <= 0) return cudaSuccess;
-  k_group_masks<<<(nmembers + 255) / 256, 256, 0, stream>>>(group_ptr, members, k, nmembers, gmask);
+cudaError_t launch_group_masks(const int32_t* group_ptr, const int32_t* members, int32_t k, uint32_t* gmask,
+                               cudaStream_t stream) {
+  k_group_masks<<<64, 256, 0, stream>>>(group_ptr, members, k, gmask);
   return cudaGetLastError();
 }
 
 cudaError_t launch_merge(const GraphDev& g, const LevelArgs& a, cudaStream_t stream) {
-  const int64_t total = (int64_t)g.V * a.m;
+  const int64_t total = (int64_t)g.V * a.stride;
   int64_t blocks = (total + kGrowThreads - 1) / kGrowThreads;
   if (blocks > (1 << 20)) blocks = 1 << 20;
   k_merge<<<(unsigned)blocks, kGrowThreads, 0, stream>>>(g, a);
@@ -477,38 +770,59 @@ cudaError_t launch_merge(const GraphDev& g, const LevelArgs& a, cudaStream_t str
 }
 
 namespace {
-template <int G, int MPL>
-cudaError_t grow_instance(const GraphDev& g, const LevelArgs& a, int num_sms, cudaStream_t stream) {
-  static int occ = 0;  // resident blocks per SM for this instance
-  if (occ == 0) {
-    int o = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_grow<G, MPL>, kGrowThreads, 0) != cudaSuccess || o < 1)
-      o = 4;
-    occ = o;
-  }
-  const int64_t small_blocks_needed = ((int64_t)g.V * G + kGrowThreads - 1) / kGrowThreads;
-  int64_t small_blocks = (int64_t)num_sms * occ;
-  if (small_blocks > small_blocks_needed) small_blocks = small_blocks_needed;
-  if (small_blocks < 1) small_blocks = 1;
-  k_grow<G, MPL><<<(unsigned)(g.nbig + small_blocks), kGrowThreads, 0, stream>>>(g, a);
+template <class Kernel>
+int resident_blocks(Kernel kern) {
+  int o = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kern, kGrowThreads, 0) != cudaSuccess || o < 1) o = 2;
+  return o;
+}
+
+// Every block of a round is resident at once (grid-stride loops inside).
+template <class Kernel>
+cudaError_t launch_round(Kernel kern, int occ, const GraphDev& g, const LevelArgs& a, int num_sms,
+                         int vertices_per_block, cudaStream_t stream) {
+  const int64_t needed = ((int64_t)g.V + vertices_per_block - 1) / vertices_per_block;
+  int64_t blocks = (int64_t)num_sms * occ;
+  if (blocks > needed) blocks = needed;
+  if (blocks < 1) blocks = 1;
+  kern<<<(unsigned)blocks, kGrowThreads, 0, stream>>>(g, a);
   return cudaGetLastError();
+}
+
+template <int MP>
+cudaError_t thread_round(const GraphDev& g, const LevelArgs& a, int num_sms, cudaStream_t stream) {
+  static const int occ = resident_blocks(k_grow_thread<MP>);
+  return launch_round(k_grow_thread<MP>, occ, g, a, num_sms, kGrowThreads, stream);
+}
+
+template <int G, int L>
+cudaError_t group_round(const GraphDev& g, const LevelArgs& a, int num_sms, cudaStream_t stream) {
+  static const int occ = resident_blocks(k_grow_group<G, L>);
+  return launch_round(k_grow_group<G, L>, occ, g, a, num_sms, kGrowThreads / G, stream);
 }
 }  // namespace
 
 cudaError_t launch_grow_round(const GraphDev& g, const LevelArgs& a, int num_sms, cudaStream_t stream) {
-  const int m = a.m;
-  if (m <= 8) return grow_instance<8, 1>(g, a, num_sms, stream);
-  if (m <= 16) return grow_instance<16, 1>(g, a, num_sms, stream);
-  if (m <= 32) return grow_instance<32, 1>(g, a, num_sms, stream);
-  if (m <= 64) return grow_instance<32, 2>(g, a, num_sms, stream);
-  if (m <= 96) return grow_instance<32, 3>(g, a, num_sms, stream);
-  return grow_instance<32, 4>(g, a, num_sms, stream);
+  switch (a.stride) {
+    case 4: return thread_round<4>(g, a, num_sms, stream);
+    case 8: return thread_round<8>(g, a, num_sms, stream);
+    case 12: return thread_round<12>(g, a, num_sms, stream);
+    case 16: return thread_round<16>(g, a, num_sms, stream);
+    case 20: return thread_round<20>(g, a, num_sms, stream);
+    case 24: return thread_round<24>(g, a, num_sms, stream);
+    default: break;
+  }
+  if (a.stride <= 32) return group_round<16, 2>(g, a, num_sms, stream);
+  if (a.stride <= 64) return group_round<32, 2>(g, a, num_sms, stream);
+  if (a.stride <= 96) return group_round<32, 3>(g, a, num_sms, stream);
+  return group_round<32, 4>(g, a, num_sms, stream);
 }
 
-cudaError_t launch_argmin(const GraphDev& g, const int32_t* full_slice, Counters* ctr, cudaStream_t stream) {
+cudaError_t launch_argmin(const GraphDev& g, const int32_t* full_slice, int32_t stride, Counters* ctr,
+                          cudaStream_t stream) {
   int blocks = (g.V + 255) / 256;
   if (blocks > 4096) blocks = 4096;
-  k_argmin<<<blocks, 256, 0, stream>>>(g.V, full_slice, ctr);
+  k_argmin<<<blocks, 256, 0, stream>>>(g.V, full_slice, stride, ctr);
   return cudaGetLastError();
 }
 

@@ -8,17 +8,26 @@
 // min_v T(v,full). The answer is argmin_v T(v,full); the tree is read back
 // from the parent records on the device.
 //
+// Two drivers run the same kernels:
+//   host loop    the host launches growth rounds in batches and polls the
+//                round's change count between batches;
+//   CUDA graph   (gst_opts.use_graph) the whole query is one captured graph,
+//                each wave's growth a conditional while node whose body is
+//                one round; the round's last block sets the condition, so a
+//                query is one graph launch and one host synchronisation.
+// Per-query scalars (bound, round cap, stats switch) live in device memory,
+// so one instantiated graph per k serves every query.
+//
 // Compared with DPBF_GPU (src/DPQ.cu:501-768): no V x 2^k host table and no
 // full-table host<->device copies (DPQ.cu:592,635,661,711), no host-side
-// re-initialisation (DPQ.cu:638-659), no managed memory, and the growth
-// loop polls the device only every few rounds instead of after every
-// launch (DPQ.cu:684-702).
+// re-initialisation (DPQ.cu:638-659), no managed memory, and no host
+// synchronisation after every launch (DPQ.cu:684-702).
 #include <cuda_runtime.h>
 
 #include <algorithm>
-#include <atomic>
 #include <cstdint>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <new>
@@ -63,16 +72,29 @@ int binom(int n, int r) {
   for (int i = 1; i <= r; ++i) c = c * (n - r + i) / i;
   return (int)c;
 }
+
+constexpr int32_t kTreePrefix = 4096;   // tree entries read back with the counters
+constexpr int kPollEvery = 8;           // host loop: rounds launched between polls
+constexpr int kEvents = 3 * GST_MAX_K + 8;
 }  // namespace
 
 // ---------------------------------------------------------------- objects --
+struct QueryGraph {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  uint64_t gen = 0;  // workspace generation it was captured against
+};
+
 struct Workspace {
+  uint64_t gen = 1;           // bumped whenever a captured buffer moves
   int32_t k_cap = 0;          // cost/par sized for this many groups
-  int32_t* cost = nullptr;    // V * (2^k_cap - 1)
+  int32_t* cost = nullptr;    // V * sum of row strides
   int32_t* par = nullptr;
   uint32_t* gmask = nullptr;  // V
-  uint8_t* flags = nullptr;   // 3 * V
+  uint8_t* flags = nullptr;   // 6 * V: change flags x3, candidate flags x3
   Counters* ctr = nullptr;
+  GrowCtl* ctl = nullptr;
+  SolveParams* d_params = nullptr;
   long long* stats = nullptr;
   MaskInfo* minfo = nullptr;  // 2^GST_MAX_K
   int32_t* lmasks = nullptr;  // 2^GST_MAX_K
@@ -85,23 +107,36 @@ struct Workspace {
   int32_t* out_v = nullptr;
   int3* out_e = nullptr;
   int32_t bt_cap = 0;
-  Counters* h_ctr = nullptr;  // pinned
-  int32_t* h_changed = nullptr;
-  cudaEvent_t ev[2 * GST_MAX_K + 4] = {};
-  std::vector<int32_t> h_lvl_base, h_lvl_m;
+  unsigned long long* hub_min = nullptr;  // nbig x hub_stride scratch minima
+  int32_t* hub_cnt = nullptr;             // nbig chunk counters
+  int32_t hub_stride = 0;
+  // pinned host mirrors
+  Counters* h_ctr = nullptr;
+  GrowCtl* h_ctl = nullptr;
+  SolveParams* h_params = nullptr;
+  long long* h_stats = nullptr;
+  int32_t* h_out_v = nullptr;
+  int3* h_out_e = nullptr;
+  cudaEvent_t ev[kEvents] = {};
+  std::vector<int32_t> h_lvl_base, h_lvl_m, h_lvl_stride;
+  QueryGraph qg[GST_MAX_K + 1];
 };
 
 struct gst_graph {
   int device = 0;
   int num_sms = 0;
   cudaStream_t stream = nullptr;
+  cudaStream_t side = nullptr;  // captures conditional bodies
   int32_t V = 0;
   int64_t nnz = 0;
   int32_t* d_row_ptr = nullptr;
   int2* d_adj = nullptr;
   int32_t* d_big = nullptr;
   int32_t nbig = 0;
-  std::vector<int32_t> h_row_ptr;
+  int32_t* d_order = nullptr;  // vertices of degree <= kDegBig, by decreasing degree
+  int2* d_hub_chunk = nullptr;  // (hub index, first CSR entry) per 32-entry chunk of a hub row
+  int64_t nchunks = 0;
+  int32_t max_w = 0;  // largest edge weight
   std::mutex mu;
   Workspace ws;
 };
@@ -127,15 +162,33 @@ GraphDev graph_dev(const gst_graph* g) {
   d.adj = g->d_adj;
   d.big = g->d_big;
   d.nbig = g->nbig;
+  d.order = g->d_order;
+  d.nsmall = g->V - g->nbig;
+  d.hub_chunk = g->d_hub_chunk;
+  d.nchunks = g->nchunks;
+  d.hub_min = g->ws.hub_min;
+  d.hub_cnt = g->ws.hub_cnt;
+  d.hub_stride = g->ws.hub_stride;
   return d;
 }
 
+void drop_graphs(Workspace& ws) {
+  for (auto& q : ws.qg) {
+    if (q.exec) cudaGraphExecDestroy(q.exec);
+    if (q.graph) cudaGraphDestroy(q.graph);
+    q = QueryGraph{};
+  }
+}
+
 void free_workspace(Workspace& ws) {
+  drop_graphs(ws);
   dfree(ws.cost);
   dfree(ws.par);
   dfree(ws.gmask);
   dfree(ws.flags);
   dfree(ws.ctr);
+  dfree(ws.ctl);
+  dfree(ws.d_params);
   dfree(ws.stats);
   dfree(ws.minfo);
   dfree(ws.lmasks);
@@ -145,10 +198,17 @@ void free_workspace(Workspace& ws) {
   dfree(ws.qb);
   dfree(ws.out_v);
   dfree(ws.out_e);
-  if (ws.h_ctr) cudaFreeHost(ws.h_ctr);
-  if (ws.h_changed) cudaFreeHost(ws.h_changed);
+  dfree(ws.hub_min);
+  dfree(ws.hub_cnt);
+  for (void* p : {(void*)ws.h_ctr, (void*)ws.h_ctl, (void*)ws.h_params, (void*)ws.h_stats, (void*)ws.h_out_v,
+                  (void*)ws.h_out_e})
+    if (p) cudaFreeHost(p);
   ws.h_ctr = nullptr;
-  ws.h_changed = nullptr;
+  ws.h_ctl = nullptr;
+  ws.h_params = nullptr;
+  ws.h_stats = nullptr;
+  ws.h_out_v = nullptr;
+  ws.h_out_e = nullptr;
   for (auto& e : ws.ev)
     if (e) {
       cudaEventDestroy(e);
@@ -160,19 +220,32 @@ void free_workspace(Workspace& ws) {
   ws.bt_cap = 0;
 }
 
+// Row strides of every level for k groups; returns their sum.
+int64_t total_stride(int32_t k) {
+  int64_t s = 0;
+  for (int l = 1; l <= k; ++l) s += row_stride(binom(k, l));
+  return s;
+}
+
 // Allocates everything a query with k groups and `nmembers` members needs.
 gst_status ensure_workspace(gst_graph* g, int32_t k, int64_t nmembers) {
   Workspace& ws = g->ws;
   const int64_t V = g->V;
   if (!ws.gmask) {
     GST_CUDA(cudaMalloc(&ws.gmask, V * sizeof(uint32_t)));
-    GST_CUDA(cudaMalloc(&ws.flags, 3 * V));
+    GST_CUDA(cudaMalloc(&ws.flags, 6 * V));
     GST_CUDA(cudaMalloc(&ws.ctr, sizeof(Counters)));
+    GST_CUDA(cudaMalloc(&ws.ctl, sizeof(GrowCtl)));
+    GST_CUDA(cudaMalloc(&ws.d_params, sizeof(SolveParams)));
     GST_CUDA(cudaMalloc(&ws.stats, kNumStats * sizeof(long long)));
     GST_CUDA(cudaMalloc(&ws.minfo, sizeof(MaskInfo) << GST_MAX_K));
     GST_CUDA(cudaMalloc(&ws.lmasks, sizeof(int32_t) << GST_MAX_K));
     GST_CUDA(cudaMallocHost(&ws.h_ctr, sizeof(Counters)));
-    GST_CUDA(cudaMallocHost(&ws.h_changed, 4 * sizeof(int32_t)));
+    GST_CUDA(cudaMallocHost(&ws.h_ctl, sizeof(GrowCtl)));
+    GST_CUDA(cudaMallocHost(&ws.h_params, sizeof(SolveParams)));
+    GST_CUDA(cudaMallocHost(&ws.h_stats, kNumStats * sizeof(long long)));
+    GST_CUDA(cudaMallocHost(&ws.h_out_v, kTreePrefix * sizeof(int32_t)));
+    GST_CUDA(cudaMallocHost(&ws.h_out_e, kTreePrefix * sizeof(int3)));
     for (auto& e : ws.ev) GST_CUDA(cudaEventCreate(&e));
     // backtrack capacity: states of one optimal derivation
     ws.bt_cap = (int32_t)std::min<int64_t>(4 * V + 256, 1 << 24);
@@ -185,16 +258,26 @@ gst_status ensure_workspace(gst_graph* g, int32_t k, int64_t nmembers) {
     dfree(ws.cost);
     dfree(ws.par);
     ws.k_cap = 0;
-    const size_t entries = (size_t)V * ((size_t(1) << k) - 1);
+    ++ws.gen;
+    const size_t entries = (size_t)V * (size_t)total_stride(k);
     GST_CUDA(cudaMalloc(&ws.cost, entries * sizeof(int32_t)));
     GST_CUDA(cudaMalloc(&ws.par, entries * sizeof(int32_t)));
+    dfree(ws.hub_min);
+    dfree(ws.hub_cnt);
+    int32_t smax = 4;
+    for (int l = 1; l <= k; ++l) smax = std::max(smax, row_stride(binom(k, l)));
+    ws.hub_stride = smax;
+    const size_t nh = std::max<size_t>(1, (size_t)g->nbig);
+    GST_CUDA(cudaMalloc(&ws.hub_min, nh * (size_t)smax * sizeof(unsigned long long)));
+    GST_CUDA(cudaMalloc(&ws.hub_cnt, nh * sizeof(int32_t)));
     ws.k_cap = k;
   }
   if (nmembers > ws.members_cap || !ws.d_group_ptr) {
     dfree(ws.d_group_ptr);
     dfree(ws.d_members);
     ws.members_cap = 0;
-    const int64_t cap = std::max<int64_t>(nmembers, 1024);
+    ++ws.gen;
+    const int64_t cap = std::max<int64_t>(2 * nmembers, 4096);
     GST_CUDA(cudaMalloc(&ws.d_group_ptr, (GST_MAX_K + 1) * sizeof(int32_t)));
     GST_CUDA(cudaMalloc(&ws.d_members, (size_t)cap * sizeof(int32_t)));
     ws.members_cap = cap;
@@ -209,21 +292,23 @@ gst_status ensure_tables(gst_graph* g, int32_t k) {
   if (ws.tables_k == k) return GST_OK;
   const int W = 1 << k;
   std::vector<MaskInfo> info((size_t)W);
-  std::vector<int32_t> lm;
-  lm.reserve((size_t)W);
+  std::vector<int32_t> lm((size_t)total_stride(k), 0);
   ws.h_lvl_base.assign((size_t)k + 2, 0);
   ws.h_lvl_m.assign((size_t)k + 2, 0);
+  ws.h_lvl_stride.assign((size_t)k + 2, 0);
   int32_t base = 0;
   for (int l = 1; l <= k; ++l) {
     ws.h_lvl_base[l] = base;
     ws.h_lvl_m[l] = binom(k, l);
+    ws.h_lvl_stride[l] = row_stride(ws.h_lvl_m[l]);
     int32_t rank = 0;
     for (int S = 1; S < W; ++S)
       if (__builtin_popcount((unsigned)S) == l) {
-        info[(size_t)S] = MaskInfo{base, ws.h_lvl_m[l], rank++, l};
-        lm.push_back(S);
+        info[(size_t)S] = MaskInfo{base, ws.h_lvl_stride[l], rank, l};
+        lm[(size_t)(base + rank)] = S;
+        ++rank;
       }
-    base += ws.h_lvl_m[l];
+    base += ws.h_lvl_stride[l];
   }
   info[0] = MaskInfo{0, 0, 0, 0};
   GST_CUDA(cudaMemcpyAsync(ws.minfo, info.data(), info.size() * sizeof(MaskInfo), cudaMemcpyHostToDevice,
@@ -249,6 +334,156 @@ gst_status validate_groups(const gst_graph* g, const int32_t* group_ptr, const i
   return GST_OK;
 }
 
+LevelArgs level_args(gst_graph* g, int32_t k, int32_t l) {
+  Workspace& ws = g->ws;
+  LevelArgs a{};
+  a.level = l;
+  a.m = ws.h_lvl_m[l];
+  a.stride = ws.h_lvl_stride[l];
+  a.k = k;
+  a.base = (int64_t)ws.h_lvl_base[l] * g->V;
+  a.stride1 = ws.h_lvl_stride[1];
+  a.lmasks = ws.lmasks + ws.h_lvl_base[l];
+  a.minfo = ws.minfo;
+  a.cost = ws.cost;
+  a.par = ws.par;
+  a.gmask = ws.gmask;
+  a.flags = ws.flags;
+  a.cand = ws.flags + 3 * (int64_t)g->V;
+  a.ctl = ws.ctl;
+  a.ctr = ws.ctr;
+  a.stats = ws.stats;
+  a.params = ws.d_params;
+  a.use_cond = 0;
+  return a;
+}
+
+// Work before the waves: group masks and counters.
+gst_status enqueue_prologue(gst_graph* g, int32_t k, cudaStream_t s, int64_t* launches) {
+  Workspace& ws = g->ws;
+  GST_CUDA(cudaMemsetAsync(ws.gmask, 0, (size_t)g->V * sizeof(uint32_t), s));
+  GST_CUDA(cudaMemsetAsync(ws.ctr, 0, sizeof(Counters), s));
+  GST_CUDA(cudaMemsetAsync(&ws.ctr->best, 0xff, sizeof(unsigned long long), s));
+  GST_CUDA(cudaMemsetAsync(ws.stats, 0, kNumStats * sizeof(long long), s));
+  if (g->nbig > 0) {  // hub scratch: minima "none", counters zero
+    GST_CUDA(cudaMemsetAsync(ws.hub_min, 0xff, (size_t)g->nbig * ws.hub_stride * sizeof(unsigned long long), s));
+    GST_CUDA(cudaMemsetAsync(ws.hub_cnt, 0, (size_t)g->nbig * sizeof(int32_t), s));
+  }
+  GST_CUDA(launch_group_masks(ws.d_group_ptr, ws.d_members, k, ws.gmask, s));
+  ++*launches;
+  return GST_OK;
+}
+
+// Wave l's merge, preceded by the reset of its flags and loop control.
+gst_status enqueue_merge(gst_graph* g, const LevelArgs& a, cudaStream_t s, int64_t* launches) {
+  Workspace& ws = g->ws;
+  GST_CUDA(cudaMemsetAsync(ws.flags, 0, 6 * (size_t)g->V, s));
+  GST_CUDA(cudaMemsetAsync(ws.ctl, 0, sizeof(GrowCtl), s));
+  GST_CUDA(launch_merge(graph_dev(g), a, s));
+  ++*launches;
+  return GST_OK;
+}
+
+// Argmin, backtrack and the read-back of counters and a tree prefix.
+gst_status enqueue_epilogue(gst_graph* g, int32_t k, cudaStream_t s, int64_t* launches) {
+  Workspace& ws = g->ws;
+  const GraphDev gd = graph_dev(g);
+  const int32_t* full_slice = ws.cost + (int64_t)ws.h_lvl_base[k] * g->V;
+  GST_CUDA(launch_argmin(gd, full_slice, ws.h_lvl_stride[k], ws.ctr, s));
+  GST_CUDA(launch_backtrack(gd, g->nnz, ws.par, ws.minfo, (1 << k) - 1, ws.ctr, ws.qa, ws.qb, ws.out_v, ws.out_e,
+                            ws.bt_cap, s));
+  *launches += 2;
+  const size_t pre = (size_t)std::min(kTreePrefix, ws.bt_cap);
+  GST_CUDA(cudaMemcpyAsync(ws.h_ctr, ws.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, s));
+  GST_CUDA(cudaMemcpyAsync(ws.h_stats, ws.stats, kNumStats * sizeof(long long), cudaMemcpyDeviceToHost, s));
+  GST_CUDA(cudaMemcpyAsync(ws.h_out_v, ws.out_v, pre * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  GST_CUDA(cudaMemcpyAsync(ws.h_out_e, ws.out_e, pre * sizeof(int3), cudaMemcpyDeviceToHost, s));
+  return GST_OK;
+}
+
+// Adds a while node to the graph being captured on `s`; its body (one
+// growth round) is captured on the side stream.
+gst_status capture_growth_loop(gst_graph* g, LevelArgs a, cudaStream_t s) {
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t cg = nullptr;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t ndeps = 0;
+  GST_CUDA(cudaStreamGetCaptureInfo(s, &cs, nullptr, &cg, &deps, nullptr, &ndeps));
+  if (cs != cudaStreamCaptureStatusActive) return fail(GST_INTERNAL, "stream is not capturing");
+  cudaGraphConditionalHandle h;
+  GST_CUDA(cudaGraphConditionalHandleCreate(&h, cg, 1, cudaGraphCondAssignDefault));
+  cudaGraphNodeParams p{};
+  p.type = cudaGraphNodeTypeConditional;
+  p.conditional.handle = h;
+  p.conditional.type = cudaGraphCondTypeWhile;
+  p.conditional.size = 1;
+  cudaGraphNode_t node;
+  GST_CUDA(cudaGraphAddNode(&node, cg, deps, nullptr, ndeps, &p));
+  GST_CUDA(cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+  cudaGraph_t body = p.conditional.phGraph_out[0];
+  a.cond = h;
+  a.use_cond = 1;
+  GST_CUDA(cudaStreamBeginCaptureToGraph(g->side, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+  const cudaError_t le = launch_grow_round(graph_dev(g), a, g->num_sms, g->side);
+  cudaGraph_t done = nullptr;
+  const cudaError_t ee = cudaStreamEndCapture(g->side, &done);
+  GST_CUDA(le);
+  GST_CUDA(ee);
+  return GST_OK;
+}
+
+// Captures and instantiates the whole query for k (workspace generation gen).
+gst_status build_query_graph(gst_graph* g, int32_t k) {
+  Workspace& ws = g->ws;
+  QueryGraph& q = ws.qg[k];
+  if (q.exec && q.gen == ws.gen) return GST_OK;
+  if (q.exec) cudaGraphExecDestroy(q.exec);
+  if (q.graph) cudaGraphDestroy(q.graph);
+  q = QueryGraph{};
+  cudaStream_t s = g->stream;
+  int64_t launches = 0;
+  GST_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
+  gst_status st = enqueue_prologue(g, k, s, &launches);
+  for (int32_t l = 1; st == GST_OK && l <= k; ++l) {
+    const LevelArgs a = level_args(g, k, l);
+    if (cudaEventRecord(ws.ev[3 * l], s) != cudaSuccess) st = fail(GST_CUDA_ERROR, "event record");
+    if (st == GST_OK) st = enqueue_merge(g, a, s, &launches);
+    if (st == GST_OK && cudaEventRecord(ws.ev[3 * l + 1], s) != cudaSuccess)
+      st = fail(GST_CUDA_ERROR, "event record");
+    if (st == GST_OK && l < k) st = capture_growth_loop(g, a, s);
+    if (st == GST_OK && cudaEventRecord(ws.ev[3 * l + 2], s) != cudaSuccess)
+      st = fail(GST_CUDA_ERROR, "event record");
+  }
+  if (st == GST_OK && cudaEventRecord(ws.ev[1], s) != cudaSuccess) st = fail(GST_CUDA_ERROR, "event record");
+  if (st == GST_OK) st = enqueue_epilogue(g, k, s, &launches);
+  cudaGraph_t graph = nullptr;
+  const cudaError_t ee = cudaStreamEndCapture(s, &graph);
+  if (st != GST_OK) {
+    if (graph) cudaGraphDestroy(graph);
+    return st;
+  }
+  GST_CUDA(ee);
+  cudaGraphExec_t exec = nullptr;
+  const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+  if (ie != cudaSuccess) {
+    cudaGraphDestroy(graph);
+    return fail(GST_CUDA_ERROR, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(ie));
+  }
+  q.graph = graph;
+  q.exec = exec;
+  q.gen = ws.gen;
+  return GST_OK;
+}
+
+float elapsed(cudaEvent_t a, cudaEvent_t b) {
+  float ms = 0.f;
+  if (cudaEventElapsedTime(&ms, a, b) != cudaSuccess) {
+    cudaGetLastError();  // a timing gap is not an error of the solve
+    ms = 0.f;
+  }
+  return ms;
+}
+
 // Builds the host result from the device walk: distinct vertices, distinct
 // edges (u < v), and a check that the edges cost exactly the DP optimum.
 gst_status collect_tree(gst_graph* g, gst_result* r, int32_t cost, int32_t root) {
@@ -258,9 +493,15 @@ gst_status collect_tree(gst_graph* g, gst_result* r, int32_t cost, int32_t root)
   const int32_t nv = c.bt_nv, ne = c.bt_ne;
   std::vector<int32_t> hv((size_t)nv);
   std::vector<int3> he((size_t)ne);
-  if (nv) GST_CUDA(cudaMemcpyAsync(hv.data(), ws.out_v, (size_t)nv * 4, cudaMemcpyDeviceToHost, g->stream));
-  if (ne) GST_CUDA(cudaMemcpyAsync(he.data(), ws.out_e, (size_t)ne * sizeof(int3), cudaMemcpyDeviceToHost, g->stream));
-  GST_CUDA(cudaStreamSynchronize(g->stream));
+  if (nv <= kTreePrefix && ne <= kTreePrefix) {
+    std::copy(ws.h_out_v, ws.h_out_v + nv, hv.begin());
+    std::copy(ws.h_out_e, ws.h_out_e + ne, he.begin());
+  } else {
+    if (nv) GST_CUDA(cudaMemcpyAsync(hv.data(), ws.out_v, (size_t)nv * 4, cudaMemcpyDeviceToHost, g->stream));
+    if (ne)
+      GST_CUDA(cudaMemcpyAsync(he.data(), ws.out_e, (size_t)ne * sizeof(int3), cudaMemcpyDeviceToHost, g->stream));
+    GST_CUDA(cudaStreamSynchronize(g->stream));
+  }
   std::sort(hv.begin(), hv.end());
   hv.erase(std::unique(hv.begin(), hv.end()), hv.end());
   std::vector<std::pair<std::pair<int32_t, int32_t>, int32_t>> es;
@@ -305,10 +546,48 @@ gst_status collect_tree(gst_graph* g, gst_result* r, int32_t cost, int32_t root)
   return GST_OK;
 }
 
-float elapsed(cudaEvent_t a, cudaEvent_t b) {
-  float ms = 0.f;
-  cudaEventElapsedTime(&ms, a, b);
-  return ms;
+// Host-loop driver: launches growth rounds in batches, polling the change
+// count of the last completed round between batches.
+gst_status run_host_loop(gst_graph* g, int32_t k, int64_t* launches, bool* timeout) {
+  Workspace& ws = g->ws;
+  cudaStream_t s = g->stream;
+  const GraphDev gd = graph_dev(g);
+  // GST_TRACE=1 in the environment: poll and report every round (slow;
+  // diagnostics of frontier sizes only)
+  static const bool trace = std::getenv("GST_TRACE") != nullptr;
+  const int batch = trace ? 1 : kPollEvery;
+  const gst_status pst = enqueue_prologue(g, k, s, launches);
+  if (pst != GST_OK) return pst;
+  for (int32_t l = 1; l <= k; ++l) {
+    const LevelArgs a = level_args(g, k, l);
+    GST_CUDA(cudaEventRecord(ws.ev[3 * l], s));
+    gst_status st = enqueue_merge(g, a, s, launches);
+    if (st != GST_OK) return st;
+    GST_CUDA(cudaEventRecord(ws.ev[3 * l + 1], s));
+    if (l < k) {
+      for (int64_t r = 0;; r += batch) {
+        for (int i = 0; i < batch; ++i) {
+          if (trace) GST_CUDA(cudaEventRecord(ws.ev[kEvents - 2], s));
+          GST_CUDA(launch_grow_round(gd, a, g->num_sms, s));
+          if (trace) GST_CUDA(cudaEventRecord(ws.ev[kEvents - 1], s));
+          ++*launches;
+        }
+        GST_CUDA(cudaMemcpyAsync(ws.h_ctl, ws.ctl, sizeof(GrowCtl), cudaMemcpyDeviceToHost, s));
+        GST_CUDA(cudaStreamSynchronize(s));
+        if (trace)
+          std::fprintf(stderr, "gst-trace wave %d round %d changed %d  %.3f ms\n", l, ws.h_ctl->round - 1,
+                       ws.h_ctl->last_changed, elapsed(ws.ev[kEvents - 2], ws.ev[kEvents - 1]));
+        if (ws.h_ctl->timeout) {
+          *timeout = true;
+          return GST_OK;
+        }
+        if (ws.h_ctl->last_changed == 0) break;
+      }
+    }
+    GST_CUDA(cudaEventRecord(ws.ev[3 * l + 2], s));
+  }
+  GST_CUDA(cudaEventRecord(ws.ev[1], s));
+  return enqueue_epilogue(g, k, s, launches);
 }
 
 // One query. Caller holds g->mu and has validated the groups.
@@ -322,107 +601,54 @@ gst_status solve_one(gst_graph* g, const int32_t* group_ptr, const int32_t* memb
   if (st != GST_OK) return st;
   cudaStream_t s = g->stream;
   const int64_t V = g->V;
-  const int32_t full = (1 << k) - 1;
-  const GraphDev gd = graph_dev(g);
-  const int64_t max_rounds = o.max_rounds > 0 ? o.max_rounds : V + 1;
+  const bool use_graph = o.use_graph != 0;
+  // a non-sticky error left by an unrelated earlier runtime call would
+  // otherwise surface at this solve's first kernel-launch check
+  cudaGetLastError();
+  if (use_graph) {
+    st = build_query_graph(g, k);
+    if (st != GST_OK) return st;
+  }
+  ws.h_params->ub = o.upper_bound > 0 ? o.upper_bound : 0;
+  ws.h_params->max_rounds = (int32_t)std::min<int64_t>(o.max_rounds > 0 ? o.max_rounds : V + 1, INT32_MAX);
+  ws.h_params->stats_on = o.collect_stats ? 1 : 0;
+  ws.h_params->k = k;
+  ws.h_params->ovf_limit = kInf - std::max<int32_t>(g->max_w, 1);
 
   GST_CUDA(cudaEventRecord(ws.ev[0], s));
+  GST_CUDA(cudaMemcpyAsync(ws.d_params, ws.h_params, sizeof(SolveParams), cudaMemcpyHostToDevice, s));
   GST_CUDA(cudaMemcpyAsync(ws.d_group_ptr, group_ptr, (size_t)(k + 1) * 4, cudaMemcpyHostToDevice, s));
   if (nmembers)
     GST_CUDA(cudaMemcpyAsync(ws.d_members, members, (size_t)nmembers * 4, cudaMemcpyHostToDevice, s));
-  GST_CUDA(cudaMemsetAsync(ws.gmask, 0, V * sizeof(uint32_t), s));
-  GST_CUDA(cudaMemsetAsync(ws.ctr, 0, sizeof(Counters), s));
-  GST_CUDA(cudaMemsetAsync(&ws.ctr->best, 0xff, sizeof(unsigned long long), s));
-  GST_CUDA(cudaMemsetAsync(ws.stats, 0, kNumStats * sizeof(long long), s));
-  GST_CUDA(launch_group_masks(ws.d_group_ptr, ws.d_members, k, (int32_t)nmembers, ws.gmask, s));
-  int64_t launches = nmembers > 0 ? 1 : 0;
-
-  uint8_t* F[3] = {ws.flags, ws.flags + V, ws.flags + 2 * V};
-  int32_t* C = ws.ctr->changed;
-  double grow_ms = 0, merge_ms = 0;
-  int ev_i = 1;
+  int64_t launches = 0;
   bool timeout = false;
-  for (int32_t l = 1; l <= k && !timeout; ++l) {
-    LevelArgs a{};
-    a.level = l;
-    a.m = ws.h_lvl_m[l];
-    a.k = k;
-    a.base = (int64_t)ws.h_lvl_base[l] * V;
-    a.lmasks = ws.lmasks + ws.h_lvl_base[l];
-    a.minfo = ws.minfo;
-    a.cost = ws.cost;
-    a.par = ws.par;
-    a.gmask = ws.gmask;
-    a.ctr = ws.ctr;
-    a.stats = o.collect_stats ? ws.stats : nullptr;
-    a.ub = (l >= 2 && o.upper_bound > 0) ? o.upper_bound : 0;
-    a.base1 = 0;
-    // merge = "round -1": writes frontier F[2] and count C[2]
-    GST_CUDA(cudaMemsetAsync(ws.flags, 0, 3 * V, s));
-    GST_CUDA(cudaMemsetAsync(C, 0, 3 * sizeof(int32_t), s));
-    a.next_flag = F[2];
-    a.cur_changed = C + 2;
-    cudaEvent_t e0 = ws.ev[ev_i++];
-    cudaEvent_t e1 = ws.ev[ev_i++];
-    GST_CUDA(cudaEventRecord(e0, s));
-    GST_CUDA(launch_merge(gd, a, s));
-    ++launches;
-    GST_CUDA(cudaEventRecord(e1, s));
-    if (l == k) {
-      GST_CUDA(cudaEventSynchronize(e1));
-      merge_ms += elapsed(e0, e1);
-      break;
-    }
-    // growth rounds, polled every `batch` launches; converged rounds exit
-    // on their first instruction
-    int64_t r = 0;
-    const int batch = 8;
-    for (;;) {
-      for (int i = 0; i < batch; ++i, ++r) {
-        a.cur_flag = F[(r + 2) % 3];
-        a.next_flag = F[r % 3];
-        a.clear_flag = F[(r + 1) % 3];
-        a.prev_changed = C + (r + 2) % 3;
-        a.cur_changed = C + r % 3;
-        a.zero_changed = C + (r + 1) % 3;
-        GST_CUDA(launch_grow_round(gd, a, g->num_sms, s));
-        ++launches;
-      }
-      GST_CUDA(cudaMemcpyAsync(ws.h_changed, C + (r - 1) % 3, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  if (use_graph) {
+    GST_CUDA(cudaGraphLaunch(ws.qg[k].exec, s));
+  } else {
+    st = run_host_loop(g, k, &launches, &timeout);
+    if (st != GST_OK) return st;
+    if (timeout) {
       GST_CUDA(cudaStreamSynchronize(s));
-      if (*ws.h_changed == 0) break;
-      if (r >= max_rounds) {
-        timeout = true;
-        break;
-      }
+      return fail(GST_TIMEOUT, "growth did not converge within max_rounds");
     }
-    cudaEvent_t e2 = ws.ev[ev_i++];
-    GST_CUDA(cudaEventRecord(e2, s));
-    GST_CUDA(cudaEventSynchronize(e2));
-    merge_ms += elapsed(e0, e1);
-    grow_ms += elapsed(e1, e2);
-    ev_i -= 3;  // reuse the three events for the next wave
   }
-  if (timeout) return fail(GST_TIMEOUT, "growth did not converge within max_rounds");
-  cudaEvent_t eb0 = ws.ev[ev_i], eb1 = ws.ev[ev_i + 1];
-  GST_CUDA(cudaEventRecord(eb0, s));
-  const int32_t* full_slice = ws.cost + (int64_t)ws.h_lvl_base[k] * V;
-  GST_CUDA(launch_argmin(gd, full_slice, ws.ctr, s));
-  GST_CUDA(launch_backtrack(gd, g->nnz, ws.par, ws.minfo, full, ws.ctr, ws.qa, ws.qb, ws.out_v, ws.out_e,
-                            ws.bt_cap, s));
-  launches += 2;
-  r->launches = launches;
-  GST_CUDA(cudaEventRecord(eb1, s));
-  GST_CUDA(cudaMemcpyAsync(ws.h_ctr, ws.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, s));
-  if (o.collect_stats)
-    GST_CUDA(cudaMemcpyAsync(r->stats, ws.stats, kNumStats * sizeof(long long), cudaMemcpyDeviceToHost, s));
+  GST_CUDA(cudaEventRecord(ws.ev[2], s));
   GST_CUDA(cudaStreamSynchronize(s));
-  r->ms[0] = elapsed(ws.ev[0], eb1);
+  const Counters& c = *ws.h_ctr;
+  if (use_graph) launches = 1 + k + c.rounds_total + 2;
+  r->launches = launches;
+  r->states = (int64_t)c.states;
+  std::copy(ws.h_stats, ws.h_stats + kNumStats, r->stats);
+  r->ms[0] = elapsed(ws.ev[0], ws.ev[2]);
+  double merge_ms = 0, grow_ms = 0;
+  for (int32_t l = 1; l <= k; ++l) {
+    merge_ms += elapsed(ws.ev[3 * l], ws.ev[3 * l + 1]);
+    if (l < k) grow_ms += elapsed(ws.ev[3 * l + 1], ws.ev[3 * l + 2]);
+  }
   r->ms[1] = grow_ms;
   r->ms[2] = merge_ms;
-  r->ms[3] = elapsed(eb0, eb1);
-  const Counters& c = *ws.h_ctr;
-  r->states = (int64_t)c.states;
+  r->ms[3] = elapsed(ws.ev[1], ws.ev[2]);
+  if (c.timeout) return fail(GST_TIMEOUT, "growth did not converge within max_rounds");
   if (c.overflow) return fail(GST_OVERFLOW, "a tree cost reached GST_COST_LIMIT");
   if (c.best == ~0ull) {
     r->status = GST_INFEASIBLE;
@@ -462,20 +688,35 @@ gst_status gst_graph_upload(const int32_t* row_ptr, const int32_t* col, const in
   for (int32_t v = 0; v < V; ++v)
     if (row_ptr[v + 1] < row_ptr[v]) return fail(GST_BAD_INPUT, "row_ptr must be non-decreasing");
   std::vector<int2> adj((size_t)nnz);
+  int32_t max_w = 0;
   for (int64_t e = 0; e < nnz; ++e) {
     if (col[e] < 0 || col[e] >= V) return fail(GST_BAD_INPUT, "col entry out of range");
     if (w[e] < 0 || w[e] >= GST_COST_LIMIT) return fail(GST_BAD_INPUT, "weights must be in [0, GST_COST_LIMIT)");
     adj[(size_t)e] = make_int2(col[e], w[e]);
+    max_w = std::max(max_w, w[e]);
   }
   auto* g = new (std::nothrow) gst_graph;
   if (!g) return fail(GST_OOM, "host allocation failed");
   g->V = V;
   g->nnz = nnz;
-  g->h_row_ptr.assign(row_ptr, row_ptr + V + 1);
-  std::vector<int32_t> big;
-  for (int32_t v = 0; v < V; ++v)
-    if (row_ptr[v + 1] - row_ptr[v] > kDegBig) big.push_back(v);
+  g->max_w = max_w;
+  // Growth order of the non-hub vertices: by decreasing degree within
+  // windows of kOrderWindow consecutive IDs, so the 32 lanes of a warp walk
+  // rows of similar length while a window's rows stay close in memory.
+  std::vector<int32_t> big, order;
+  for (int32_t v = 0; v < V; ++v) (row_ptr[v + 1] - row_ptr[v] > kDegBig ? big : order).push_back(v);
+  constexpr size_t kOrderWindow = 1024;
+  for (size_t w0 = 0; w0 < order.size(); w0 += kOrderWindow) {
+    const size_t w1 = std::min(order.size(), w0 + kOrderWindow);
+    std::stable_sort(order.begin() + (ptrdiff_t)w0, order.begin() + (ptrdiff_t)w1, [&](int32_t a, int32_t b) {
+      return row_ptr[a + 1] - row_ptr[a] > row_ptr[b + 1] - row_ptr[b];
+    });
+  }
   g->nbig = (int32_t)big.size();
+  std::vector<int2> chunks;
+  for (int32_t h = 0; h < g->nbig; ++h)
+    for (int32_t e = row_ptr[big[(size_t)h]]; e < row_ptr[big[(size_t)h] + 1]; e += 32) chunks.push_back(make_int2(h, e));
+  g->nchunks = (int64_t)chunks.size();
   auto cleanup = [&](gst_status s) {
     gst_graph_free(g);
     return s;
@@ -483,7 +724,8 @@ gst_status gst_graph_upload(const int32_t* row_ptr, const int32_t* col, const in
   cudaError_t e;
   if ((e = cudaGetDevice(&g->device)) != cudaSuccess ||
       (e = cudaDeviceGetAttribute(&g->num_sms, cudaDevAttrMultiProcessorCount, g->device)) != cudaSuccess ||
-      (e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking)) != cudaSuccess)
+      (e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking)) != cudaSuccess ||
+      (e = cudaStreamCreateWithFlags(&g->side, cudaStreamNonBlocking)) != cudaSuccess)
     return cleanup(fail(GST_CUDA_ERROR, std::string("device setup: ") + cudaGetErrorString(e)));
   auto up = [&](void** dst, const void* src, size_t bytes) -> cudaError_t {
     cudaError_t x = cudaMalloc(dst, bytes ? bytes : 4);
@@ -493,6 +735,8 @@ gst_status gst_graph_upload(const int32_t* row_ptr, const int32_t* col, const in
   if ((e = up((void**)&g->d_row_ptr, row_ptr, (size_t)(V + 1) * 4)) != cudaSuccess ||
       (e = up((void**)&g->d_adj, adj.data(), adj.size() * sizeof(int2))) != cudaSuccess ||
       (e = up((void**)&g->d_big, big.data(), big.size() * 4)) != cudaSuccess ||
+      (e = up((void**)&g->d_order, order.data(), order.size() * 4)) != cudaSuccess ||
+      (e = up((void**)&g->d_hub_chunk, chunks.data(), chunks.size() * sizeof(int2))) != cudaSuccess ||
       (e = cudaStreamSynchronize(g->stream)) != cudaSuccess)
     return cleanup(fail(e == cudaErrorMemoryAllocation ? GST_OOM : GST_CUDA_ERROR,
                         std::string("graph upload: ") + cudaGetErrorString(e)));
@@ -510,7 +754,10 @@ void gst_graph_free(gst_graph* g) {
   dfree(g->d_row_ptr);
   dfree(g->d_adj);
   dfree(g->d_big);
+  dfree(g->d_order);
+  dfree(g->d_hub_chunk);
   if (g->stream) cudaStreamDestroy(g->stream);
+  if (g->side) cudaStreamDestroy(g->side);
   if (prev >= 0) cudaSetDevice(prev);
   delete g;
 }
@@ -596,16 +843,16 @@ gst_status gst_graph_debug_table(gst_graph* g, int32_t k, int32_t* out) {
   if (ws.tables_k != k || ws.k_cap < k || !ws.cost) return fail(GST_BAD_INPUT, "no solve with this k on record");
   const int64_t V = g->V;
   const int64_t W = int64_t(1) << k;
-  std::vector<int32_t> dev((size_t)(V * (W - 1)));
+  std::vector<int32_t> dev((size_t)(V * total_stride(k)));
   GST_CUDA(cudaMemcpy(dev.data(), ws.cost, dev.size() * sizeof(int32_t), cudaMemcpyDeviceToHost));
   for (int64_t v = 0; v < V; ++v) out[v * W] = kInf;
   for (int l = 1; l <= k; ++l) {
     const int64_t base = (int64_t)ws.h_lvl_base[l] * V;
-    const int32_t m = ws.h_lvl_m[l];
+    const int32_t s = ws.h_lvl_stride[l];
     int32_t rank = 0;
     for (int32_t S = 1; S < (int32_t)W; ++S) {
       if (__builtin_popcount((unsigned)S) != l) continue;
-      for (int64_t v = 0; v < V; ++v) out[v * W + S] = dev[(size_t)(base + v * m + rank)];
+      for (int64_t v = 0; v < V; ++v) out[v * W + S] = dev[(size_t)(base + v * s + rank)];
       ++rank;
     }
   }
@@ -613,6 +860,6 @@ gst_status gst_graph_debug_table(gst_graph* g, int32_t k, int32_t* out) {
 }
 
 const char* gst_last_error(void) { return g_last_error.c_str(); }
-const char* gst_version(void) { return "gst-gb300 0.1 (sm_103a)"; }
+const char* gst_version(void) { return "gst-gb300 0.2 (sm_103a)"; }
 
 }  // extern "C"

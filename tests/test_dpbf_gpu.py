@@ -32,23 +32,28 @@ def test_fixture_simple_iterative():
         assert cost == 16
 
 
-def test_golden_costs_bit_exact(golden):
+MODES = [pytest.param(False, id="host-loop"), pytest.param(True, id="cuda-graph")]
+
+
+@pytest.mark.parametrize("use_graph", MODES)
+def test_golden_costs_bit_exact(golden, use_graph):
     graphs = {}
     for case in golden["cases"]:
         g, gp, mem = make_instance(case)
         key = tuple(case["graph"])
         if key not in graphs:
             graphs[key] = native.Graph(g.row_ptr, g.col, g.w)
-        res = graphs[key].solve(gp, mem)
+        res = graphs[key].solve(gp, mem, use_graph=use_graph)
         _check(g.row_ptr, g.col, g.w, gp, mem, res, case["dpbf"])
     for dg in graphs.values():
         dg.close()
 
 
-def test_edge_cases():
+@pytest.mark.parametrize("use_graph", MODES)
+def test_edge_cases(use_graph):
     for name, c in load_edge_cases().items():
         with native.Graph(c["rp"], c["col"], c["w"]) as g:
-            res = g.solve(c["gp"], c["mem"])
+            res = g.solve(c["gp"], c["mem"], use_graph=use_graph)
             if int(c["cost"]) < 0:
                 assert res.status == Status.INFEASIBLE, name
                 assert res.cost == -1 and len(res.vertices) == 0
@@ -63,8 +68,9 @@ def test_empty_group_is_infeasible():
         assert g.solve(gp2, mem).status == Status.INFEASIBLE
 
 
+@pytest.mark.parametrize("use_graph", MODES)
 @pytest.mark.parametrize("idx", [0, 1, 2, 3, 200, 201, 202, 203, 204])
-def test_full_state_table_matches_oracle(golden, idx):
+def test_full_state_table_matches_oracle(golden, idx, use_graph):
     case = golden["cases"][idx]
     g, gp, mem = make_instance(case)
     if g.V > 6000:
@@ -73,7 +79,7 @@ def test_full_state_table_matches_oracle(golden, idx):
     want = oracle.dp_table(g.row_ptr, g.col, g.w, gp, mem)
     want = np.where(want == ORACLE_INF, native.COST_LIMIT, want)
     with native.Graph(g.row_ptr, g.col, g.w) as dg:
-        res = dg.solve(gp, mem)
+        res = dg.solve(gp, mem, use_graph=use_graph)
         assert res.status == Status.OK
         got = dg.debug_table(k)
     # the last wave is merged but not grown (growth cannot lower the optimum)
@@ -83,7 +89,8 @@ def test_full_state_table_matches_oracle(golden, idx):
     assert np.all(got[:, full] >= want[:, full])
 
 
-def test_upper_bound_pruning_is_exact(golden):
+@pytest.mark.parametrize("use_graph", MODES)
+def test_upper_bound_pruning_is_exact(golden, use_graph):
     for case in golden["cases"][::20] + golden["cases"][200:]:
         g, gp, mem = make_instance(case)
         opt = case["dpbf"]
@@ -91,11 +98,12 @@ def test_upper_bound_pruning_is_exact(golden):
             for ub in (opt, opt + 1, opt + 50, 2 * opt + 1):
                 if ub <= 0:
                     continue
-                res = dg.solve(gp, mem, upper_bound=ub)
+                res = dg.solve(gp, mem, upper_bound=ub, use_graph=use_graph)
                 _check(g.row_ptr, g.col, g.w, gp, mem, res, opt)
             if opt > 1:
                 # a bound below the optimum prunes every full tree
-                assert dg.solve(gp, mem, upper_bound=opt - 1).status == Status.INFEASIBLE
+                res = dg.solve(gp, mem, upper_bound=opt - 1, use_graph=use_graph)
+                assert res.status == Status.INFEASIBLE
 
 
 def test_hub_rows_use_block_path():
@@ -130,13 +138,14 @@ def test_many_group_counts(k):
         _check(g.row_ptr, g.col, g.w, gp, mem, res, want.cost)
 
 
-def test_workspace_reuse_across_k_and_repeat():
+@pytest.mark.parametrize("use_graph", MODES)
+def test_workspace_reuse_across_k_and_repeat(use_graph):
     g = native.gen_barabasi_albert(4000, 4, 1, 100, 3)
     with native.Graph(g.row_ptr, g.col, g.w) as dg:
-        for k, seed in [(3, 1), (6, 2), (4, 3), (6, 2), (2, 5)]:
+        for k, seed in [(3, 1), (6, 2), (4, 3), (6, 2), (2, 5), (7, 9), (6, 2)]:
             gp, mem = native.gen_groups_zipf_degree(g, k, 1.2, 5, 500, seed)
             want = oracle.dpbf(g.row_ptr, g.col, g.w, gp, mem)
-            res = dg.solve(gp, mem)
+            res = dg.solve(gp, mem, use_graph=use_graph)
             _check(g.row_ptr, g.col, g.w, gp, mem, res, want.cost)
 
 
@@ -176,12 +185,27 @@ def test_bad_member_is_rejected():
         assert e.value.status == Status.BAD_INPUT
 
 
-def test_timeout_status_is_reported():
+@pytest.mark.parametrize("use_graph", MODES)
+def test_timeout_status_is_reported(use_graph):
     g = native.gen_random_connected(2000, 4000, 1, 100, 8)
     gp, mem = native.gen_groups_uniform(2000, 3, 2, 9)
     with native.Graph(g.row_ptr, g.col, g.w) as dg:
-        res = dg.solve(gp, mem, max_rounds=1, raise_on_error=False)
+        res = dg.solve(gp, mem, max_rounds=1, raise_on_error=False, use_graph=use_graph)
         assert res.status == Status.TIMEOUT
         # the graph stays usable after the error
         want = oracle.dpbf(g.row_ptr, g.col, g.w, gp, mem)
-        _check(g.row_ptr, g.col, g.w, gp, mem, dg.solve(gp, mem), want.cost)
+        _check(g.row_ptr, g.col, g.w, gp, mem, dg.solve(gp, mem, use_graph=use_graph), want.cost)
+
+
+@pytest.mark.parametrize("use_graph", MODES)
+def test_stats_and_launch_count(use_graph):
+    g = native.gen_barabasi_albert(20000, 4, 1, 100, 5)
+    gp, mem = native.gen_groups_zipf_degree(g, 5, 1.2, 5, 500, 6)
+    with native.Graph(g.row_ptr, g.col, g.w) as dg:
+        res = dg.solve(gp, mem, use_graph=use_graph, collect_stats=True)
+        assert res.status == Status.OK
+        st = res.stats
+        assert st["rounds"] > 0 and st["vertices"] > 0 and st["entries"] > 0 and st["bytes"] > 0
+        # each state evaluates its unordered splits, except states of cost 0
+        assert 0 < st["splits"] <= 20000 * (3**5 - 2**6 + 1) // 2
+        assert res.launches >= 1 + 5 + st["rounds"] + 2
