@@ -192,6 +192,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="ba1m_k6", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--driver", default="graph", choices=["graph", "host"],
+                    help="graph: one captured CUDA graph per query; host: host-launched growth rounds")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     wl = WORKLOADS[args.workload]
@@ -233,7 +235,7 @@ def main():
         torch.cuda.synchronize()
         gp, mem = queries[i]
         t0 = time.perf_counter()
-        r = dg.solve(gp, mem, collect_stats=stats)
+        r = dg.solve(gp, mem, collect_stats=stats, use_graph=args.driver == "graph")
         wall = time.perf_counter() - t0
         assert r.status == N.Status.OK, r.status
         return r, wall
@@ -270,7 +272,7 @@ def main():
         "data": "synthetic (seeded generators; no public dataset)",
         "config": {
             "workload": args.workload, "desc": wl["desc"], "V": g.V, "nnz": g.nnz, "k": wl["k"],
-            "method": "plain DPBF (no pruning)", "l2": "flushed before every step (256 MiB device write); "
+            "method": "plain DPBF (no pruning)", "driver": args.driver, "l2": "flushed before every step (256 MiB device write); "
             "state table 504 MB > L2", "graph_upload_ms": upload_ms,
             "costs": [r.cost for r, _ in results],
         },

@@ -27,6 +27,13 @@ constexpr int32_t kLeaf = INT32_MIN;
 constexpr int kDegBig = 64;        // rows longer than this go to a CTA of their own
 constexpr int kGrowThreads = 256;  // block size of growth / merge kernels
 constexpr int kMaxThreadMasks = 24;  // waves with stride <= this: a thread per vertex
+// Sparse rounds scan candidate flags in tiles of this many consecutive
+// vertex IDs (one warp each). The graph is relabelled at upload so that
+// every tile holds a mix of degrees (see gst_graph_upload).
+constexpr int kCandTile = 512;
+// Dense rounds when the previous round changed more than V >> this
+// (sparse rounds with marking stay cheaper up to about half the graph).
+constexpr int kDefaultDenseShift = 1;
 
 __host__ __device__ constexpr int32_t row_stride(int32_t m) { return (m + 3) & ~3; }
 
@@ -62,7 +69,8 @@ struct SolveParams {
   // weight to a finite cost stays below kInf, so relaxations need no
   // overflow test. A cost that reaches the limit is reported (GST_OVERFLOW).
   int32_t ovf_limit;
-  int32_t pad[3];
+  int32_t dense_shift;  // dense round when the previous one changed > V >> dense_shift
+  int32_t pad[2];
 };
 
 // Growth-loop control of the current wave (reset before each wave).
@@ -114,8 +122,9 @@ struct LevelArgs {
   int32_t* cost;
   int32_t* par;
   const uint32_t* gmask;       // groups(v) bit mask
-  uint8_t* flags;              // changed flags F[0..2] (V bytes each)
-  uint8_t* cand;               // candidate flags C[0..2] (V bytes each)
+  int32_t vpad;                // V rounded up to a multiple of 16: stride of the flag arrays
+  uint8_t* flags;              // changed flags F[0..2] (vpad bytes each)
+  uint8_t* cand;               // candidate flags C[0..2] (vpad bytes each, 16-byte aligned)
   GrowCtl* ctl;
   Counters* ctr;
   long long* stats;
@@ -125,10 +134,15 @@ struct LevelArgs {
 };
 
 // Launchers (dpbf_kernels.cu). All asynchronous on `stream`.
-cudaError_t launch_group_masks(const int32_t* group_ptr, const int32_t* members, int32_t k, uint32_t* gmask,
-                               cudaStream_t stream);
+// members are caller IDs; perm maps them to internal IDs
+cudaError_t launch_group_masks(const int32_t* group_ptr, const int32_t* members, const int32_t* perm, int32_t k,
+                               uint32_t* gmask, cudaStream_t stream);
 cudaError_t launch_merge(const GraphDev& g, const LevelArgs& a, cudaStream_t stream);
-cudaError_t launch_grow_round(const GraphDev& g, const LevelArgs& a, int num_sms, cudaStream_t stream);
+// One growth round: a hub-relaxation kernel (when the graph has hubs) and
+// the round kernel proper. Adds the kernels launched to *launches.
+cudaError_t launch_grow_round(const GraphDev& g, const LevelArgs& a, int num_sms, cudaStream_t stream,
+                              int64_t* launches);
+cudaError_t launch_seed(const GraphDev& g, const LevelArgs& a, int num_sms, cudaStream_t stream);
 cudaError_t launch_argmin(const GraphDev& g, const int32_t* full_slice, int32_t stride, Counters* ctr,
                           cudaStream_t stream);
 cudaError_t launch_backtrack(const GraphDev& g, int64_t nnz, const int32_t* par, const MaskInfo* minfo,

@@ -52,27 +52,45 @@ __device__ __forceinline__ void add_stat(long long* stats, int slot, long long x
 }
 
 // Largest cost allowed for state (v,S) under the bound: ub - LB(v, full^S)
-// with LB = max over groups g outside S of T(v,{g}) (one-label bound,
-// src/DPQ.cu:361-403, applied per remaining group set). -1 = state dead.
+// with LB = max over groups g outside S of dist(v, g) (one-label bound,
+// src/DPQ.cu:361-403, applied per remaining group set). Under a bound, wave
+// 1 grows only light states (2 * cost <= ub, see below), so T(v,{g}) is the
+// exact distance when it is light and otherwise only known to exceed ub/2:
+// min(T(v,{g}), ub/2 + 1) is a valid lower bound in both cases.
+// -1 = state dead.
 __device__ __forceinline__ int32_t prune_cap(const LevelArgs& a, int32_t ub, int32_t v, uint32_t S) {
   const int32_t* d = a.cost + (int64_t)v * a.stride1;  // wave 1 slice starts at 0; rank({g}) = g
+  const int32_t beyond = ub / 2 + 1;
   int32_t lb = 0;
-  for (int g = 0; g < a.k; ++g)
-    if (!((S >> g) & 1u)) lb = max(lb, __ldg(d + g));
+#pragma unroll
+  for (int gg = 0; gg < 16; ++gg)  // predicated, so the loads overlap
+    if (gg < a.k && !((S >> gg) & 1u)) lb = max(lb, min(__ldg(d + gg), beyond));
   const int32_t cap = ub - lb;
   return cap < 0 ? -1 : cap;
+}
+
+// Under a bound ub >= OPT, a state of cost c is "light" when 2c <= ub. An
+// optimal tree has a vertex r (its weighted centroid) where every subtree
+// hanging off r costs at most OPT/2, so it is derived from light states by
+// growth and by merges of light states, except for the merges at r itself,
+// whose last step joins a state with its complement (the rule of PrunedDP++,
+// rucgraph/graph_v_of_v_idealID_PrunedDPPlusPlus.h:795). Hence: only light
+// states grow; merges below the last wave use light parts only; the last
+// wave merges any parts. Heavy states are kept for that last merge.
+__device__ __forceinline__ int32_t light_or_inf(int32_t c, int32_t ub) {
+  return (ub > 0 && 2 * c > ub) ? kInf : c;  // 2 * kInf < 2^31: no wrap
 }
 
 }  // namespace
 
 // ------------------------------------------------------------ group masks --
 __global__ void k_group_masks(const int32_t* __restrict__ group_ptr, const int32_t* __restrict__ members,
-                              int32_t k, uint32_t* __restrict__ gmask) {
+                              const int32_t* __restrict__ perm, int32_t k, uint32_t* __restrict__ gmask) {
   const int32_t n = group_ptr[k];
   for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     int32_t g = 0;
     while (g + 1 < k && group_ptr[g + 1] <= i) ++g;
-    atomicOr(gmask + members[i], 1u << g);
+    atomicOr(gmask + perm[members[i]], 1u << g);
   }
 }
 
@@ -87,8 +105,9 @@ __global__ void __launch_bounds__(kGrowThreads) k_merge(GraphDev g, LevelArgs a)
   const int64_t total = (int64_t)g.V * a.stride;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   const int32_t ub = (a.level >= 2) ? a.params->ub : 0;
+  const int32_t ub_light = a.params->ub;
   const int32_t ovf_limit = a.params->ovf_limit;
-  uint8_t* flag2 = a.flags + 2 * (int64_t)g.V;
+  uint8_t* flag2 = a.flags + 2 * (int64_t)a.vpad;
   long long acc[3] = {0, 0, 0};  // finite states, splits, overflow
   for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += stride) {
     const int32_t v = (int32_t)(idx / a.stride);
@@ -103,8 +122,12 @@ __global__ void __launch_bounds__(kGrowThreads) k_merge(GraphDev g, LevelArgs a)
         for (uint32_t sub = (rest - 1u) & rest;; sub = (sub - 1u) & rest) {
           const uint32_t s1 = sub | low, s2 = S ^ s1;
           const MaskInfo i1 = a.minfo[s1], i2 = a.minfo[s2];
-          const int32_t c1 = a.cost[(int64_t)i1.base * g.V + (int64_t)v * i1.stride + i1.rank];
-          const int32_t c2 = a.cost[(int64_t)i2.base * g.V + (int64_t)v * i2.stride + i2.rank];
+          int32_t c1 = a.cost[(int64_t)i1.base * g.V + (int64_t)v * i1.stride + i1.rank];
+          int32_t c2 = a.cost[(int64_t)i2.base * g.V + (int64_t)v * i2.stride + i2.rank];
+          if (a.level < a.k) {
+            c1 = light_or_inf(c1, ub_light);
+            c2 = light_or_inf(c2, ub_light);
+          }
           const int32_t c = c1 + c2;  // both <= kInf < 2^30: no wrap
           if (c1 < kInf && c2 < kInf) {
             if (c >= ovf_limit)
@@ -138,7 +161,6 @@ __global__ void __launch_bounds__(kGrowThreads) k_merge(GraphDev g, LevelArgs a)
     }
     if (a.params->stats_on) add_stat(a.stats, kStatSplits, acc[1]);
     if (acc[2]) atomicExch(&a.ctr->overflow, 1);
-    if (blockIdx.x == 0) a.ctl->dense[2] = 1;  // round 0 sweeps every vertex
   }
 }
 
@@ -175,7 +197,8 @@ constexpr int kGatherUnroll = 4;
 struct RoundState {
   int32_t r;
   bool dense, all_cand, stats;
-  int32_t ub;
+  int32_t ub;        // one-label pruning bound (waves >= 2)
+  int32_t ub_light;  // only states with 2 * cost <= ub_light grow (all waves)
   int32_t ovf_limit;  // stored costs must stay below this (kInf - largest weight)
   const uint8_t* cur_flag;
   uint8_t* next_flag;
@@ -197,19 +220,78 @@ __device__ __forceinline__ bool round_begin(const GraphDev& g, const LevelArgs& 
     if (a.use_cond && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(a.cond, 0);
     return false;
   }
-  rs.dense = prev > (g.V >> 1);
+  rs.dense = prev > (g.V >> a.params->dense_shift);
   rs.all_cand = rs.dense || ctl->dense[(rs.r + 2) % 3] != 0;
   rs.stats = a.params->stats_on != 0;
-  rs.ub = a.level >= 2 ? a.params->ub : 0;  // wave 1 is the bound's own input: never pruned
+  rs.ub = a.level >= 2 ? a.params->ub : 0;  // wave 1 is the bound's own input: not pruned by it
+  rs.ub_light = a.params->ub;
   rs.ovf_limit = a.params->ovf_limit;
-  const int64_t V = g.V;
-  rs.cur_flag = a.flags + (int64_t)((rs.r + 2) % 3) * V;
-  rs.next_flag = a.flags + (int64_t)(rs.r % 3) * V;
-  rs.clear_flag = a.flags + (int64_t)((rs.r + 1) % 3) * V;
-  rs.cand_cur = a.cand + (int64_t)(rs.r % 3) * V;
-  rs.cand_next = a.cand + (int64_t)((rs.r + 1) % 3) * V;
-  rs.cand_clear = a.cand + (int64_t)((rs.r + 2) % 3) * V;
+  const int64_t P = a.vpad;  // flag arrays are padded to keep word atomics aligned
+  rs.cur_flag = a.flags + (int64_t)((rs.r + 2) % 3) * P;
+  rs.next_flag = a.flags + (int64_t)(rs.r % 3) * P;
+  rs.clear_flag = a.flags + (int64_t)((rs.r + 1) % 3) * P;
+  rs.cand_cur = a.cand + (int64_t)(rs.r % 3) * P;
+  rs.cand_next = a.cand + (int64_t)((rs.r + 1) % 3) * P;
+  rs.cand_clear = a.cand + (int64_t)((rs.r + 2) % 3) * P;
   return true;
+}
+
+// Makes v a candidate of the next round (an idempotent byte store).
+__device__ __forceinline__ void mark_candidate(uint8_t* cand, int32_t v, uint32_t (&acc)[kAccN]) {
+  cand[v] = 1;
+  ++acc[kAccMarks];
+}
+
+// One-label bound of vertex v, loaded once: dd[g] = min(T(v,{g}), ub/2+1)
+// for the k groups, 0 for absent groups (wave 1 is not written while waves
+// >= 2 grow). Rows of wave 1 are 16-byte aligned.
+__device__ __forceinline__ void load_label_bound(const LevelArgs& a, int32_t ub, int32_t v, int32_t (&dd)[16]) {
+  const int4* d4 = reinterpret_cast<const int4*>(a.cost + (int64_t)v * a.stride1);
+  const int32_t beyond = ub / 2 + 1;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    int4 t = make_int4(0, 0, 0, 0);
+    if (4 * q < a.k) t = __ldg(d4 + q);
+    dd[4 * q] = 4 * q < a.k ? min(t.x, beyond) : 0;
+    dd[4 * q + 1] = 4 * q + 1 < a.k ? min(t.y, beyond) : 0;
+    dd[4 * q + 2] = 4 * q + 2 < a.k ? min(t.z, beyond) : 0;
+    dd[4 * q + 3] = 4 * q + 3 < a.k ? min(t.w, beyond) : 0;
+  }
+}
+
+// max over groups outside S of dd (the bound on completing S to the full set)
+__device__ __forceinline__ int32_t label_bound(const int32_t (&dd)[16], uint32_t S) {
+  int32_t lb = 0;
+#pragma unroll
+  for (int gg = 0; gg < 16; ++gg) lb = max(lb, ((S >> gg) & 1u) ? 0 : dd[gg]);
+  return lb;
+}
+
+// Does some entry j of vals (light-filtered costs of the marking vertex,
+// edge weight w still to add) improve vertex v's entry y(j)? With a bound
+// the improved value must also pass v's one-label cap for mask j. Masks go
+// in passes of 32: the comparisons of a pass are independent (their loads
+// overlap) and leave a bit set per improved mask; v's bound is loaded only
+// when some bit is set.
+template <class Vals, class Row>
+__device__ __forceinline__ bool improves_row(const LevelArgs& a, int32_t ub, int32_t v, int32_t w, const Vals& vals,
+                                             const Row& y, int m) {
+  for (int j0 = 0; j0 < m; j0 += 32) {
+    const int n = min(32, m - j0);
+    uint32_t bits = 0;
+#pragma unroll 8
+    for (int jj = 0; jj < n; ++jj) bits |= (vals(j0 + jj) + w < y(j0 + jj) ? 1u : 0u) << jj;
+    if (!bits) continue;
+    if (ub <= 0) return true;
+    int32_t dd[16];
+    load_label_bound(a, ub, v, dd);
+    while (bits) {
+      const int j = j0 + __ffs(bits) - 1;
+      bits &= bits - 1u;
+      if (vals(j) + w + label_bound(dd, (uint32_t)__ldg(a.lmasks + j)) <= ub) return true;
+    }
+  }
+  return false;
 }
 
 // Block-level accumulators of a growth round: every warp folds its counters
@@ -226,34 +308,37 @@ __device__ __forceinline__ void block_acc_init(BlockAcc& ba) {
   __syncthreads();
 }
 
-__device__ __forceinline__ void round_end(const LevelArgs& a, const RoundState& rs, long long (&acc)[kAccN],
-                                          BlockAcc& ba) {
+// Folds the block's counters into the round totals; true in the one thread
+// of the block that did so (after every warp of the block has arrived).
+__device__ __forceinline__ bool round_flush(const LevelArgs& a, const RoundState& rs, uint32_t (&acc)[kAccN],
+                                            BlockAcc& ba) {
   const int lane = threadIdx.x & 31;
+  long long tot[kAccN];
 #pragma unroll
-  for (int i = 0; i < kAccN; ++i) acc[i] = warp_sum_ll(acc[i]);
+  for (int i = 0; i < kAccN; ++i) tot[i] = warp_sum_ll((long long)acc[i]);
   int last = 0;
   if (lane == 0) {
 #pragma unroll
     for (int i = 0; i < kAccN; ++i)
-      if (acc[i]) atomicAdd(&ba.v[i], (unsigned long long)acc[i]);
+      if (tot[i]) atomicAdd(&ba.v[i], (unsigned long long)tot[i]);
     __threadfence_block();
     last = atomicAdd(&ba.warps_done, 1u) == (blockDim.x >> 5) - 1;
   }
-  if (!last) return;
+  if (!last) return false;
   __threadfence_block();
 #pragma unroll
-  for (int i = 0; i < kAccN; ++i) acc[i] = (long long)atomicAdd(&ba.v[i], 0ull);
+  for (int i = 0; i < kAccN; ++i) tot[i] = (long long)atomicAdd(&ba.v[i], 0ull);
   GrowCtl* ctl = a.ctl;
-  if (acc[kAccChanged]) atomicAdd(&ctl->changed[rs.r % 3], (int32_t)acc[kAccChanged]);
-  if (acc[kAccImproved]) atomicAdd(&a.ctr->states, (unsigned long long)acc[kAccImproved]);
-  if (acc[kAccOverflow]) atomicExch(&a.ctr->overflow, 1);
+  if (tot[kAccChanged]) atomicAdd(&ctl->changed[rs.r % 3], (int32_t)tot[kAccChanged]);
+  if (tot[kAccImproved]) atomicAdd(&a.ctr->states, (unsigned long long)tot[kAccImproved]);
+  if (tot[kAccOverflow]) atomicExch(&a.ctr->overflow, 1);
   if (rs.stats) {
     const long long m = a.m, s = a.stride;
-    add_stat(a.stats, kStatVertices, acc[kAccVert]);
-    add_stat(a.stats, kStatEntries, acc[kAccEnt]);
-    add_stat(a.stats, kStatRows, acc[kAccRows]);
-    add_stat(a.stats, kStatGathered, acc[kAccRows] * m);
-    add_stat(a.stats, kStatImproved, acc[kAccImproved]);
+    add_stat(a.stats, kStatVertices, tot[kAccVert]);
+    add_stat(a.stats, kStatEntries, tot[kAccEnt]);
+    add_stat(a.stats, kStatRows, tot[kAccRows]);
+    add_stat(a.stats, kStatGathered, tot[kAccRows] * m);
+    add_stat(a.stats, kStatImproved, tot[kAccImproved]);
     // algorithmic bytes: per processed vertex the row_ptr pair, its own row
     // and its candidate byte; per CSR entry scanned (col,w) and, in sparse
     // rounds, the change flag; one neighbour row per gather; the parent per
@@ -261,9 +346,18 @@ __device__ __forceinline__ void round_end(const LevelArgs& a, const RoundState& 
     // (col,w) + a candidate byte per mark
     const long long flag_bytes = rs.dense ? 0 : 1;
     add_stat(a.stats, kStatBytes,
-             acc[kAccVert] * (9 + 4 * s) + acc[kAccEnt] * (8 + flag_bytes) + acc[kAccRows] * 4 * s +
-                 acc[kAccImproved] * 4 + acc[kAccChanged] * (4 * s + 1) + acc[kAccMarks] * 9);
+             tot[kAccVert] * (9 + 4 * s) + tot[kAccEnt] * (8 + flag_bytes) + tot[kAccRows] * 4 * s +
+                 tot[kAccImproved] * 4 + tot[kAccChanged] * (4 * s + 1) + tot[kAccMarks] * 9);
   }
+  return true;
+}
+
+// round_flush, then the last block of the round kernel publishes the
+// round's change count and advances the round.
+__device__ __forceinline__ void round_end(const LevelArgs& a, const RoundState& rs, uint32_t (&acc)[kAccN],
+                                          BlockAcc& ba) {
+  if (!round_flush(a, rs, acc, ba)) return;
+  GrowCtl* ctl = a.ctl;
   __threadfence();
   const uint32_t t = atomicAdd(&ctl->done, 1u);
   if (t != gridDim.x - 1) return;
@@ -291,7 +385,7 @@ template <int G, int L>
 __device__ __forceinline__ void group_relax(const GraphDev& g, const LevelArgs& a, const RoundState& rs, int32_t e0,
                                             int32_t end, int jc, int glane, int gbase, unsigned gmask_lanes,
                                             unsigned gbits, int32_t (&best)[L], int32_t (&code)[L],
-                                            long long (&acc)[kAccN]) {
+                                            uint32_t (&acc)[kAccN]) {
   const int32_t e = e0 + glane;
   int32_t nv = 0, nw = 0;
   bool act = false;
@@ -325,7 +419,7 @@ __device__ __forceinline__ void group_relax(const GraphDev& g, const LevelArgs& 
 #pragma unroll
       for (int t = 0; t < L; ++t) {
         const int j = glane + t * G;
-        c[i][t] = (src[i] >= 0 && jc + j < s) ? a.cost[rowv + j] : kInf;
+        c[i][t] = (src[i] >= 0 && jc + j < s) ? light_or_inf(a.cost[rowv + j], rs.ub_light) : kInf;
       }
     }
 #pragma unroll
@@ -353,11 +447,13 @@ __device__ __forceinline__ void group_relax(const GraphDev& g, const LevelArgs& 
 // a 64-bit atomicMin of (cost << 32 | CSR entry), and counts the chunk as
 // done; the warp that finishes a hub's last chunk applies the scratch row
 // to the hub's state row (its single writer), clears the scratch row and
-// the counter for the next round, and marks the hub's neighbours. No warp
-// ever waits for another.
+// the counter for the next round and flags the hub as changed. No warp
+// ever waits for another. This runs as a kernel of its own before the
+// round kernel, which then marks the changed hubs' neighbours chunk by
+// chunk (hub_mark), so no single warp walks a whole hub row.
 template <int L>
-__device__ __forceinline__ void hub_chunks(const GraphDev& g, const LevelArgs& a, const RoundState& rs,
-                                           long long (&acc)[kAccN]) {
+__device__ __forceinline__ void hub_relax(const GraphDev& g, const LevelArgs& a, const RoundState& rs,
+                                          uint32_t (&acc)[kAccN]) {
   constexpr int G = 32;
   constexpr int CH = G * L;
   const int lane = threadIdx.x & 31;
@@ -411,154 +507,303 @@ __device__ __forceinline__ void hub_chunks(const GraphDev& g, const LevelArgs& a
       atomicExch(g.hub_cnt + hc.x, 0);
       ++acc[kAccVert];
     }
-    if (__ballot_sync(0xffffffffu, imp)) {
-      if (!rs.dense) {
-        for (int32_t e = beg + lane; e < end; e += G) {
-          rs.cand_next[g.adj[e].x] = 1;
-          ++acc[kAccMarks];
-        }
-      }
-      if (lane == 0) {
-        rs.next_flag[u] = 1;
-        ++acc[kAccChanged];
-      }
+    if (__ballot_sync(0xffffffffu, imp) && lane == 0) {
+      rs.next_flag[u] = 1;
+      ++acc[kAccChanged];
     }
+  }
+}
+
+// Sparse rounds: for every hub that changed in this round's hub kernel, the
+// warp that takes one of its 32-entry chunks marks the chunk's neighbours
+// that the hub's new row improves (within their bound). Lanes read the
+// hub's row at the same addresses (broadcast loads).
+__device__ __forceinline__ void hub_mark(const GraphDev& g, const LevelArgs& a, const RoundState& rs,
+                                         uint32_t (&acc)[kAccN]) {
+  if (rs.dense) return;
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int32_t s = a.stride;
+  for (int64_t c = warp; c < g.nchunks; c += nwarps) {
+    const int2 hc = g.hub_chunk[c];
+    const int32_t u = g.big[hc.x];
+    if (!rs.next_flag[u]) continue;
+    const int32_t e = hc.y + lane;
+    if (e >= g.row_ptr[u + 1]) continue;
+    const int2 x = g.adj[e];
+    const int32_t* hv = a.cost + a.base + (int64_t)u * s;
+    const int32_t* yv = a.cost + a.base + (int64_t)x.x * s;
+    if (improves_row(a, rs.ub, x.x, x.y, [&](int j) { return light_or_inf(hv[j], rs.ub_light); },
+                     [&](int j) { return yv[j]; }, a.m))
+      mark_candidate(rs.cand_next, x.x, acc);
   }
 }
 
 }  // namespace
 
+// --------------------------------------------------------------- seeding --
+// Chooses how round 0 of a wave starts. When the merge left more than
+// V >> dense_shift vertices with a finite state, round 0 is dense.
+// Otherwise only neighbours that a light finite merged state can improve
+// (within their bound) become round 0's candidates. Hub rows are walked a
+// 32-entry chunk per warp; the other vertices 32 at a time per warp, which
+// finds those with a light state by ballot and walks each one's (at most
+// kDegBig) neighbours with its 32 lanes.
+__global__ void __launch_bounds__(kGrowThreads) k_seed(GraphDev g, LevelArgs a) {
+  GrowCtl* ctl = a.ctl;
+  if (ctl->changed[2] > (g.V >> a.params->dense_shift)) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) ctl->dense[2] = 1;
+    return;
+  }
+  const int32_t ub_light = a.params->ub;
+  const int32_t ub = a.level >= 2 ? a.params->ub : 0;
+  uint8_t* cand0 = a.cand;  // candidates of round 0
+  uint32_t acc[kAccN] = {0, 0, 0, 0, 0, 0, 0};
+  const int32_t s = a.stride;
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  auto seed_entry = [&](const int32_t* hv, int32_t e) {
+    const int2 x = g.adj[e];
+    const int32_t* yu = a.cost + a.base + (int64_t)x.x * s;
+    if (improves_row(a, ub, x.x, x.y, [&](int j) { return light_or_inf(hv[j], ub_light); },
+                     [&](int j) { return yu[j]; }, a.m))
+      mark_candidate(cand0, x.x, acc);
+  };
+  for (int64_t c = warp; c < g.nchunks; c += nwarps) {
+    const int2 hc = g.hub_chunk[c];
+    const int32_t u = g.big[hc.x];
+    const int32_t* hv = a.cost + a.base + (int64_t)u * s;
+    bool light = false;
+    for (int j = lane; j < a.m; j += 32) light |= light_or_inf(hv[j], ub_light) < kInf;
+    if (!__any_sync(0xffffffffu, light)) continue;
+    const int32_t e = hc.y + lane;
+    if (e < g.row_ptr[u + 1]) seed_entry(hv, e);
+  }
+  for (int64_t vbase = warp * 32; vbase < g.V; vbase += nwarps * 32) {
+    const int64_t vl = vbase + lane;
+    bool light = false;
+    if (vl < g.V && g.row_ptr[vl + 1] - g.row_ptr[vl] <= kDegBig) {
+      const int32_t* hv = a.cost + a.base + vl * s;
+      for (int j = 0; j < a.m; ++j) light |= light_or_inf(hv[j], ub_light) < kInf;
+    }
+    unsigned lm = __ballot_sync(0xffffffffu, light);
+    while (lm) {
+      const int32_t v = (int32_t)(vbase + __ffs(lm) - 1);
+      lm &= lm - 1u;
+      const int32_t* hv = a.cost + a.base + (int64_t)v * s;
+      const int32_t end = g.row_ptr[v + 1];
+      for (int32_t e = g.row_ptr[v] + lane; e < end; e += 32) seed_entry(hv, e);
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) ctl->dense[2] = 0;
+}
+
+// Hub relaxation of a sparse round (hub_relax), ahead of the round kernel,
+// which then marks the changed hubs' neighbours. Dense rounds mark nothing
+// and relax the hubs inside the round kernel, beside the other vertices.
+template <int L>
+__global__ void __launch_bounds__(kGrowThreads) k_grow_hubs(GraphDev g, LevelArgs a) {
+  RoundState rs;
+  if (!round_begin(g, a, rs) || rs.dense) return;
+  __shared__ BlockAcc ba;
+  block_acc_init(ba);
+  uint32_t acc[kAccN] = {0, 0, 0, 0, 0, 0, 0};
+  hub_relax<L>(g, a, rs, acc);
+  round_flush(a, rs, acc, ba);
+}
+
 // Thread per vertex: the vertex's MP-entry row lives in registers.
+template <int MP>
+__device__ __forceinline__ void thread_vertex(const GraphDev& g, const LevelArgs& a, const RoundState& rs,
+                                              int32_t u, uint32_t (&acc)[kAccN]) {
+  constexpr int U = MP <= 8 ? 4 : 2;
+  constexpr int Q = MP / 4;
+  const int32_t beg = g.row_ptr[u], end = g.row_ptr[u + 1];
+  if (end - beg > kDegBig) return;  // hub: handled in 32-entry chunks
+  int4* rowc = reinterpret_cast<int4*>(a.cost + a.base + (int64_t)u * MP);
+  int32_t best[MP];
+  // parent of entry j as (CSR entry - beg), one byte each (rows are at most
+  // kDegBig long); 0xff = unchanged
+  uint32_t code[Q];
+#pragma unroll
+  for (int q = 0; q < Q; ++q) {
+    const int4 x = rowc[q];
+    best[4 * q] = x.x;
+    best[4 * q + 1] = x.y;
+    best[4 * q + 2] = x.z;
+    best[4 * q + 3] = x.w;
+    code[q] = 0xffffffffu;
+  }
+  bool live = false;
+#pragma unroll
+  for (int j = 0; j < MP; ++j) live |= j < a.m && best[j] != 0;  // cost-0 states cannot improve
+  ++acc[kAccVert];
+  acc[kAccEnt] += end - beg;
+  if (!live) return;
+  for (int32_t e0 = beg; e0 < end; e0 += U) {
+    int32_t nv[U], nw[U];
+    bool act[U];
+#pragma unroll
+    for (int i = 0; i < U; ++i) {
+      act[i] = e0 + i < end;
+      nv[i] = 0;
+      nw[i] = 0;
+      if (act[i]) {
+        const int2 x = g.adj[e0 + i];
+        nv[i] = x.x;
+        nw[i] = x.y;
+      }
+    }
+    if (!rs.dense) {
+#pragma unroll
+      for (int i = 0; i < U; ++i) act[i] = act[i] && rs.cur_flag[nv[i]] != 0;
+    }
+    int32_t rows[U][MP];
+#pragma unroll
+    for (int i = 0; i < U; ++i) {
+      if (act[i]) {
+        ++acc[kAccRows];
+        const int4* rv = reinterpret_cast<const int4*>(a.cost + a.base + (int64_t)nv[i] * MP);
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+          const int4 x = rv[q];
+          rows[i][4 * q] = x.x;
+          rows[i][4 * q + 1] = x.y;
+          rows[i][4 * q + 2] = x.z;
+          rows[i][4 * q + 3] = x.w;
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < MP; ++j) rows[i][j] = kInf;
+      }
+    }
+    // a kInf (or heavy) row entry gives c >= kInf and never wins; rows hold
+    // values below ovf_limit (checked when stored), so c cannot wrap or
+    // reach kInf from a finite entry
+#pragma unroll
+    for (int i = 0; i < U; ++i) {
+      const uint32_t rel = (uint32_t)(e0 + i - beg);
+#pragma unroll
+      for (int j = 0; j < MP; ++j) {
+        const int32_t c = light_or_inf(rows[i][j], rs.ub_light) + nw[i];
+        const bool lt = c < best[j];
+        best[j] = lt ? c : best[j];
+        const int sh = 8 * (j & 3);
+        code[j >> 2] = lt ? ((code[j >> 2] & ~(0xffu << sh)) | (rel << sh)) : code[j >> 2];
+      }
+    }
+  }
+  bool any = false;
+#pragma unroll
+  for (int j = 0; j < MP; ++j) {
+    const int sh = 8 * (j & 3);
+    const bool imp = ((code[j >> 2] >> sh) & 0xffu) != 0xffu;
+    if (imp && best[j] >= rs.ovf_limit) acc[kAccOverflow] = 1;
+    if (imp && rs.ub > 0 && best[j] > prune_cap(a, rs.ub, u, (uint32_t)__ldg(a.lmasks + j))) {
+      best[j] = a.cost[a.base + (int64_t)u * MP + j];  // keep the stored value
+      code[j >> 2] |= 0xffu << sh;
+    }
+    any |= ((code[j >> 2] >> sh) & 0xffu) != 0xffu;
+  }
+  if (!any) return;
+#pragma unroll
+  for (int q = 0; q < Q; ++q) rowc[q] = make_int4(best[4 * q], best[4 * q + 1], best[4 * q + 2], best[4 * q + 3]);
+  int32_t* rowp = a.par + a.base + (int64_t)u * MP;
+#pragma unroll
+  for (int j = 0; j < MP; ++j) {
+    const uint32_t rel = (code[j >> 2] >> (8 * (j & 3))) & 0xffu;
+    if (rel != 0xffu) {
+      rowp[j] = beg + (int32_t)rel;
+      ++acc[kAccImproved];
+    }
+  }
+  rs.next_flag[u] = 1;
+  ++acc[kAccChanged];
+  if (rs.dense) return;  // the next round sweeps every vertex
+  // mark a neighbour only if the new row improves it for some mask (within
+  // its bound): its row can only decrease later, so an unmarked neighbour
+  // never needs this row
+#pragma unroll
+  for (int j = 0; j < MP; ++j) best[j] = light_or_inf(best[j], rs.ub_light);
+  for (int32_t e = beg; e < end; ++e) {
+    const int2 x = g.adj[e];
+    const int4* rv = reinterpret_cast<const int4*>(a.cost + a.base + (int64_t)x.x * MP);
+    uint32_t bits = 0;  // masks the new row improves at x
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+      const int4 t = rv[q];
+      bits |= (best[4 * q] + x.y < t.x ? 1u : 0u) << (4 * q);
+      bits |= (best[4 * q + 1] + x.y < t.y ? 1u : 0u) << (4 * q + 1);
+      bits |= (best[4 * q + 2] + x.y < t.z ? 1u : 0u) << (4 * q + 2);
+      bits |= (best[4 * q + 3] + x.y < t.w ? 1u : 0u) << (4 * q + 3);
+    }
+    bool better = bits != 0;
+    if (better && rs.ub > 0) {  // the same test under x's one-label caps
+      int32_t dd[16];
+      load_label_bound(a, rs.ub, x.x, dd);
+      better = false;
+#pragma unroll
+      for (int j = 0; j < MP; ++j)
+        better |= ((bits >> j) & 1u) && best[j] + x.y + label_bound(dd, (uint32_t)__ldg(a.lmasks + j)) <= rs.ub;
+    }
+    if (better) mark_candidate(rs.cand_next, x.x, acc);
+  }
+}
+
 template <int MP>
 __global__ void __launch_bounds__(kGrowThreads, (MP <= 16 ? 3 : 2)) k_grow_thread(GraphDev g, LevelArgs a) {
   RoundState rs;
   if (!round_begin(g, a, rs)) return;
   __shared__ BlockAcc ba;
   block_acc_init(ba);
-  long long acc[kAccN] = {0, 0, 0, 0, 0, 0, 0};
-  constexpr int U = MP <= 8 ? 4 : 2;
-  constexpr int Q = MP / 4;
+  uint32_t acc[kAccN] = {0, 0, 0, 0, 0, 0, 0};
   const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = t0; i < g.V; i += nthreads) {
     rs.clear_flag[i] = 0;
     rs.cand_clear[i] = 0;
   }
-  hub_chunks<(MP + 31) / 32>(g, a, rs, acc);
-  {
-    // vertices by decreasing degree: a warp's lanes walk rows of similar
-    // length, and the longest rows start first
-    // odd rounds sweep backwards: in-place updates then also carry along
-    // the order in the other direction within one round
-    for (int64_t i = t0; i < g.nsmall; i += nthreads) {
-      const int32_t u = g.order[(rs.r & 1) ? g.nsmall - 1 - i : i];
-      if (!rs.all_cand && !rs.cand_cur[u]) continue;
-      const int32_t beg = g.row_ptr[u], end = g.row_ptr[u + 1];
-      int4* rowc = reinterpret_cast<int4*>(a.cost + a.base + (int64_t)u * MP);
-      int32_t best[MP];
-      // parent of entry j as (CSR entry - beg), one byte each (rows are at
-      // most kDegBig long); 0xff = unchanged
-      uint32_t code[Q];
+  if (rs.dense)
+    hub_relax<(MP + 31) / 32>(g, a, rs, acc);
+  else
+    hub_mark(g, a, rs, acc);
+  if (rs.all_cand) {
+    // every vertex; odd rounds sweep backwards, so in-place updates also
+    // carry along the order in the other direction within one round
+    for (int64_t i = t0; i < g.nsmall; i += nthreads)
+      thread_vertex<MP>(g, a, rs, g.order[(rs.r & 1) ? g.nsmall - 1 - i : i], acc);
+  } else {
+    // candidates only: a warp reads 512 candidate bytes at a time (16 per
+    // lane, one int4), compacts the set ones in shared memory and its lanes
+    // take them in turn
+    __shared__ int32_t tile[kGrowThreads / 32][kCandTile];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int64_t warp = t0 >> 5, nwarps = nthreads >> 5;
+    static_assert(kCandTile == 16 * 32, "a lane reads 16 flag bytes");
+    for (int64_t base = warp * kCandTile; base < g.V; base += nwarps * kCandTile) {
+      const int64_t v0 = base + 16 * lane;
+      uint4 f = make_uint4(0, 0, 0, 0);
+      if (v0 < g.V) f = *reinterpret_cast<const uint4*>(rs.cand_cur + v0);  // arrays padded to 16 bytes
+      const uint32_t w4[4] = {f.x, f.y, f.z, f.w};
+      int cnt = 0;
 #pragma unroll
-      for (int q = 0; q < Q; ++q) {
-        const int4 x = rowc[q];
-        best[4 * q] = x.x;
-        best[4 * q + 1] = x.y;
-        best[4 * q + 2] = x.z;
-        best[4 * q + 3] = x.w;
-        code[q] = 0xffffffffu;
+      for (int b = 0; b < 16; ++b) cnt += ((w4[b >> 2] >> (8 * (b & 3))) & 0xffu) != 0;
+      int pre = cnt;  // inclusive prefix over lanes
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, pre, o);
+        if (lane >= o) pre += t;
       }
-      bool live = false;
+      const int total = __shfl_sync(0xffffffffu, pre, 31);
+      int pos = pre - cnt;
 #pragma unroll
-      for (int j = 0; j < MP; ++j) live |= j < a.m && best[j] != 0;  // cost-0 states cannot improve
-      ++acc[kAccVert];
-      acc[kAccEnt] += end - beg;
-      if (!live) continue;
-      for (int32_t e0 = beg; e0 < end; e0 += U) {
-        int32_t nv[U], nw[U];
-        bool act[U];
-#pragma unroll
-        for (int i = 0; i < U; ++i) {
-          act[i] = e0 + i < end;
-          nv[i] = 0;
-          nw[i] = 0;
-          if (act[i]) {
-            const int2 x = g.adj[e0 + i];
-            nv[i] = x.x;
-            nw[i] = x.y;
-          }
-        }
-        if (!rs.dense) {
-#pragma unroll
-          for (int i = 0; i < U; ++i) act[i] = act[i] && rs.cur_flag[nv[i]] != 0;
-        }
-        int32_t rows[U][MP];
-#pragma unroll
-        for (int i = 0; i < U; ++i) {
-          if (act[i]) {
-            ++acc[kAccRows];
-            const int4* rv = reinterpret_cast<const int4*>(a.cost + a.base + (int64_t)nv[i] * MP);
-#pragma unroll
-            for (int q = 0; q < Q; ++q) {
-              const int4 x = rv[q];
-              rows[i][4 * q] = x.x;
-              rows[i][4 * q + 1] = x.y;
-              rows[i][4 * q + 2] = x.z;
-              rows[i][4 * q + 3] = x.w;
-            }
-          } else {
-#pragma unroll
-            for (int j = 0; j < MP; ++j) rows[i][j] = kInf;
-          }
-        }
-        // a kInf row entry gives c >= kInf and never wins; rows hold values
-        // below ovf_limit (checked when stored), so c cannot wrap or reach
-        // kInf from a finite entry
-#pragma unroll
-        for (int i = 0; i < U; ++i) {
-          const uint32_t rel = (uint32_t)(e0 + i - beg);
-#pragma unroll
-          for (int j = 0; j < MP; ++j) {
-            const int32_t c = rows[i][j] + nw[i];
-            const bool lt = c < best[j];
-            best[j] = lt ? c : best[j];
-            const int sh = 8 * (j & 3);
-            code[j >> 2] = lt ? ((code[j >> 2] & ~(0xffu << sh)) | (rel << sh)) : code[j >> 2];
-          }
-        }
-      }
-      bool any = false;
-#pragma unroll
-      for (int j = 0; j < MP; ++j) {
-        const int sh = 8 * (j & 3);
-        const bool imp = ((code[j >> 2] >> sh) & 0xffu) != 0xffu;
-        if (imp && best[j] >= rs.ovf_limit) acc[kAccOverflow] = 1;
-        if (imp && rs.ub > 0 && best[j] > prune_cap(a, rs.ub, u, (uint32_t)__ldg(a.lmasks + j))) {
-          best[j] = a.cost[a.base + (int64_t)u * MP + j];  // keep the stored value
-          code[j >> 2] |= 0xffu << sh;
-        }
-        any |= ((code[j >> 2] >> sh) & 0xffu) != 0xffu;
-      }
-      if (!any) continue;
-#pragma unroll
-      for (int q = 0; q < Q; ++q) rowc[q] = make_int4(best[4 * q], best[4 * q + 1], best[4 * q + 2], best[4 * q + 3]);
-      int32_t* rowp = a.par + a.base + (int64_t)u * MP;
-#pragma unroll
-      for (int j = 0; j < MP; ++j) {
-        const uint32_t rel = (code[j >> 2] >> (8 * (j & 3))) & 0xffu;
-        if (rel != 0xffu) {
-          rowp[j] = beg + (int32_t)rel;
-          ++acc[kAccImproved];
-        }
-      }
-      rs.next_flag[u] = 1;
-      ++acc[kAccChanged];
-      if (!rs.dense) {
-        for (int32_t e = beg; e < end; ++e) {
-          rs.cand_next[g.adj[e].x] = 1;
-          ++acc[kAccMarks];
-        }
-      }
+      for (int b = 0; b < 16; ++b)
+        if (((w4[b >> 2] >> (8 * (b & 3))) & 0xffu) != 0) tile[wib][pos++] = (int32_t)(v0 + b);
+      __syncwarp();
+      for (int i = lane; i < total; i += 32) thread_vertex<MP>(g, a, rs, tile[wib][i], acc);
+      __syncwarp();
     }
   }
   round_end(a, rs, acc, ba);
@@ -573,7 +818,7 @@ __global__ void __launch_bounds__(kGrowThreads, (L >= 3 ? 3 : 4)) k_grow_group(G
   if (!round_begin(g, a, rs)) return;
   __shared__ BlockAcc ba;
   block_acc_init(ba);
-  long long acc[kAccN] = {0, 0, 0, 0, 0, 0, 0};
+  uint32_t acc[kAccN] = {0, 0, 0, 0, 0, 0, 0};
   {
     const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
@@ -582,7 +827,10 @@ __global__ void __launch_bounds__(kGrowThreads, (L >= 3 ? 3 : 4)) k_grow_group(G
       rs.cand_clear[i] = 0;
     }
   }
-  hub_chunks<((G * L + 31) / 32 < 4 ? (G * L + 31) / 32 : 4)>(g, a, rs, acc);
+  if (rs.dense)
+    hub_relax<((G * L + 31) / 32 < 4 ? (G * L + 31) / 32 : 4)>(g, a, rs, acc);
+  else
+    hub_mark(g, a, rs, acc);
   {
     const int tid = threadIdx.x, lane = tid & 31;
     const int glane = lane & (G - 1), gbase = lane & ~(G - 1);
@@ -635,10 +883,7 @@ __global__ void __launch_bounds__(kGrowThreads, (L >= 3 ? 3 : 4)) k_grow_group(G
           imp_any |= (__ballot_sync(gmask_lanes, imp) & gmask_lanes) != 0;
         }
         if (imp_any && !rs.dense) {
-          for (int32_t e = beg + glane; e < end; e += G) {
-            rs.cand_next[g.adj[e].x] = 1;
-            ++acc[kAccMarks];
-          }
+          for (int32_t e = beg + glane; e < end; e += G) mark_candidate(rs.cand_next, g.adj[e].x, acc);
         }
         if (glane == 0) {
           ++acc[kAccVert];
@@ -755,9 +1000,9 @@ __global__ void __launch_bounds__(256) k_backtrack(GraphDev g, int64_t nnz, cons
 }
 
 // ---------------------------------------------------------------- launchers --
-cudaError_t launch_group_masks(const int32_t* group_ptr, const int32_t* members, int32_t k, uint32_t* gmask,
-                               cudaStream_t stream) {
-  k_group_masks<<<64, 256, 0, stream>>>(group_ptr, members, k, gmask);
+cudaError_t launch_group_masks(const int32_t* group_ptr, const int32_t* members, const int32_t* perm, int32_t k,
+                               uint32_t* gmask, cudaStream_t stream) {
+  k_group_masks<<<64, 256, 0, stream>>>(group_ptr, members, perm, k, gmask);
   return cudaGetLastError();
 }
 
@@ -789,6 +1034,18 @@ cudaError_t launch_round(Kernel kern, int occ, const GraphDev& g, const LevelArg
   return cudaGetLastError();
 }
 
+template <int L>
+cudaError_t hub_round(const GraphDev& g, const LevelArgs& a, int num_sms, cudaStream_t stream, int64_t* launches) {
+  if (g.nchunks == 0) return cudaSuccess;
+  static const int occ = resident_blocks(k_grow_hubs<L>);
+  const int64_t warps_per_block = kGrowThreads / 32;
+  int64_t blocks = (g.nchunks + warps_per_block - 1) / warps_per_block;
+  if (blocks > (int64_t)num_sms * occ) blocks = (int64_t)num_sms * occ;
+  k_grow_hubs<L><<<(unsigned)blocks, kGrowThreads, 0, stream>>>(g, a);
+  ++*launches;
+  return cudaGetLastError();
+}
+
 template <int MP>
 cudaError_t thread_round(const GraphDev& g, const LevelArgs& a, int num_sms, cudaStream_t stream) {
   static const int occ = resident_blocks(k_grow_thread<MP>);
@@ -802,7 +1059,15 @@ cudaError_t group_round(const GraphDev& g, const LevelArgs& a, int num_sms, cuda
 }
 }  // namespace
 
-cudaError_t launch_grow_round(const GraphDev& g, const LevelArgs& a, int num_sms, cudaStream_t stream) {
+cudaError_t launch_grow_round(const GraphDev& g, const LevelArgs& a, int num_sms, cudaStream_t stream,
+                              int64_t* launches) {
+  const int lanes = (a.stride + 31) / 32;  // masks per lane in the hub kernel, in passes of at most 4
+  const cudaError_t he = lanes <= 1   ? hub_round<1>(g, a, num_sms, stream, launches)
+                         : lanes == 2 ? hub_round<2>(g, a, num_sms, stream, launches)
+                         : lanes == 3 ? hub_round<3>(g, a, num_sms, stream, launches)
+                                      : hub_round<4>(g, a, num_sms, stream, launches);
+  if (he != cudaSuccess) return he;
+  ++*launches;
   switch (a.stride) {
     case 4: return thread_round<4>(g, a, num_sms, stream);
     case 8: return thread_round<8>(g, a, num_sms, stream);
@@ -816,6 +1081,13 @@ cudaError_t launch_grow_round(const GraphDev& g, const LevelArgs& a, int num_sms
   if (a.stride <= 64) return group_round<32, 2>(g, a, num_sms, stream);
   if (a.stride <= 96) return group_round<32, 3>(g, a, num_sms, stream);
   return group_round<32, 4>(g, a, num_sms, stream);
+}
+
+cudaError_t launch_seed(const GraphDev& g, const LevelArgs& a, int num_sms, cudaStream_t stream) {
+  int64_t blocks = ((int64_t)g.V + kGrowThreads - 1) / kGrowThreads;  // >= one warp per 32 vertices
+  if (blocks > (int64_t)num_sms * 8) blocks = (int64_t)num_sms * 8;
+  k_seed<<<(unsigned)blocks, kGrowThreads, 0, stream>>>(g, a);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_argmin(const GraphDev& g, const int32_t* full_slice, int32_t stride, Counters* ctr,

@@ -91,7 +91,7 @@ struct Workspace {
   int32_t* cost = nullptr;    // V * sum of row strides
   int32_t* par = nullptr;
   uint32_t* gmask = nullptr;  // V
-  uint8_t* flags = nullptr;   // 6 * V: change flags x3, candidate flags x3
+  uint8_t* flags = nullptr;   // 6 * vpad: change flags x3, candidate flags x3
   Counters* ctr = nullptr;
   GrowCtl* ctl = nullptr;
   SolveParams* d_params = nullptr;
@@ -137,6 +137,9 @@ struct gst_graph {
   int2* d_hub_chunk = nullptr;  // (hub index, first CSR entry) per 32-entry chunk of a hub row
   int64_t nchunks = 0;
   int32_t max_w = 0;  // largest edge weight
+  // Internal vertex IDs: perm[caller ID] and its inverse (see gst_graph_upload)
+  std::vector<int32_t> perm, inv;
+  int32_t* d_perm = nullptr;
   std::mutex mu;
   Workspace ws;
 };
@@ -220,6 +223,10 @@ void free_workspace(Workspace& ws) {
   ws.bt_cap = 0;
 }
 
+// Stride of the flag arrays: V rounded up to 16 bytes, so word atomics on
+// candidate bytes stay aligned in every array.
+int64_t vpad_of(int64_t V) { return (V + 15) & ~int64_t(15); }
+
 // Row strides of every level for k groups; returns their sum.
 int64_t total_stride(int32_t k) {
   int64_t s = 0;
@@ -233,7 +240,7 @@ gst_status ensure_workspace(gst_graph* g, int32_t k, int64_t nmembers) {
   const int64_t V = g->V;
   if (!ws.gmask) {
     GST_CUDA(cudaMalloc(&ws.gmask, V * sizeof(uint32_t)));
-    GST_CUDA(cudaMalloc(&ws.flags, 6 * V));
+    GST_CUDA(cudaMalloc(&ws.flags, 6 * (size_t)vpad_of(V)));
     GST_CUDA(cudaMalloc(&ws.ctr, sizeof(Counters)));
     GST_CUDA(cudaMalloc(&ws.ctl, sizeof(GrowCtl)));
     GST_CUDA(cudaMalloc(&ws.d_params, sizeof(SolveParams)));
@@ -348,8 +355,9 @@ LevelArgs level_args(gst_graph* g, int32_t k, int32_t l) {
   a.cost = ws.cost;
   a.par = ws.par;
   a.gmask = ws.gmask;
+  a.vpad = (int32_t)vpad_of(g->V);
   a.flags = ws.flags;
-  a.cand = ws.flags + 3 * (int64_t)g->V;
+  a.cand = ws.flags + 3 * vpad_of(g->V);
   a.ctl = ws.ctl;
   a.ctr = ws.ctr;
   a.stats = ws.stats;
@@ -369,7 +377,7 @@ gst_status enqueue_prologue(gst_graph* g, int32_t k, cudaStream_t s, int64_t* la
     GST_CUDA(cudaMemsetAsync(ws.hub_min, 0xff, (size_t)g->nbig * ws.hub_stride * sizeof(unsigned long long), s));
     GST_CUDA(cudaMemsetAsync(ws.hub_cnt, 0, (size_t)g->nbig * sizeof(int32_t), s));
   }
-  GST_CUDA(launch_group_masks(ws.d_group_ptr, ws.d_members, k, ws.gmask, s));
+  GST_CUDA(launch_group_masks(ws.d_group_ptr, ws.d_members, g->d_perm, k, ws.gmask, s));
   ++*launches;
   return GST_OK;
 }
@@ -377,10 +385,14 @@ gst_status enqueue_prologue(gst_graph* g, int32_t k, cudaStream_t s, int64_t* la
 // Wave l's merge, preceded by the reset of its flags and loop control.
 gst_status enqueue_merge(gst_graph* g, const LevelArgs& a, cudaStream_t s, int64_t* launches) {
   Workspace& ws = g->ws;
-  GST_CUDA(cudaMemsetAsync(ws.flags, 0, 6 * (size_t)g->V, s));
+  GST_CUDA(cudaMemsetAsync(ws.flags, 0, 6 * (size_t)vpad_of(g->V), s));
   GST_CUDA(cudaMemsetAsync(ws.ctl, 0, sizeof(GrowCtl), s));
   GST_CUDA(launch_merge(graph_dev(g), a, s));
   ++*launches;
+  if (a.level < a.k) {  // how round 0 of the wave starts
+    GST_CUDA(launch_seed(graph_dev(g), a, g->num_sms, s));
+    ++*launches;
+  }
   return GST_OK;
 }
 
@@ -424,7 +436,8 @@ gst_status capture_growth_loop(gst_graph* g, LevelArgs a, cudaStream_t s) {
   a.cond = h;
   a.use_cond = 1;
   GST_CUDA(cudaStreamBeginCaptureToGraph(g->side, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
-  const cudaError_t le = launch_grow_round(graph_dev(g), a, g->num_sms, g->side);
+  int64_t body_launches = 0;
+  const cudaError_t le = launch_grow_round(graph_dev(g), a, g->num_sms, g->side, &body_launches);
   cudaGraph_t done = nullptr;
   const cudaError_t ee = cudaStreamEndCapture(g->side, &done);
   GST_CUDA(le);
@@ -502,6 +515,13 @@ gst_status collect_tree(gst_graph* g, gst_result* r, int32_t cost, int32_t root)
       GST_CUDA(cudaMemcpyAsync(he.data(), ws.out_e, (size_t)ne * sizeof(int3), cudaMemcpyDeviceToHost, g->stream));
     GST_CUDA(cudaStreamSynchronize(g->stream));
   }
+  // back to caller IDs (the walk checked every ID against V)
+  for (auto& v : hv) v = g->inv[(size_t)v];
+  for (auto& e : he) {
+    e.x = g->inv[(size_t)e.x];
+    e.y = g->inv[(size_t)e.y];
+  }
+  root = g->inv[(size_t)root];
   std::sort(hv.begin(), hv.end());
   hv.erase(std::unique(hv.begin(), hv.end()), hv.end());
   std::vector<std::pair<std::pair<int32_t, int32_t>, int32_t>> es;
@@ -568,9 +588,8 @@ gst_status run_host_loop(gst_graph* g, int32_t k, int64_t* launches, bool* timeo
       for (int64_t r = 0;; r += batch) {
         for (int i = 0; i < batch; ++i) {
           if (trace) GST_CUDA(cudaEventRecord(ws.ev[kEvents - 2], s));
-          GST_CUDA(launch_grow_round(gd, a, g->num_sms, s));
+          GST_CUDA(launch_grow_round(gd, a, g->num_sms, s, launches));
           if (trace) GST_CUDA(cudaEventRecord(ws.ev[kEvents - 1], s));
-          ++*launches;
         }
         GST_CUDA(cudaMemcpyAsync(ws.h_ctl, ws.ctl, sizeof(GrowCtl), cudaMemcpyDeviceToHost, s));
         GST_CUDA(cudaStreamSynchronize(s));
@@ -614,6 +633,7 @@ gst_status solve_one(gst_graph* g, const int32_t* group_ptr, const int32_t* memb
   ws.h_params->stats_on = o.collect_stats ? 1 : 0;
   ws.h_params->k = k;
   ws.h_params->ovf_limit = kInf - std::max<int32_t>(g->max_w, 1);
+  ws.h_params->dense_shift = o.dense_shift > 0 && o.dense_shift < 31 ? o.dense_shift : kDefaultDenseShift;
 
   GST_CUDA(cudaEventRecord(ws.ev[0], s));
   GST_CUDA(cudaMemcpyAsync(ws.d_params, ws.h_params, sizeof(SolveParams), cudaMemcpyHostToDevice, s));
@@ -635,7 +655,7 @@ gst_status solve_one(gst_graph* g, const int32_t* group_ptr, const int32_t* memb
   GST_CUDA(cudaEventRecord(ws.ev[2], s));
   GST_CUDA(cudaStreamSynchronize(s));
   const Counters& c = *ws.h_ctr;
-  if (use_graph) launches = 1 + k + c.rounds_total + 2;
+  if (use_graph) launches = 1 + k + (k - 1) + (int64_t)c.rounds_total * (g->nchunks > 0 ? 2 : 1) + 2;
   r->launches = launches;
   r->states = (int64_t)c.states;
   std::copy(ws.h_stats, ws.h_stats + kNumStats, r->stats);
@@ -687,12 +707,10 @@ gst_status gst_graph_upload(const int32_t* row_ptr, const int32_t* col, const in
   if (row_ptr[0] != 0 || row_ptr[V] != nnz) return fail(GST_BAD_INPUT, "row_ptr[0] must be 0 and row_ptr[V] nnz");
   for (int32_t v = 0; v < V; ++v)
     if (row_ptr[v + 1] < row_ptr[v]) return fail(GST_BAD_INPUT, "row_ptr must be non-decreasing");
-  std::vector<int2> adj((size_t)nnz);
   int32_t max_w = 0;
   for (int64_t e = 0; e < nnz; ++e) {
     if (col[e] < 0 || col[e] >= V) return fail(GST_BAD_INPUT, "col entry out of range");
     if (w[e] < 0 || w[e] >= GST_COST_LIMIT) return fail(GST_BAD_INPUT, "weights must be in [0, GST_COST_LIMIT)");
-    adj[(size_t)e] = make_int2(col[e], w[e]);
     max_w = std::max(max_w, w[e]);
   }
   auto* g = new (std::nothrow) gst_graph;
@@ -700,6 +718,49 @@ gst_status gst_graph_upload(const int32_t* row_ptr, const int32_t* col, const in
   g->V = V;
   g->nnz = nnz;
   g->max_w = max_w;
+  // Relabelling. Sparse rounds give each warp a tile of kCandTile
+  // consecutive IDs, and a lane works through its share of the tile's
+  // candidates one vertex at a time, so a tile of high-degree vertices is a
+  // long serial tail (generators and real graphs alike tend to give the
+  // high-degree vertices neighbouring IDs). Vertices ranked by decreasing
+  // degree are cut into runs of kDealRun consecutive ranks, and the runs are
+  // dealt out over the tiles round-robin: a tile holds at most a run or two
+  // of the heaviest vertices (about one per lane), while the rows of
+  // similarly hot vertices stay side by side, sharing cache lines in the
+  // dense rounds' neighbour gathers.
+  constexpr int64_t kDealRun = 32;
+  static_assert(kCandTile % kDealRun == 0, "tiles hold whole runs");
+  const int32_t* rp = row_ptr;  // the caller's CSR
+  std::vector<int32_t> bydeg((size_t)V);
+  for (int32_t v = 0; v < V; ++v) bydeg[(size_t)v] = v;
+  std::stable_sort(bydeg.begin(), bydeg.end(),
+                   [&](int32_t a, int32_t b) { return rp[a + 1] - rp[a] > rp[b + 1] - rp[b]; });
+  g->perm.resize((size_t)V);
+  g->inv.resize((size_t)V);
+  {
+    const int64_t ntiles = ((int64_t)V + kCandTile - 1) / kCandTile;
+    size_t r = 0;
+    for (int64_t run = 0; run < kCandTile / kDealRun; ++run)
+      for (int64_t t = 0; t < ntiles; ++t)
+        for (int64_t i = 0; i < kDealRun; ++i) {
+          const int64_t id = t * kCandTile + run * kDealRun + i;
+          if (id >= V) continue;
+          const int32_t old = bydeg[r++];
+          g->perm[(size_t)old] = (int32_t)id;
+          g->inv[(size_t)id] = old;
+        }
+  }
+  // the CSR in internal IDs, each row's entries in the caller's order
+  std::vector<int32_t> nrow((size_t)V + 1);
+  std::vector<int2> adj((size_t)nnz);
+  nrow[0] = 0;
+  for (int32_t n = 0; n < V; ++n) {
+    const int32_t o = g->inv[(size_t)n];
+    int32_t pos = nrow[(size_t)n];
+    for (int32_t e = rp[o]; e < rp[o + 1]; ++e) adj[(size_t)pos++] = make_int2(g->perm[(size_t)col[e]], w[e]);
+    nrow[(size_t)n + 1] = pos;
+  }
+  row_ptr = nrow.data();
   // Growth order of the non-hub vertices: by decreasing degree within
   // windows of kOrderWindow consecutive IDs, so the 32 lanes of a warp walk
   // rows of similar length while a window's rows stay close in memory.
@@ -733,6 +794,7 @@ gst_status gst_graph_upload(const int32_t* row_ptr, const int32_t* col, const in
     return cudaMemcpyAsync(*dst, src, bytes, cudaMemcpyHostToDevice, g->stream);
   };
   if ((e = up((void**)&g->d_row_ptr, row_ptr, (size_t)(V + 1) * 4)) != cudaSuccess ||
+      (e = up((void**)&g->d_perm, g->perm.data(), (size_t)V * 4)) != cudaSuccess ||
       (e = up((void**)&g->d_adj, adj.data(), adj.size() * sizeof(int2))) != cudaSuccess ||
       (e = up((void**)&g->d_big, big.data(), big.size() * 4)) != cudaSuccess ||
       (e = up((void**)&g->d_order, order.data(), order.size() * 4)) != cudaSuccess ||
@@ -752,6 +814,7 @@ void gst_graph_free(gst_graph* g) {
   if (g->stream) cudaStreamSynchronize(g->stream);
   free_workspace(g->ws);
   dfree(g->d_row_ptr);
+  dfree(g->d_perm);
   dfree(g->d_adj);
   dfree(g->d_big);
   dfree(g->d_order);
@@ -852,7 +915,7 @@ gst_status gst_graph_debug_table(gst_graph* g, int32_t k, int32_t* out) {
     int32_t rank = 0;
     for (int32_t S = 1; S < (int32_t)W; ++S) {
       if (__builtin_popcount((unsigned)S) != l) continue;
-      for (int64_t v = 0; v < V; ++v) out[v * W + S] = dev[(size_t)(base + v * s + rank)];
+      for (int64_t v = 0; v < V; ++v) out[v * W + S] = dev[(size_t)(base + (int64_t)g->perm[(size_t)v] * s + rank)];
       ++rank;
     }
   }

@@ -49,7 +49,8 @@ class Opts(C.Structure):
         ("max_rounds", C.c_int32),
         ("use_graph", C.c_int32),
         ("collect_stats", C.c_int32),
-        ("reserved", C.c_int32 * 11),
+        ("dense_shift", C.c_int32),
+        ("reserved", C.c_int32 * 10),
     ]
 
 
@@ -191,13 +192,15 @@ def _read_result(r) -> Result:
     )
 
 
-def make_opts(upper_bound: int = 0, max_rounds: int = 0, use_graph: bool = False, collect_stats: bool = False) -> Opts:
+def make_opts(upper_bound: int = 0, max_rounds: int = 0, use_graph: bool = False, collect_stats: bool = False,
+              dense_shift: int = 0) -> Opts:
     o = Opts()
     o.struct_size = C.sizeof(Opts)
     o.upper_bound = int(upper_bound)
     o.max_rounds = int(max_rounds)
     o.use_graph = int(bool(use_graph))
     o.collect_stats = int(bool(collect_stats))
+    o.dense_shift = int(dense_shift)
     return o
 
 
@@ -246,13 +249,13 @@ class Graph:
         self.close()
 
     def solve(self, group_ptr, members=None, *, upper_bound=0, max_rounds=0, use_graph=False,
-              collect_stats=False, raise_on_error=True) -> Result:
+              collect_stats=False, dense_shift=0, raise_on_error=True) -> Result:
         """Solves one query. `group_ptr` may be a list of member lists."""
         if members is None:
             group_ptr, members = groups_to_csr(group_ptr)
         gp, mem = _i32(group_ptr), _i32(members)
         k = len(gp) - 1
-        o = make_opts(upper_bound, max_rounds, use_graph, collect_stats)
+        o = make_opts(upper_bound, max_rounds, use_graph, collect_stats, dense_shift)
         r = C.c_void_p()
         st = lib().gst_solve(self._h, _ptr(gp), _ptr(mem), k, C.byref(o), C.byref(r))
         msg = last_error()

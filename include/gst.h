@@ -68,7 +68,12 @@ typedef struct gst_opts {
   int32_t use_graph;
   /* 1 = fill the per-kernel statistics returned by gst_result_stats. */
   int32_t collect_stats;
-  int32_t reserved[11];
+  /* A growth round runs dense (every vertex, every neighbour row, no
+   * candidate marks) when the previous round changed more than
+   * V >> dense_shift vertices; 0 = the default (1). A tuning knob only:
+   * results do not depend on it. */
+  int32_t dense_shift;
+  int32_t reserved[10];
 } gst_opts;
 
 /* ---------------------------------------------------------------- graph -- */

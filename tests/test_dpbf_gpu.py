@@ -91,7 +91,7 @@ def test_full_state_table_matches_oracle(golden, idx, use_graph):
 
 @pytest.mark.parametrize("use_graph", MODES)
 def test_upper_bound_pruning_is_exact(golden, use_graph):
-    for case in golden["cases"][::20] + golden["cases"][200:]:
+    for case in golden["cases"][::5] + golden["cases"][200:]:
         g, gp, mem = make_instance(case)
         opt = case["dpbf"]
         with native.Graph(g.row_ptr, g.col, g.w) as dg:
