@@ -25,7 +25,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC"]
 
-CU_SOURCES = ["dpbf_kernels.cu", "engine.cu", "noalloc.cu"]
+CU_SOURCES = ["dpbf_kernels.cu", "learn_kernels.cu", "engine.cu", "noalloc.cu"]
 CXX_SOURCES = ["gen.cpp"]
 
 

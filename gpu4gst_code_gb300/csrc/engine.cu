@@ -25,10 +25,12 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <mutex>
 #include <new>
 #include <string>
@@ -39,6 +41,8 @@
 #include "dpbf.cuh"
 #include "gst.h"
 #include "gst_debug.h"
+#include "gst_learn.h"
+#include "learn.cuh"
 
 using namespace gst;
 
@@ -122,6 +126,38 @@ struct Workspace {
   QueryGraph qg[GST_MAX_K + 1];
 };
 
+// Buffers of the learned proposal (allocated on first use).
+struct LearnWs {
+  int32_t V = 0;
+  // features + inference
+  uint32_t* r1 = nullptr;
+  uint32_t* r2 = nullptr;
+  uint32_t* r3 = nullptr;
+  int32_t* mnb = nullptr;
+  float* x = nullptr;                 // V x kFeat
+  __nv_bfloat16* hb[2] = {nullptr, nullptr};  // V x kHid each
+  float* hub_sum = nullptr;           // nbig x kHid
+  float* scores = nullptr;            // V
+  unsigned long long* best = nullptr;
+  int3* pe = nullptr;                 // proposal path edges
+  int32_t* pn = nullptr;              // [count, stopped, unreachable]
+  int32_t pe_cap = 0;
+  // training (fp32)
+  float* h[kMpLayers + 1] = {};       // h0..h3, V x kHid
+  float* a[kMpLayers + 1] = {};       // a1..a3 (a[0] unused)
+  float* dz = nullptr;
+  float* dzp = nullptr;
+  float* t = nullptr;
+  float* u = nullptr;
+  float* s = nullptr;                 // V
+  float* ds = nullptr;                // V
+  uint8_t* label = nullptr;           // V
+  int32_t* ids = nullptr;             // tree vertices
+  int32_t ids_cap = 0;
+  float* red = nullptr;               // loss scratch (2) + loss (1)
+  float* grad = nullptr;              // kNumParams
+};
+
 struct gst_graph {
   int device = 0;
   int num_sms = 0;
@@ -140,8 +176,12 @@ struct gst_graph {
   // Internal vertex IDs: perm[caller ID] and its inverse (see gst_graph_upload)
   std::vector<int32_t> perm, inv;
   int32_t* d_perm = nullptr;
+  int32_t* d_hub_of = nullptr;  // hub index of a vertex, -1 for the others
+  std::vector<int32_t> h_row;   // host copy of the internal CSR (proposal repair)
+  std::vector<int2> h_adj;
   std::mutex mu;
   Workspace ws;
+  LearnWs lw;
 };
 
 struct gst_result {
@@ -154,6 +194,17 @@ struct gst_result {
   int64_t launches = 0;  // kernels this solve launched
   double ms[4] = {0, 0, 0, 0};
   int64_t stats[kNumStats] = {};
+  int32_t ub = 0;          // bound that pruned the solve (learned path)
+  double propose_ms = 0;   // host wall time of the proposal
+};
+
+struct gst_scorer {
+  int device = 0;
+  float* params = nullptr;         // kNumParams fp32
+  __nv_bfloat16* wcat = nullptr;   // kMpLayers x kHid x 2 kHid bf16
+  float* m = nullptr;              // Adam moments
+  float* v = nullptr;
+  int32_t t = 0;                   // Adam steps taken
 };
 
 namespace {
@@ -181,6 +232,34 @@ void drop_graphs(Workspace& ws) {
     if (q.graph) cudaGraphDestroy(q.graph);
     q = QueryGraph{};
   }
+}
+
+void free_learn(LearnWs& lw) {
+  dfree(lw.r1);
+  dfree(lw.r2);
+  dfree(lw.r3);
+  dfree(lw.mnb);
+  dfree(lw.x);
+  dfree(lw.hb[0]);
+  dfree(lw.hb[1]);
+  dfree(lw.hub_sum);
+  dfree(lw.scores);
+  dfree(lw.best);
+  dfree(lw.pe);
+  dfree(lw.pn);
+  for (auto& p : lw.h) dfree(p);
+  for (auto& p : lw.a) dfree(p);
+  dfree(lw.dz);
+  dfree(lw.dzp);
+  dfree(lw.t);
+  dfree(lw.u);
+  dfree(lw.s);
+  dfree(lw.ds);
+  dfree(lw.label);
+  dfree(lw.ids);
+  dfree(lw.red);
+  dfree(lw.grad);
+  lw = LearnWs{};
 }
 
 void free_workspace(Workspace& ws) {
@@ -691,6 +770,309 @@ gst_opts resolve_opts(const gst_opts* opts) {
   return o;
 }
 
+
+// ------------------------------------------------------- learned proposal --
+gst_status ensure_learn_infer(gst_graph* g) {
+  LearnWs& lw = g->lw;
+  if (lw.x) return GST_OK;
+  const size_t V = (size_t)g->V;
+  lw.V = g->V;
+  GST_CUDA(cudaMalloc(&lw.r1, V * 4));
+  GST_CUDA(cudaMalloc(&lw.r2, V * 4));
+  GST_CUDA(cudaMalloc(&lw.r3, V * 4));
+  GST_CUDA(cudaMalloc(&lw.mnb, V * 4));
+  GST_CUDA(cudaMalloc(&lw.x, V * kFeat * sizeof(float)));
+  GST_CUDA(cudaMalloc(&lw.hb[0], V * kHid * sizeof(__nv_bfloat16)));
+  GST_CUDA(cudaMalloc(&lw.hb[1], V * kHid * sizeof(__nv_bfloat16)));
+  GST_CUDA(cudaMalloc(&lw.hub_sum, std::max<size_t>(1, (size_t)g->nbig) * kHid * sizeof(float)));
+  GST_CUDA(cudaMalloc(&lw.scores, V * sizeof(float)));
+  GST_CUDA(cudaMalloc(&lw.best, sizeof(unsigned long long)));
+  lw.pe_cap = (int32_t)std::min<int64_t>((int64_t)GST_MAX_K * (g->V + 1), 1 << 22);
+  GST_CUDA(cudaMalloc(&lw.pe, (size_t)lw.pe_cap * sizeof(int3)));
+  GST_CUDA(cudaMalloc(&lw.pn, 4 * sizeof(int32_t)));
+  return GST_OK;
+}
+
+gst_status ensure_learn_train(gst_graph* g, int32_t nids) {
+  LearnWs& lw = g->lw;
+  const size_t V = (size_t)g->V;
+  if (!lw.h[0]) {
+    const size_t act = V * kHid * sizeof(float);
+    for (auto& p : lw.h) GST_CUDA(cudaMalloc(&p, act));
+    for (int l = 1; l <= kMpLayers; ++l) GST_CUDA(cudaMalloc(&lw.a[l], act));
+    GST_CUDA(cudaMalloc(&lw.dz, act));
+    GST_CUDA(cudaMalloc(&lw.dzp, act));
+    GST_CUDA(cudaMalloc(&lw.t, act));
+    GST_CUDA(cudaMalloc(&lw.u, act));
+    GST_CUDA(cudaMalloc(&lw.s, V * sizeof(float)));
+    GST_CUDA(cudaMalloc(&lw.ds, V * sizeof(float)));
+    GST_CUDA(cudaMalloc(&lw.label, V));
+    GST_CUDA(cudaMalloc(&lw.red, 4 * sizeof(float)));
+    GST_CUDA(cudaMalloc(&lw.grad, kNumParams * sizeof(float)));
+  }
+  if (nids > lw.ids_cap) {
+    dfree(lw.ids);
+    lw.ids_cap = 0;
+    GST_CUDA(cudaMalloc(&lw.ids, (size_t)std::max(nids, 1024) * sizeof(int32_t)));
+    lw.ids_cap = std::max(nids, 1024);
+  }
+  return GST_OK;
+}
+
+// Group masks of a query into ws.gmask (internal IDs).
+gst_status upload_groups(gst_graph* g, const int32_t* group_ptr, const int32_t* members, int32_t k) {
+  Workspace& ws = g->ws;
+  const int64_t nmembers = group_ptr[k];
+  gst_status st = ensure_workspace(g, k, nmembers);
+  if (st != GST_OK) return st;
+  cudaStream_t s = g->stream;
+  GST_CUDA(cudaMemcpyAsync(ws.d_group_ptr, group_ptr, (size_t)(k + 1) * 4, cudaMemcpyHostToDevice, s));
+  if (nmembers)
+    GST_CUDA(cudaMemcpyAsync(ws.d_members, members, (size_t)nmembers * 4, cudaMemcpyHostToDevice, s));
+  GST_CUDA(cudaMemsetAsync(ws.gmask, 0, (size_t)g->V * sizeof(uint32_t), s));
+  GST_CUDA(launch_group_masks(ws.d_group_ptr, ws.d_members, g->d_perm, k, ws.gmask, s));
+  return GST_OK;
+}
+
+// Query features into lw.x (after upload_groups).
+gst_status compute_features(gst_graph* g, int32_t k) {
+  LearnWs& lw = g->lw;
+  const GraphDev gd = graph_dev(g);
+  cudaStream_t s = g->stream;
+  GST_CUDA(launch_reach(gd, g->ws.gmask, lw.r1, lw.mnb, s));
+  GST_CUDA(launch_reach(gd, lw.r1, lw.r2, nullptr, s));
+  GST_CUDA(launch_reach(gd, lw.r2, lw.r3, nullptr, s));
+  GST_CUDA(launch_features(gd, g->ws.gmask, lw.r1, lw.r2, lw.r3, lw.mnb, k, lw.x, s));
+  return GST_OK;
+}
+
+// bf16 inference: scores into lw.scores.
+gst_status infer_scores(gst_graph* g, const gst_scorer* sc) {
+  LearnWs& lw = g->lw;
+  const GraphDev gd = graph_dev(g);
+  cudaStream_t s = g->stream;
+  GST_CUDA(launch_infer_l0(g->V, lw.x, sc->params, lw.hb[0], s));
+  for (int l = 1; l <= kMpLayers; ++l) {
+    const __nv_bfloat16* hin = lw.hb[(l - 1) & 1];
+    if (g->nbig > 0) {
+      GST_CUDA(cudaMemsetAsync(lw.hub_sum, 0, (size_t)g->nbig * kHid * sizeof(float), s));
+      GST_CUDA(launch_hub_sum_bf16(gd, hin, lw.hub_sum, s));
+    }
+    const bool last = l == kMpLayers;
+    GST_CUDA(launch_infer_layer(gd, g->d_hub_of, lw.hub_sum, hin, sc->wcat + (size_t)(l - 1) * kHid * 2 * kHid,
+                                sc->params, l, last ? nullptr : lw.hb[l & 1], last ? lw.scores : nullptr, s));
+  }
+  return GST_OK;
+}
+
+// fp32 forward: activations into lw.h / lw.a, scores into lw.s.
+gst_status train_forward(gst_graph* g, const gst_scorer* sc) {
+  LearnWs& lw = g->lw;
+  const GraphDev gd = graph_dev(g);
+  cudaStream_t s = g->stream;
+  const int32_t V = g->V;
+  const float* p = sc->params;
+  GST_CUDA(launch_dense_fwd(V, lw.x, kFeat, p + kOffW0, nullptr, nullptr, p + kOffB0, lw.h[0], s));
+  for (int l = 1; l <= kMpLayers; ++l) {
+    const float* L = p + layer_off(l);
+    GST_CUDA(launch_mean_agg(gd, lw.h[l - 1], lw.a[l], s));
+    GST_CUDA(launch_dense_fwd(V, lw.h[l - 1], kHid, L, lw.a[l], L + kHid * kHid, L + 2 * kHid * kHid, lw.h[l], s));
+  }
+  GST_CUDA(launch_score(V, lw.h[kMpLayers], p, lw.s, s));
+  return GST_OK;
+}
+
+// Gradient of the listwise loss into lw.grad (after train_forward and the labels).
+gst_status train_backward(gst_graph* g, const gst_scorer* sc, int32_t n) {
+  LearnWs& lw = g->lw;
+  const GraphDev gd = graph_dev(g);
+  cudaStream_t s = g->stream;
+  const int32_t V = g->V;
+  const float* p = sc->params;
+  GST_CUDA(cudaMemsetAsync(lw.grad, 0, kNumParams * sizeof(float), s));
+  GST_CUDA(cudaMemsetAsync(lw.red + 2, 0, sizeof(float), s));
+  GST_CUDA(launch_softmax_loss(V, lw.s, lw.label, n, lw.ds, lw.red + 2, lw.red, s));
+  GST_CUDA(launch_out_bwd(V, lw.ds, lw.h[kMpLayers], p, lw.grad, lw.dz, s));
+  for (int l = kMpLayers; l >= 1; --l) {
+    const float* L = p + layer_off(l);
+    float* G = lw.grad + layer_off(l);
+    GST_CUDA(launch_dense_bwd_weight(V, lw.dz, lw.h[l - 1], kHid, G, G + 2 * kHid * kHid, s));
+    GST_CUDA(launch_dense_bwd_weight(V, lw.dz, lw.a[l], kHid, G + kHid * kHid, nullptr, s));
+    GST_CUDA(launch_dense_bwd_data(V, lw.dz, L + kHid * kHid, lw.t, s));  // through Wn, then the aggregation
+    GST_CUDA(launch_dense_bwd_data(V, lw.dz, L, lw.u, s));                // through Ws
+    GST_CUDA(launch_agg_bwd(gd, lw.t, lw.u, lw.h[l - 1], lw.dzp, s));
+    std::swap(lw.dz, lw.dzp);
+  }
+  GST_CUDA(launch_dense_bwd_weight(V, lw.dz, lw.x, kFeat, lw.grad + kOffW0, lw.grad + kOffB0, s));
+  return GST_OK;
+}
+
+// A feasible tree of the query rooted at the top-scored vertex (or the
+// fixed feature score with sc NULL), written into r (caller IDs).
+gst_status propose_tree(gst_graph* g, const gst_scorer* sc, const int32_t* group_ptr, const int32_t* members,
+                        int32_t k, const gst_opts& o, gst_result* r) {
+  LearnWs& lw = g->lw;
+  Workspace& ws = g->ws;
+  cudaStream_t s = g->stream;
+  gst_status st = ensure_learn_infer(g);
+  if (st != GST_OK) return st;
+  st = upload_groups(g, group_ptr, members, k);
+  if (st != GST_OK) return st;
+  st = compute_features(g, k);
+  if (st != GST_OK) return st;
+  if (sc) {
+    st = infer_scores(g, sc);
+    if (st != GST_OK) return st;
+  } else {
+    GST_CUDA(launch_feature_score(g->V, lw.x, lw.scores, s));
+  }
+  GST_CUDA(cudaMemsetAsync(lw.best, 0, sizeof(unsigned long long), s));
+  GST_CUDA(launch_argmax(g->V, lw.scores, lw.best, s));
+  unsigned long long best = 0;
+  GST_CUDA(cudaMemcpyAsync(&best, lw.best, sizeof(best), cudaMemcpyDeviceToHost, s));
+  GST_CUDA(cudaStreamSynchronize(s));
+  if (best == 0) return fail(GST_INTERNAL, "no vertex scored");
+  const int32_t root = (int32_t)(0xffffffffull - (best & 0xffffffffull));
+  // distances to the root: a two-group solve whose groups are both {root}
+  // grows wave 1 to the full shortest-path fixpoint from the root (a
+  // one-group solve would stop after its only, last, wave's merge); the
+  // row of wave 1 has stride 4 either way
+  const int32_t gp1[3] = {0, 1, 2};
+  const int32_t mem1[2] = {g->inv[(size_t)root], g->inv[(size_t)root]};
+  gst_opts o1 = o;
+  o1.upper_bound = 0;
+  gst_result tmp;
+  st = solve_one(g, gp1, mem1, 2, o1, &tmp);
+  if (st != GST_OK) return st;
+  // nearest member of every group and its path to the root
+  const int64_t nmembers = group_ptr[k];
+  GST_CUDA(cudaMemcpyAsync(ws.d_group_ptr, group_ptr, (size_t)(k + 1) * 4, cudaMemcpyHostToDevice, s));
+  if (nmembers)
+    GST_CUDA(cudaMemcpyAsync(ws.d_members, members, (size_t)nmembers * 4, cudaMemcpyHostToDevice, s));
+  GST_CUDA(cudaMemsetAsync(lw.pn, 0, 4 * sizeof(int32_t), s));
+  GST_CUDA(launch_ub_paths(graph_dev(g), ws.cost, ws.par, ws.h_lvl_stride[1], ws.d_group_ptr, ws.d_members,
+                           g->d_perm, k, lw.pe, lw.pn, lw.pe_cap, s));
+  int32_t pn[4];
+  GST_CUDA(cudaMemcpyAsync(pn, lw.pn, sizeof(pn), cudaMemcpyDeviceToHost, s));
+  GST_CUDA(cudaStreamSynchronize(s));
+  if (pn[2]) return fail(GST_INFEASIBLE, "a group cannot reach the proposal's root");
+  if (pn[1] || pn[0] > lw.pe_cap) return fail(GST_INTERNAL, "proposal path walk failed");
+  std::vector<int3> pe((size_t)pn[0]);
+  if (pn[0]) GST_CUDA(cudaMemcpy(pe.data(), lw.pe, pe.size() * sizeof(int3), cudaMemcpyDeviceToHost));
+
+  // union of the paths (a subtree of the shortest-path tree)
+  std::vector<int32_t> tv{root};
+  std::vector<std::pair<std::pair<int32_t, int32_t>, int32_t>> te;
+  for (const int3& e : pe) {
+    tv.push_back(e.x);
+    tv.push_back(e.y);
+    te.push_back({{std::min(e.x, e.y), std::max(e.x, e.y)}, e.z});
+  }
+  std::sort(tv.begin(), tv.end());
+  tv.erase(std::unique(tv.begin(), tv.end()), tv.end());
+  std::sort(te.begin(), te.end());
+  te.erase(std::unique(te.begin(), te.end(), [](auto& a, auto& b) { return a.first == b.first; }), te.end());
+  int64_t cost1 = 0;
+  for (auto& e : te) cost1 += e.second;
+
+  // MST repair: a minimum spanning tree of the subgraph induced by the
+  // tree's vertices, then leaves whose groups other vertices still cover
+  // are removed while any remain
+  const size_t nv = tv.size();
+  auto idx = [&](int32_t v) -> int64_t {
+    auto it = std::lower_bound(tv.begin(), tv.end(), v);
+    return (it != tv.end() && *it == v) ? it - tv.begin() : -1;
+  };
+  std::vector<std::pair<int32_t, std::pair<int32_t, int32_t>>> ind;  // (w, (i, j))
+  for (size_t i = 0; i < nv; ++i) {
+    const int32_t v = tv[i];
+    for (int32_t e = g->h_row[(size_t)v]; e < g->h_row[(size_t)v + 1]; ++e) {
+      const int2 x = g->h_adj[(size_t)e];
+      if (x.x <= v) continue;
+      const int64_t j = idx(x.x);
+      if (j >= 0) ind.push_back({x.y, {(int32_t)i, (int32_t)j}});
+    }
+  }
+  std::sort(ind.begin(), ind.end());
+  std::vector<int32_t> dsu(nv);
+  for (size_t i = 0; i < nv; ++i) dsu[i] = (int32_t)i;
+  std::function<int32_t(int32_t)> find = [&](int32_t a) { return dsu[(size_t)a] == a ? a : dsu[(size_t)a] = find(dsu[(size_t)a]); };
+  std::vector<std::vector<std::pair<int32_t, int32_t>>> adj(nv);  // (neighbour, w)
+  for (auto& e : ind) {
+    const int32_t a = find(e.second.first), b = find(e.second.second);
+    if (a == b) continue;
+    dsu[(size_t)a] = b;
+    adj[(size_t)e.second.first].push_back({e.second.second, e.first});
+    adj[(size_t)e.second.second].push_back({e.second.first, e.first});
+  }
+  std::vector<uint32_t> bits(nv, 0u);
+  for (int32_t gi = 0; gi < k; ++gi)
+    for (int32_t i = group_ptr[gi]; i < group_ptr[gi + 1]; ++i) {
+      const int64_t j = idx(g->perm[(size_t)members[i]]);
+      if (j >= 0) bits[(size_t)j] |= 1u << gi;
+    }
+  std::vector<int32_t> cover((size_t)k, 0);
+  for (size_t i = 0; i < nv; ++i)
+    for (int32_t gi = 0; gi < k; ++gi) cover[(size_t)gi] += (bits[i] >> gi) & 1u;
+  std::vector<char> alive(nv, 1);
+  std::vector<int32_t> deg(nv);
+  for (size_t i = 0; i < nv; ++i) deg[i] = (int32_t)adj[i].size();
+  size_t left = nv;
+  for (bool again = true; again && left > 1;) {
+    again = false;
+    for (size_t i = 0; i < nv && left > 1; ++i) {
+      if (!alive[i] || deg[i] > 1) continue;
+      bool needed = false;
+      for (int32_t gi = 0; gi < k; ++gi)
+        if (((bits[i] >> gi) & 1u) && cover[(size_t)gi] <= 1) needed = true;
+      if (needed) continue;
+      alive[i] = 0;
+      --left;
+      again = true;
+      for (int32_t gi = 0; gi < k; ++gi) cover[(size_t)gi] -= (bits[i] >> gi) & 1u;
+      for (auto& nb : adj[i])
+        if (alive[(size_t)nb.first]) --deg[(size_t)nb.first];
+    }
+  }
+  int64_t cost2 = 0;
+  std::vector<std::pair<std::pair<int32_t, int32_t>, int32_t>> te2;
+  for (size_t i = 0; i < nv; ++i) {
+    if (!alive[i]) continue;
+    for (auto& nb : adj[i])
+      if ((size_t)nb.first > i && alive[(size_t)nb.first]) {
+        cost2 += nb.second;
+        te2.push_back({{tv[i], tv[(size_t)nb.first]}, nb.second});
+      }
+  }
+  bool connected = true;  // the MST spans the path union, which is connected
+  {
+    int32_t c = -1;
+    for (size_t i = 0; i < nv; ++i)
+      if (alive[i]) {
+        const int32_t ri = find((int32_t)i);
+        if (c < 0) c = ri;
+        connected &= ri == c;
+      }
+  }
+  const bool use2 = connected && cost2 < cost1;
+  r->vertices.clear();
+  r->edges.clear();
+  for (size_t i = 0; i < nv; ++i)
+    if (!use2 || alive[i]) r->vertices.push_back(g->inv[(size_t)tv[i]]);
+  std::sort(r->vertices.begin(), r->vertices.end());
+  for (auto& e : use2 ? te2 : te) {
+    const int32_t a = g->inv[(size_t)e.first.first], b = g->inv[(size_t)e.first.second];
+    r->edges.push_back(std::min(a, b));
+    r->edges.push_back(std::max(a, b));
+    r->edges.push_back(e.second);
+  }
+  const int64_t c = use2 ? cost2 : cost1;
+  if (c >= GST_COST_LIMIT) return fail(GST_OVERFLOW, "proposal cost reached GST_COST_LIMIT");
+  r->cost = (int32_t)c;
+  r->root = g->inv[(size_t)root];
+  r->status = GST_OK;
+  return GST_OK;
+}
 }  // namespace
 
 // ------------------------------------------------------------------ C ABI --
@@ -774,6 +1156,8 @@ gst_status gst_graph_upload(const int32_t* row_ptr, const int32_t* col, const in
     });
   }
   g->nbig = (int32_t)big.size();
+  std::vector<int32_t> hub_of((size_t)V, -1);
+  for (int32_t h = 0; h < g->nbig; ++h) hub_of[(size_t)big[(size_t)h]] = h;
   std::vector<int2> chunks;
   for (int32_t h = 0; h < g->nbig; ++h)
     for (int32_t e = row_ptr[big[(size_t)h]]; e < row_ptr[big[(size_t)h] + 1]; e += 32) chunks.push_back(make_int2(h, e));
@@ -795,6 +1179,7 @@ gst_status gst_graph_upload(const int32_t* row_ptr, const int32_t* col, const in
   };
   if ((e = up((void**)&g->d_row_ptr, row_ptr, (size_t)(V + 1) * 4)) != cudaSuccess ||
       (e = up((void**)&g->d_perm, g->perm.data(), (size_t)V * 4)) != cudaSuccess ||
+      (e = up((void**)&g->d_hub_of, hub_of.data(), (size_t)V * 4)) != cudaSuccess ||
       (e = up((void**)&g->d_adj, adj.data(), adj.size() * sizeof(int2))) != cudaSuccess ||
       (e = up((void**)&g->d_big, big.data(), big.size() * 4)) != cudaSuccess ||
       (e = up((void**)&g->d_order, order.data(), order.size() * 4)) != cudaSuccess ||
@@ -802,6 +1187,8 @@ gst_status gst_graph_upload(const int32_t* row_ptr, const int32_t* col, const in
       (e = cudaStreamSynchronize(g->stream)) != cudaSuccess)
     return cleanup(fail(e == cudaErrorMemoryAllocation ? GST_OOM : GST_CUDA_ERROR,
                         std::string("graph upload: ") + cudaGetErrorString(e)));
+  g->h_row = std::move(nrow);
+  g->h_adj = std::move(adj);
   *out = g;
   return GST_OK;
 }
@@ -813,8 +1200,10 @@ void gst_graph_free(gst_graph* g) {
   cudaSetDevice(g->device);
   if (g->stream) cudaStreamSynchronize(g->stream);
   free_workspace(g->ws);
+  free_learn(g->lw);
   dfree(g->d_row_ptr);
   dfree(g->d_perm);
+  dfree(g->d_hub_of);
   dfree(g->d_adj);
   dfree(g->d_big);
   dfree(g->d_order);
@@ -921,6 +1310,222 @@ gst_status gst_graph_debug_table(gst_graph* g, int32_t k, int32_t* out) {
   }
   return GST_OK;
 }
+
+
+// ------------------------------------------------------ learned proposal --
+int64_t gst_scorer_num_params(void) { return kNumParams; }
+
+gst_status gst_scorer_create(const float* params, gst_scorer** out) {
+  g_last_error.clear();
+  if (!out || !params) return fail(GST_BAD_INPUT, "params / out is NULL");
+  *out = nullptr;
+  auto* sc = new (std::nothrow) gst_scorer;
+  if (!sc) return fail(GST_OOM, "host allocation failed");
+  auto bad = [&](cudaError_t e) {
+    gst_scorer_free(sc);
+    return fail(e == cudaErrorMemoryAllocation ? GST_OOM : GST_CUDA_ERROR,
+                std::string("scorer setup: ") + cudaGetErrorString(e));
+  };
+  cudaError_t e;
+  if ((e = cudaGetDevice(&sc->device)) != cudaSuccess) return bad(e);
+  const size_t pb = kNumParams * sizeof(float);
+  if ((e = cudaMalloc(&sc->params, pb)) != cudaSuccess || (e = cudaMalloc(&sc->m, pb)) != cudaSuccess ||
+      (e = cudaMalloc(&sc->v, pb)) != cudaSuccess ||
+      (e = cudaMalloc(&sc->wcat, (size_t)kMpLayers * kHid * 2 * kHid * sizeof(__nv_bfloat16))) != cudaSuccess ||
+      (e = cudaMemcpy(sc->params, params, pb, cudaMemcpyHostToDevice)) != cudaSuccess ||
+      (e = cudaMemset(sc->m, 0, pb)) != cudaSuccess || (e = cudaMemset(sc->v, 0, pb)) != cudaSuccess ||
+      (e = launch_pack_bf16(sc->params, sc->wcat, 0)) != cudaSuccess || (e = cudaDeviceSynchronize()) != cudaSuccess)
+    return bad(e);
+  *out = sc;
+  return GST_OK;
+}
+
+void gst_scorer_free(gst_scorer* sc) {
+  if (!sc) return;
+  int prev = -1;
+  cudaGetDevice(&prev);
+  cudaSetDevice(sc->device);
+  dfree(sc->params);
+  dfree(sc->wcat);
+  dfree(sc->m);
+  dfree(sc->v);
+  if (prev >= 0) cudaSetDevice(prev);
+  delete sc;
+}
+
+gst_status gst_scorer_get_params(const gst_scorer* sc, float* out) {
+  g_last_error.clear();
+  if (!sc || !out) return fail(GST_BAD_INPUT, "bad arguments");
+  GST_CUDA(cudaMemcpy(out, sc->params, kNumParams * sizeof(float), cudaMemcpyDeviceToHost));
+  return GST_OK;
+}
+
+namespace {
+// Common checks of the learned entry points; takes the graph's lock.
+gst_status learn_enter(gst_graph* g, const int32_t* group_ptr, const int32_t* members, int32_t k) {
+  g_last_error.clear();
+  if (!g) return fail(GST_BAD_INPUT, "graph is NULL");
+  bool empty = false;
+  gst_status st = validate_groups(g, group_ptr, members, k, &empty);
+  if (st != GST_OK) return st;
+  if (empty) return fail(GST_INFEASIBLE, "a group has no members");
+  return GST_OK;
+}
+
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    cudaGetDevice(&prev);
+    if (prev != dev) cudaSetDevice(dev);
+  }
+  ~DeviceGuard() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+};
+}  // namespace
+
+gst_status gst_scorer_scores(gst_graph* g, gst_scorer* sc, const int32_t* group_ptr, const int32_t* members, int32_t k,
+                             int32_t precision, float* scores) {
+  gst_status st = learn_enter(g, group_ptr, members, k);
+  if (st != GST_OK) return st;
+  if (!sc || !scores) return fail(GST_BAD_INPUT, "scorer / scores is NULL");
+  std::lock_guard<std::mutex> lock(g->mu);
+  DeviceGuard dg(g->device);
+  cudaGetLastError();
+  st = ensure_learn_infer(g);
+  if (st == GST_OK && precision) st = ensure_learn_train(g, 0);
+  if (st == GST_OK) st = upload_groups(g, group_ptr, members, k);
+  if (st == GST_OK) st = compute_features(g, k);
+  if (st != GST_OK) return st;
+  const float* src = g->lw.scores;
+  if (precision) {
+    st = train_forward(g, sc);
+    src = g->lw.s;
+  } else {
+    st = infer_scores(g, sc);
+  }
+  if (st != GST_OK) return st;
+  std::vector<float> tmp((size_t)g->V);
+  GST_CUDA(cudaMemcpyAsync(tmp.data(), src, tmp.size() * sizeof(float), cudaMemcpyDeviceToHost, g->stream));
+  GST_CUDA(cudaStreamSynchronize(g->stream));
+  for (int32_t v = 0; v < g->V; ++v) scores[v] = tmp[(size_t)g->perm[(size_t)v]];
+  return GST_OK;
+}
+
+gst_status gst_scorer_train_step(gst_graph* g, gst_scorer* sc, const int32_t* group_ptr, const int32_t* members,
+                                 int32_t k, const int32_t* tree_vertices, int32_t n, float lr, int32_t apply,
+                                 float* loss, float* grads) {
+  gst_status st = learn_enter(g, group_ptr, members, k);
+  if (st != GST_OK) return st;
+  if (!sc || !tree_vertices || n < 1) return fail(GST_BAD_INPUT, "scorer / tree vertices missing");
+  std::vector<int32_t> ids;
+  ids.reserve((size_t)n);
+  for (int32_t i = 0; i < n; ++i) {
+    if (tree_vertices[i] < 0 || tree_vertices[i] >= g->V) return fail(GST_BAD_INPUT, "tree vertex out of range");
+    ids.push_back(g->perm[(size_t)tree_vertices[i]]);
+  }
+  std::sort(ids.begin(), ids.end());
+  ids.erase(std::unique(ids.begin(), ids.end()), ids.end());
+  std::lock_guard<std::mutex> lock(g->mu);
+  DeviceGuard dg(g->device);
+  cudaGetLastError();
+  cudaStream_t s = g->stream;
+  st = ensure_learn_infer(g);
+  if (st == GST_OK) st = ensure_learn_train(g, (int32_t)ids.size());
+  if (st == GST_OK) st = upload_groups(g, group_ptr, members, k);
+  if (st == GST_OK) st = compute_features(g, k);
+  if (st == GST_OK) st = train_forward(g, sc);
+  if (st != GST_OK) return st;
+  LearnWs& lw = g->lw;
+  GST_CUDA(cudaMemsetAsync(lw.label, 0, (size_t)g->V, s));
+  GST_CUDA(cudaMemcpyAsync(lw.ids, ids.data(), ids.size() * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+  GST_CUDA(launch_set_labels(lw.ids, (int32_t)ids.size(), lw.label, s));
+  st = train_backward(g, sc, (int32_t)ids.size());
+  if (st != GST_OK) return st;
+  float l = 0.0f;
+  GST_CUDA(cudaMemcpyAsync(&l, lw.red + 2, sizeof(float), cudaMemcpyDeviceToHost, s));
+  if (grads) GST_CUDA(cudaMemcpyAsync(grads, lw.grad, kNumParams * sizeof(float), cudaMemcpyDeviceToHost, s));
+  if (apply) {
+    ++sc->t;
+    GST_CUDA(launch_adam(kNumParams, sc->params, lw.grad, sc->m, sc->v, lr, sc->t, s));
+    GST_CUDA(launch_pack_bf16(sc->params, sc->wcat, s));
+  }
+  GST_CUDA(cudaStreamSynchronize(s));
+  if (loss) *loss = l;
+  return GST_OK;
+}
+
+gst_status gst_propose(gst_graph* g, gst_scorer* sc, const int32_t* group_ptr, const int32_t* members, int32_t k,
+                       gst_result** out) {
+  if (!out) return fail(GST_BAD_INPUT, "out is NULL");
+  *out = nullptr;
+  gst_status st = learn_enter(g, group_ptr, members, k);
+  if (st != GST_OK) return st;
+  auto* r = new (std::nothrow) gst_result;
+  if (!r) return fail(GST_OOM, "host allocation failed");
+  *out = r;
+  std::lock_guard<std::mutex> lock(g->mu);
+  DeviceGuard dg(g->device);
+  cudaGetLastError();
+  const auto t0 = std::chrono::steady_clock::now();
+  gst_opts o = resolve_opts(nullptr);
+  o.use_graph = 1;
+  st = propose_tree(g, sc, group_ptr, members, k, o, r);
+  r->propose_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  r->status = st;
+  return st;
+}
+
+gst_status gst_solve_learned(gst_graph* g, gst_scorer* sc, const int32_t* group_ptr, const int32_t* members, int32_t k,
+                             const gst_opts* opts, gst_result** out) {
+  if (!out) return fail(GST_BAD_INPUT, "out is NULL");
+  *out = nullptr;
+  g_last_error.clear();
+  if (!g) return fail(GST_BAD_INPUT, "graph is NULL");
+  bool empty = false;
+  gst_status st = validate_groups(g, group_ptr, members, k, &empty);
+  if (st != GST_OK) return st;
+  auto* r = new (std::nothrow) gst_result;
+  if (!r) return fail(GST_OOM, "host allocation failed");
+  *out = r;
+  if (empty) {
+    r->status = GST_INFEASIBLE;
+    return GST_INFEASIBLE;
+  }
+  gst_opts o = resolve_opts(opts);
+  std::lock_guard<std::mutex> lock(g->mu);
+  DeviceGuard dg(g->device);
+  cudaGetLastError();
+  const auto t0 = std::chrono::steady_clock::now();
+  gst_result prop;
+  const gst_status pst = propose_tree(g, sc, group_ptr, members, k, o, &prop);
+  const double pms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  if (pst == GST_OK && prop.cost > 0) {
+    o.upper_bound = prop.cost;
+    st = solve_one(g, group_ptr, members, k, o, r);
+    if (st == GST_OK) {
+      r->status = GST_OK;
+      r->ub = prop.cost;
+      r->propose_ms = pms;
+      return GST_OK;
+    }
+    if (st != GST_INFEASIBLE) {
+      r->status = st;
+      return st;
+    }
+  }
+  // no usable proposal (or a zero-cost one): the unpruned DP decides
+  g_last_error.clear();
+  *r = gst_result{};
+  o.upper_bound = 0;
+  st = solve_one(g, group_ptr, members, k, o, r);
+  r->status = st;
+  r->propose_ms = pms;
+  return st;
+}
+
+int32_t gst_result_upper_bound(const gst_result* r) { return r ? r->ub : 0; }
+double gst_result_proposal_ms(const gst_result* r) { return r ? r->propose_ms : 0.0; }
 
 const char* gst_last_error(void) { return g_last_error.c_str(); }
 const char* gst_version(void) { return "gst-gb300 0.2 (sm_103a)"; }

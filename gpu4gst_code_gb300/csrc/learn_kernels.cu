@@ -1,0 +1,679 @@
+// Kernels of the learned upper-bound proposal (declared in learn.cuh):
+// query features, bf16 inference with tensor-core mma over 16-vertex
+// tiles, fp32 forward/backward training kernels and the Adam update.
+//
+// Query features x[v][0..15] (internal vertex IDs, k groups):
+//   0  1                          6  all k groups within 1 hop
+//   1  log(1 + deg) / 8           7  all k groups within 2 hops
+//   2  groups v belongs to / k    8  all k groups within 3 hops
+//   3  groups within 1 hop / k    9  neighbours in some group / deg
+//   4  groups within 2 hops / k   10 v belongs to some group
+//   5  groups within 3 hops / k   11..15 zero
+// ("within h hops" includes v itself.)
+#include <cstdint>
+
+#include "learn.cuh"
+
+namespace gst {
+namespace {
+
+__device__ __forceinline__ int64_t gwarp() { return ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; }
+__device__ __forceinline__ int64_t nwarps() { return ((int64_t)gridDim.x * blockDim.x) >> 5; }
+
+int grid_for(int64_t items, int per_block, int cap = 152 * 16) {
+  int64_t b = (items + per_block - 1) / per_block;
+  if (b < 1) b = 1;
+  if (b > cap) b = cap;
+  return (int)b;
+}
+
+// -------------------------------------------------------------- features --
+__global__ void k_reach(GraphDev g, const uint32_t* __restrict__ in, uint32_t* __restrict__ out,
+                        int32_t* __restrict__ member_nbrs) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t v = gwarp(); v < g.V; v += nwarps()) {
+    const int32_t beg = g.row_ptr[v], end = g.row_ptr[v + 1];
+    uint32_t acc = 0;
+    int32_t cnt = 0;
+    for (int32_t e = beg + lane; e < end; e += 32) {
+      const uint32_t m = in[g.adj[e].x];
+      acc |= m;
+      cnt += m != 0u;
+    }
+    acc = __reduce_or_sync(0xffffffffu, acc);
+    cnt = (int32_t)__reduce_add_sync(0xffffffffu, (uint32_t)cnt);
+    if (lane == 0) {
+      out[v] = acc | in[v];
+      if (member_nbrs) member_nbrs[v] = cnt;
+    }
+  }
+}
+
+__global__ void k_features(GraphDev g, const uint32_t* __restrict__ m0, const uint32_t* __restrict__ r1,
+                           const uint32_t* __restrict__ r2, const uint32_t* __restrict__ r3,
+                           const int32_t* __restrict__ member_nbrs, int32_t k, float* __restrict__ x) {
+  const float ik = 1.0f / (float)k;
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < g.V; v += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t deg = g.row_ptr[v + 1] - g.row_ptr[v];
+    const int c0 = __popc(m0[v]), c1 = __popc(r1[v]), c2 = __popc(r2[v]), c3 = __popc(r3[v]);
+    float f[kFeat];
+    f[0] = 1.0f;
+    f[1] = log1pf((float)deg) * 0.125f;
+    f[2] = c0 * ik;
+    f[3] = c1 * ik;
+    f[4] = c2 * ik;
+    f[5] = c3 * ik;
+    f[6] = c1 == k ? 1.0f : 0.0f;
+    f[7] = c2 == k ? 1.0f : 0.0f;
+    f[8] = c3 == k ? 1.0f : 0.0f;
+    f[9] = deg > 0 ? (float)member_nbrs[v] / (float)deg : 0.0f;
+    f[10] = c0 > 0 ? 1.0f : 0.0f;
+#pragma unroll
+    for (int i = 11; i < kFeat; ++i) f[i] = 0.0f;
+    float4* xo = reinterpret_cast<float4*>(x + v * kFeat);
+#pragma unroll
+    for (int q = 0; q < kFeat / 4; ++q) xo[q] = make_float4(f[4 * q], f[4 * q + 1], f[4 * q + 2], f[4 * q + 3]);
+  }
+}
+
+// ------------------------------------------------------------- inference --
+__global__ void k_pack_bf16(const float* __restrict__ p, __nv_bfloat16* __restrict__ wcat) {
+  const int64_t n = (int64_t)kMpLayers * kHid * 2 * kHid;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int l = (int)(i / (kHid * 2 * kHid)) + 1;
+    const int r = (int)(i % (kHid * 2 * kHid));
+    const int o = r / (2 * kHid), c = r % (2 * kHid);
+    const float* base = p + layer_off(l);
+    const float w = c < kHid ? base[o * kHid + c] : base[kHid * kHid + o * kHid + (c - kHid)];
+    wcat[i] = __float2bfloat16_rn(w);
+  }
+}
+
+// block: 4 vertices x 64 outputs
+__global__ void __launch_bounds__(256) k_infer_l0(int32_t V, const float* __restrict__ x, const float* __restrict__ p,
+                                                  __nv_bfloat16* __restrict__ h) {
+  __shared__ float sw[kHid][kFeat + 1];
+  __shared__ float sb[kHid];
+  for (int i = threadIdx.x; i < kHid * kFeat; i += blockDim.x) sw[i / kFeat][i % kFeat] = p[kOffW0 + i];
+  if (threadIdx.x < kHid) sb[threadIdx.x] = p[kOffB0 + threadIdx.x];
+  __syncthreads();
+  const int o = threadIdx.x & (kHid - 1), vi = threadIdx.x >> 6;
+  for (int64_t v = (int64_t)blockIdx.x * 4 + vi; v < V; v += (int64_t)gridDim.x * 4) {
+    const float* xv = x + v * kFeat;
+    float acc = sb[o];
+#pragma unroll
+    for (int c = 0; c < kFeat; ++c) acc = fmaf(sw[o][c], xv[c], acc);
+    h[v * kHid + o] = __float2bfloat16_rn(fmaxf(acc, 0.0f));
+  }
+}
+
+__global__ void k_hub_sum_bf16(GraphDev g, const __nv_bfloat16* __restrict__ hin, float* __restrict__ hub_sum) {
+  const int lane = threadIdx.x & 31;
+  const __nv_bfloat162* h2 = reinterpret_cast<const __nv_bfloat162*>(hin);
+  for (int64_t c = gwarp(); c < g.nchunks; c += nwarps()) {
+    const int2 hc = g.hub_chunk[c];
+    const int32_t u = g.big[hc.x];
+    const int32_t end = min(g.row_ptr[u + 1], hc.y + 32);
+    float ax = 0.0f, ay = 0.0f;
+    for (int32_t e = hc.y; e < end; ++e) {
+      const float2 f = __bfloat1622float2(h2[(int64_t)g.adj[e].x * (kHid / 2) + lane]);
+      ax += f.x;
+      ay += f.y;
+    }
+    atomicAdd(hub_sum + (int64_t)hc.x * kHid + 2 * lane, ax);
+    atomicAdd(hub_sum + (int64_t)hc.x * kHid + 2 * lane + 1, ay);
+  }
+}
+
+__device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
+  const __nv_bfloat162 b = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<const uint32_t*>(&b);
+}
+
+// D += A * B for one m16n8k16 tile (bf16 in, fp32 accumulate)
+__device__ __forceinline__ void mma_bf16(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
+                                         uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+constexpr int kInfWarps = 4;
+constexpr int kRowPad = 2 * kHid + 8;  // bf16 per shared row: 68 words, so fragment reads hit 32 banks
+
+// One message-passing layer over 16-vertex tiles per warp. The warp stages
+// A = [h(v) | mean_{u in N(v)} h(u)] (16 x 128, bf16) in shared memory,
+// multiplies it by [Ws | Wn]^T (128 x 64) with 8 x 8 mma tiles, adds the
+// bias, applies the ReLU and stores bf16 activations, or on the last
+// layer reduces them against wo into scores.
+__global__ void __launch_bounds__(kInfWarps * 32) k_infer_layer(GraphDev g, const int32_t* __restrict__ hub_of,
+                                                                const float* __restrict__ hub_sum,
+                                                                const __nv_bfloat16* __restrict__ hin,
+                                                                const __nv_bfloat16* __restrict__ wcat,
+                                                                const float* __restrict__ bias,
+                                                                const float* __restrict__ wo,
+                                                                const float* __restrict__ bo_ptr,
+                                                                __nv_bfloat16* __restrict__ hout,
+                                                                float* __restrict__ scores) {
+  __shared__ __align__(16) __nv_bfloat16 sB[kHid][kRowPad];
+  __shared__ __align__(16) __nv_bfloat16 sA[kInfWarps][16][kRowPad];
+  __shared__ float sbias[kHid], swo[kHid];
+  for (int i = threadIdx.x; i < kHid * 2 * kHid / 2; i += blockDim.x) {
+    const int o = i / kHid, c2 = i % kHid;  // pairs of columns
+    reinterpret_cast<uint32_t*>(&sB[o][0])[c2] = reinterpret_cast<const uint32_t*>(wcat)[i];
+  }
+  if (threadIdx.x < kHid) {
+    sbias[threadIdx.x] = bias[threadIdx.x];
+    swo[threadIdx.x] = wo ? wo[threadIdx.x] : 0.0f;
+  }
+  __syncthreads();
+  const float bo = bo_ptr ? *bo_ptr : 0.0f;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int gq = lane >> 2, tq = lane & 3;
+  const __nv_bfloat162* h2 = reinterpret_cast<const __nv_bfloat162*>(hin);
+  const int64_t ntiles = ((int64_t)g.V + 15) / 16;
+  for (int64_t tile = (int64_t)blockIdx.x * kInfWarps + w; tile < ntiles; tile += (int64_t)gridDim.x * kInfWarps) {
+    for (int i = 0; i < 16; ++i) {
+      const int64_t v = tile * 16 + i;
+      uint32_t hv = 0, av = 0;
+      if (v < g.V) {
+        hv = *reinterpret_cast<const uint32_t*>(&h2[v * (kHid / 2) + lane]);
+        const int32_t beg = g.row_ptr[v], end = g.row_ptr[v + 1];
+        const float inv = end > beg ? 1.0f / (float)(end - beg) : 0.0f;
+        float ax = 0.0f, ay = 0.0f;
+        const int32_t hb = hub_of[v];
+        if (hb >= 0) {
+          ax = hub_sum[(int64_t)hb * kHid + 2 * lane];
+          ay = hub_sum[(int64_t)hb * kHid + 2 * lane + 1];
+        } else {
+          int32_t e = beg;
+          for (; e + 4 <= end; e += 4) {
+            float2 f[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) f[j] = __bfloat1622float2(h2[(int64_t)g.adj[e + j].x * (kHid / 2) + lane]);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+              ax += f[j].x;
+              ay += f[j].y;
+            }
+          }
+          for (; e < end; ++e) {
+            const float2 f = __bfloat1622float2(h2[(int64_t)g.adj[e].x * (kHid / 2) + lane]);
+            ax += f.x;
+            ay += f.y;
+          }
+        }
+        av = pack_bf16x2(ax * inv, ay * inv);
+      }
+      reinterpret_cast<uint32_t*>(&sA[w][i][0])[lane] = hv;
+      reinterpret_cast<uint32_t*>(&sA[w][i][kHid])[lane] = av;
+    }
+    __syncwarp();
+    float acc[kHid / 8][4];
+#pragma unroll
+    for (int nt = 0; nt < kHid / 8; ++nt) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.0f;
+#pragma unroll
+    for (int kt = 0; kt < 2 * kHid / 16; ++kt) {
+      const int c = kt * 16 + 2 * tq;
+      const uint32_t a0 = *reinterpret_cast<const uint32_t*>(&sA[w][gq][c]);
+      const uint32_t a1 = *reinterpret_cast<const uint32_t*>(&sA[w][gq + 8][c]);
+      const uint32_t a2 = *reinterpret_cast<const uint32_t*>(&sA[w][gq][c + 8]);
+      const uint32_t a3 = *reinterpret_cast<const uint32_t*>(&sA[w][gq + 8][c + 8]);
+#pragma unroll
+      for (int nt = 0; nt < kHid / 8; ++nt) {
+        const uint32_t b0 = *reinterpret_cast<const uint32_t*>(&sB[nt * 8 + gq][c]);
+        const uint32_t b1 = *reinterpret_cast<const uint32_t*>(&sB[nt * 8 + gq][c + 8]);
+        mma_bf16(acc[nt], a0, a1, a2, a3, b0, b1);
+      }
+    }
+    const int64_t v0 = tile * 16 + gq, v1 = v0 + 8;
+    if (scores) {
+      float s0 = 0.0f, s1 = 0.0f;
+#pragma unroll
+      for (int nt = 0; nt < kHid / 8; ++nt) {
+        const int col = nt * 8 + 2 * tq;
+        s0 += fmaxf(acc[nt][0] + sbias[col], 0.0f) * swo[col] + fmaxf(acc[nt][1] + sbias[col + 1], 0.0f) * swo[col + 1];
+        s1 += fmaxf(acc[nt][2] + sbias[col], 0.0f) * swo[col] + fmaxf(acc[nt][3] + sbias[col + 1], 0.0f) * swo[col + 1];
+      }
+      s0 += __shfl_xor_sync(0xffffffffu, s0, 1);
+      s0 += __shfl_xor_sync(0xffffffffu, s0, 2);
+      s1 += __shfl_xor_sync(0xffffffffu, s1, 1);
+      s1 += __shfl_xor_sync(0xffffffffu, s1, 2);
+      if (tq == 0) {
+        if (v0 < g.V) scores[v0] = s0 + bo;
+        if (v1 < g.V) scores[v1] = s1 + bo;
+      }
+    } else {
+      uint32_t* o2 = reinterpret_cast<uint32_t*>(hout);
+#pragma unroll
+      for (int nt = 0; nt < kHid / 8; ++nt) {
+        const int col = nt * 8 + 2 * tq;
+        if (v0 < g.V)
+          o2[(v0 * kHid + col) / 2] =
+              pack_bf16x2(fmaxf(acc[nt][0] + sbias[col], 0.0f), fmaxf(acc[nt][1] + sbias[col + 1], 0.0f));
+        if (v1 < g.V)
+          o2[(v1 * kHid + col) / 2] =
+              pack_bf16x2(fmaxf(acc[nt][2] + sbias[col], 0.0f), fmaxf(acc[nt][3] + sbias[col + 1], 0.0f));
+      }
+    }
+    __syncwarp();
+  }
+}
+
+__global__ void k_feature_score(int32_t V, const float* __restrict__ x, float* __restrict__ s) {
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < V; v += (int64_t)gridDim.x * blockDim.x) {
+    const float* f = x + v * kFeat;
+    s[v] = 1000.0f * f[3] + 100.0f * f[4] + 10.0f * f[5] + f[1];
+  }
+}
+
+__device__ __forceinline__ uint32_t order_key(float f) {
+  const uint32_t u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+__global__ void k_argmax(int32_t V, const float* __restrict__ s, unsigned long long* best) {
+  unsigned long long b = 0ull;
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < V; v += (int64_t)gridDim.x * blockDim.x) {
+    const float f = s[v];
+    if (f != f) continue;  // NaN never wins
+    const unsigned long long key = ((unsigned long long)order_key(f) << 32) | (0xffffffffull - (uint64_t)v);
+    b = key > b ? key : b;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long x = __shfl_xor_sync(0xffffffffu, b, o);
+    b = x > b ? x : b;
+  }
+  if ((threadIdx.x & 31) == 0 && b) atomicMax(best, b);
+}
+
+// -------------------------------------------------------------- training --
+// block: 4 vertices x 64 outputs; W rows padded by one float
+__global__ void __launch_bounds__(256) k_dense_fwd(int32_t V, const float* __restrict__ x1, int k1,
+                                                   const float* __restrict__ w1, const float* __restrict__ x2,
+                                                   const float* __restrict__ w2, const float* __restrict__ b,
+                                                   float* __restrict__ y) {
+  __shared__ float sw1[kHid][kHid + 1], sw2[kHid][kHid + 1];
+  __shared__ float sx1[4][kHid], sx2[4][kHid];
+  for (int i = threadIdx.x; i < kHid * k1; i += blockDim.x) sw1[i / k1][i % k1] = w1[i];
+  if (x2)
+    for (int i = threadIdx.x; i < kHid * kHid; i += blockDim.x) sw2[i / kHid][i % kHid] = w2[i];
+  const int o = threadIdx.x & (kHid - 1), vi = threadIdx.x >> 6;
+  const float bo = b[o];
+  for (int64_t vb = (int64_t)blockIdx.x * 4; vb < V; vb += (int64_t)gridDim.x * 4) {
+    __syncthreads();
+    const int64_t v = vb + vi;
+    if (o < k1) sx1[vi][o] = v < V ? x1[v * k1 + o] : 0.0f;
+    if (x2) sx2[vi][o] = v < V ? x2[v * kHid + o] : 0.0f;
+    __syncthreads();
+    if (v >= V) continue;
+    float acc = bo;
+    for (int c = 0; c < k1; ++c) acc = fmaf(sw1[o][c], sx1[vi][c], acc);
+    if (x2)
+      for (int c = 0; c < kHid; ++c) acc = fmaf(sw2[o][c], sx2[vi][c], acc);
+    y[v * kHid + o] = fmaxf(acc, 0.0f);
+  }
+}
+
+__global__ void __launch_bounds__(256) k_dense_bwd_data(int32_t V, const float* __restrict__ dz,
+                                                        const float* __restrict__ w, float* __restrict__ y) {
+  __shared__ float sw[kHid][kHid];
+  __shared__ float sdz[4][kHid];
+  for (int i = threadIdx.x; i < kHid * kHid; i += blockDim.x) sw[i / kHid][i % kHid] = w[i];
+  const int c = threadIdx.x & (kHid - 1), vi = threadIdx.x >> 6;
+  for (int64_t vb = (int64_t)blockIdx.x * 4; vb < V; vb += (int64_t)gridDim.x * 4) {
+    __syncthreads();
+    const int64_t v = vb + vi;
+    sdz[vi][c] = v < V ? dz[v * kHid + c] : 0.0f;
+    __syncthreads();
+    if (v >= V) continue;
+    float acc = 0.0f;
+    for (int o = 0; o < kHid; ++o) acc = fmaf(sdz[vi][o], sw[o][c], acc);
+    y[v * kHid + c] = acc;
+  }
+}
+
+// thread t owns output row o = t / 4 and columns c = t % 4 + 4 j
+__global__ void __launch_bounds__(256) k_dense_bwd_weight(int32_t V, const float* __restrict__ dz,
+                                                          const float* __restrict__ x, int k, float* __restrict__ dw,
+                                                          float* __restrict__ db) {
+  constexpr int kChunk = 32;
+  __shared__ float sdz[kChunk][kHid + 1];
+  __shared__ float sx[kChunk][kHid + 1];
+  const int o = threadIdx.x >> 2, cl = threadIdx.x & 3;
+  const int nc = k / 4;  // columns per thread (k is a multiple of 4, at most kHid)
+  float acc[kHid / 4];
+#pragma unroll
+  for (int j = 0; j < kHid / 4; ++j) acc[j] = 0.0f;
+  float accb = 0.0f;
+  for (int64_t vb = (int64_t)blockIdx.x * kChunk; vb < V; vb += (int64_t)gridDim.x * kChunk) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < kChunk * kHid; i += blockDim.x) {
+      const int r = i / kHid, c = i % kHid;
+      const int64_t v = vb + r;
+      sdz[r][c] = v < V ? dz[v * kHid + c] : 0.0f;
+      if (c < k) sx[r][c] = v < V ? x[v * k + c] : 0.0f;
+    }
+    __syncthreads();
+    for (int r = 0; r < kChunk; ++r) {
+      const float d = sdz[r][o];
+      accb += d;
+#pragma unroll
+      for (int j = 0; j < kHid / 4; ++j)
+        if (j < nc) acc[j] = fmaf(d, sx[r][cl + 4 * j], acc[j]);
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < kHid / 4; ++j)
+    if (j < nc) atomicAdd(dw + o * k + cl + 4 * j, acc[j]);
+  if (db && cl == 0) atomicAdd(db + o, accb);
+}
+
+__global__ void k_mean_agg(GraphDev g, const float* __restrict__ x, float* __restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  const float2* x2 = reinterpret_cast<const float2*>(x);
+  for (int64_t v = gwarp(); v < g.V; v += nwarps()) {
+    const int32_t beg = g.row_ptr[v], end = g.row_ptr[v + 1];
+    float ax = 0.0f, ay = 0.0f;
+    for (int32_t e = beg; e < end; ++e) {
+      const float2 f = x2[(int64_t)g.adj[e].x * (kHid / 2) + lane];
+      ax += f.x;
+      ay += f.y;
+    }
+    const float inv = end > beg ? 1.0f / (float)(end - beg) : 0.0f;
+    reinterpret_cast<float2*>(out)[v * (kHid / 2) + lane] = make_float2(ax * inv, ay * inv);
+  }
+}
+
+__global__ void k_agg_bwd(GraphDev g, const float* __restrict__ t, const float* __restrict__ add,
+                          const float* __restrict__ h, float* __restrict__ dz_prev) {
+  const int lane = threadIdx.x & 31;
+  const float2* t2 = reinterpret_cast<const float2*>(t);
+  for (int64_t u = gwarp(); u < g.V; u += nwarps()) {
+    const int32_t beg = g.row_ptr[u], end = g.row_ptr[u + 1];
+    float2 a = reinterpret_cast<const float2*>(add)[u * (kHid / 2) + lane];
+    for (int32_t e = beg; e < end; ++e) {
+      const int32_t v = g.adj[e].x;
+      const int32_t dv = g.row_ptr[v + 1] - g.row_ptr[v];  // >= 1: v lists u
+      const float inv = 1.0f / (float)dv;
+      const float2 f = t2[(int64_t)v * (kHid / 2) + lane];
+      a.x = fmaf(f.x, inv, a.x);
+      a.y = fmaf(f.y, inv, a.y);
+    }
+    const float2 hh = reinterpret_cast<const float2*>(h)[u * (kHid / 2) + lane];
+    reinterpret_cast<float2*>(dz_prev)[u * (kHid / 2) + lane] =
+        make_float2(hh.x > 0.0f ? a.x : 0.0f, hh.y > 0.0f ? a.y : 0.0f);
+  }
+}
+
+__global__ void k_score(int32_t V, const float* __restrict__ h, const float* __restrict__ p, float* __restrict__ s) {
+  const int lane = threadIdx.x & 31;
+  const float2 wo = reinterpret_cast<const float2*>(p + kOffWo)[lane];
+  const float bo = p[kOffBo];
+  for (int64_t v = gwarp(); v < V; v += nwarps()) {
+    const float2 f = reinterpret_cast<const float2*>(h)[v * (kHid / 2) + lane];
+    float acc = f.x * wo.x + f.y * wo.y;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) s[v] = acc + bo;
+  }
+}
+
+__device__ __forceinline__ int32_t float_ord(float f) {
+  const int32_t i = __float_as_int(f);
+  return i >= 0 ? i : i ^ 0x7fffffff;
+}
+__device__ __forceinline__ float ord_float(int32_t i) { return __int_as_float(i >= 0 ? i : i ^ 0x7fffffff); }
+
+__global__ void k_loss_init(float* red) {
+  reinterpret_cast<int32_t*>(red)[0] = float_ord(-3.0e38f);
+  red[1] = 0.0f;
+}
+
+__global__ void k_loss_max(int32_t V, const float* __restrict__ s, float* red) {
+  float m = -3.0e38f;
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < V; v += (int64_t)gridDim.x * blockDim.x)
+    m = fmaxf(m, s[v]);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(reinterpret_cast<int32_t*>(red), float_ord(m));
+}
+
+__global__ void k_loss_sum(int32_t V, const float* __restrict__ s, float* red) {
+  const float m = ord_float(reinterpret_cast<const int32_t*>(red)[0]);
+  float acc = 0.0f;
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < V; v += (int64_t)gridDim.x * blockDim.x)
+    acc += expf(s[v] - m);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(red + 1, acc);
+}
+
+__global__ void k_loss_grad(int32_t V, const float* __restrict__ s, const uint8_t* __restrict__ label, int32_t n,
+                            const float* red, float* __restrict__ ds, float* loss) {
+  const float m = ord_float(reinterpret_cast<const int32_t*>(red)[0]);
+  const float sum = red[1];
+  const float lse = m + logf(sum);
+  const float inv_n = 1.0f / (float)n;
+  float acc = 0.0f;
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < V; v += (int64_t)gridDim.x * blockDim.x) {
+    const float p = expf(s[v] - m) / sum;
+    const bool y = label[v] != 0;
+    ds[v] = p - (y ? inv_n : 0.0f);
+    if (y) acc -= (s[v] - lse) * inv_n;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0 && acc != 0.0f) atomicAdd(loss, acc);
+}
+
+// block: 4 vertex lanes x 64 channels
+__global__ void __launch_bounds__(256) k_out_bwd(int32_t V, const float* __restrict__ ds, const float* __restrict__ h,
+                                                 const float* __restrict__ p, float* __restrict__ grad,
+                                                 float* __restrict__ dz) {
+  __shared__ float red[4][kHid];
+  __shared__ float redb[4];
+  const int c = threadIdx.x & (kHid - 1), vi = threadIdx.x >> 6;
+  const float wo = p[kOffWo + c];
+  float acc = 0.0f, accb = 0.0f;
+  for (int64_t v = (int64_t)blockIdx.x * 4 + vi; v < V; v += (int64_t)gridDim.x * 4) {
+    const float d = ds[v];
+    const float hv = h[v * kHid + c];
+    acc = fmaf(d, hv, acc);
+    if (c == 0) accb += d;
+    dz[v * kHid + c] = hv > 0.0f ? d * wo : 0.0f;
+  }
+  red[vi][c] = acc;
+  if (c == 0) redb[vi] = accb;
+  __syncthreads();
+  if (vi == 0) {
+    atomicAdd(grad + kOffWo + c, red[0][c] + red[1][c] + red[2][c] + red[3][c]);
+    if (c == 0) atomicAdd(grad + kOffBo, redb[0] + redb[1] + redb[2] + redb[3]);
+  }
+}
+
+__global__ void k_adam(int64_t n, float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m,
+                       float* __restrict__ v, float lr, float c1, float c2) {
+  const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.0f - b1) * gi;
+    const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+  }
+}
+
+__global__ void k_set_labels(const int32_t* __restrict__ ids, int32_t n, uint8_t* __restrict__ label) {
+  for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) label[ids[i]] = 1;
+}
+
+__global__ void __launch_bounds__(256) k_ub_paths(GraphDev g, const int32_t* __restrict__ dist,
+                                                  const int32_t* __restrict__ par, int32_t stride,
+                                                  const int32_t* __restrict__ group_ptr,
+                                                  const int32_t* __restrict__ members, const int32_t* __restrict__ perm,
+                                                  int3* __restrict__ out_e, int32_t* out_n, int32_t cap) {
+  __shared__ unsigned long long best;
+  if (threadIdx.x == 0) best = ~0ull;
+  __syncthreads();
+  const int gi = blockIdx.x;
+  unsigned long long b = ~0ull;
+  for (int32_t i = group_ptr[gi] + threadIdx.x; i < group_ptr[gi + 1]; i += blockDim.x) {
+    const int32_t v = perm[members[i]];
+    const int32_t d = dist[(int64_t)v * stride];
+    if (d < kInf) {
+      const unsigned long long key = ((unsigned long long)(uint32_t)d << 32) | (uint32_t)v;
+      b = key < b ? key : b;
+    }
+  }
+  atomicMin(&best, b);
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  if (best == ~0ull) {
+    atomicExch(out_n + 2, 1);
+    return;
+  }
+  int32_t v = (int32_t)(best & 0xffffffffull);
+  for (int32_t step = 0; step <= g.V; ++step) {
+    const int32_t e = par[(int64_t)v * stride];
+    if (e == kLeaf) return;  // the root
+    if (e < g.row_ptr[v] || e >= g.row_ptr[v + 1]) break;  // not a growth record: stop
+    const int2 x = g.adj[e];
+    const int32_t i = atomicAdd(out_n, 1);
+    if (i >= cap) break;
+    out_e[i] = make_int3(v, x.x, x.y);
+    v = x.x;
+  }
+  atomicExch(out_n + 1, 1);
+}
+
+}  // namespace
+
+// -------------------------------------------------------------- launchers --
+cudaError_t launch_reach(const GraphDev& g, const uint32_t* in, uint32_t* out, int32_t* member_nbrs,
+                         cudaStream_t s) {
+  k_reach<<<grid_for((int64_t)g.V * 32, 256), 256, 0, s>>>(g, in, out, member_nbrs);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_features(const GraphDev& g, const uint32_t* m0, const uint32_t* r1, const uint32_t* r2,
+                            const uint32_t* r3, const int32_t* member_nbrs, int32_t k, float* x, cudaStream_t s) {
+  k_features<<<grid_for(g.V, 256), 256, 0, s>>>(g, m0, r1, r2, r3, member_nbrs, k, x);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pack_bf16(const float* params, __nv_bfloat16* wcat, cudaStream_t s) {
+  k_pack_bf16<<<96, 256, 0, s>>>(params, wcat);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_infer_l0(int32_t V, const float* x, const float* params, __nv_bfloat16* h0, cudaStream_t s) {
+  k_infer_l0<<<grid_for(V, 4), 256, 0, s>>>(V, x, params, h0);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_hub_sum_bf16(const GraphDev& g, const __nv_bfloat16* hin, float* hub_sum, cudaStream_t s) {
+  if (g.nchunks == 0) return cudaSuccess;
+  k_hub_sum_bf16<<<grid_for(g.nchunks * 32, 256), 256, 0, s>>>(g, hin, hub_sum);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_infer_layer(const GraphDev& g, const int32_t* hub_of, const float* hub_sum,
+                               const __nv_bfloat16* hin, const __nv_bfloat16* wcat_l, const float* params, int l,
+                               __nv_bfloat16* hout, float* scores, cudaStream_t s) {
+  const float* bias = params + layer_off(l) + 2 * kHid * kHid;
+  const float* wo = scores ? params + kOffWo : nullptr;
+  const float* bo = scores ? params + kOffBo : nullptr;
+  const int64_t tiles = ((int64_t)g.V + 15) / 16;
+  k_infer_layer<<<grid_for(tiles, kInfWarps, 152 * 12), kInfWarps * 32, 0, s>>>(g, hub_of, hub_sum, hin, wcat_l,
+                                                                                bias, wo, bo, hout, scores);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_feature_score(int32_t V, const float* x, float* s, cudaStream_t st) {
+  k_feature_score<<<grid_for(V, 256), 256, 0, st>>>(V, x, s);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_argmax(int32_t V, const float* scores, unsigned long long* best, cudaStream_t s) {
+  k_argmax<<<grid_for(V, 256, 152 * 4), 256, 0, s>>>(V, scores, best);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_dense_fwd(int32_t V, const float* x1, int k1, const float* w1, const float* x2, const float* w2,
+                             const float* b, float* y, cudaStream_t s) {
+  k_dense_fwd<<<grid_for(V, 4, 152 * 8), 256, 0, s>>>(V, x1, k1, w1, x2, w2, b, y);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_dense_bwd_data(int32_t V, const float* dz, const float* w, float* y, cudaStream_t s) {
+  k_dense_bwd_data<<<grid_for(V, 4, 152 * 8), 256, 0, s>>>(V, dz, w, y);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_dense_bwd_weight(int32_t V, const float* dz, const float* x, int k, float* dw, float* db,
+                                    cudaStream_t s) {
+  k_dense_bwd_weight<<<grid_for(V, 32, 152 * 2), 256, 0, s>>>(V, dz, x, k, dw, db);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mean_agg(const GraphDev& g, const float* x, float* out, cudaStream_t s) {
+  k_mean_agg<<<grid_for((int64_t)g.V * 32, 256), 256, 0, s>>>(g, x, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_agg_bwd(const GraphDev& g, const float* t, const float* add, const float* h, float* dz_prev,
+                           cudaStream_t s) {
+  k_agg_bwd<<<grid_for((int64_t)g.V * 32, 256), 256, 0, s>>>(g, t, add, h, dz_prev);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_score(int32_t V, const float* h, const float* params, float* s, cudaStream_t st) {
+  k_score<<<grid_for((int64_t)V * 32, 256), 256, 0, st>>>(V, h, params, s);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_softmax_loss(int32_t V, const float* s, const uint8_t* label, int32_t n, float* ds, float* loss,
+                                float* red, cudaStream_t st) {
+  const int gb = grid_for(V, 256, 152 * 4);
+  k_loss_init<<<1, 1, 0, st>>>(red);
+  k_loss_max<<<gb, 256, 0, st>>>(V, s, red);
+  k_loss_sum<<<gb, 256, 0, st>>>(V, s, red);
+  k_loss_grad<<<gb, 256, 0, st>>>(V, s, label, n, red, ds, loss);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_out_bwd(int32_t V, const float* ds, const float* h, const float* params, float* grad, float* dz,
+                           cudaStream_t s) {
+  k_out_bwd<<<grid_for(V, 4, 152 * 8), 256, 0, s>>>(V, ds, h, params, grad, dz);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_set_labels(const int32_t* ids, int32_t n, uint8_t* label, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_set_labels<<<grid_for(n, 256, 64), 256, 0, s>>>(ids, n, label);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ub_paths(const GraphDev& g, const int32_t* dist, const int32_t* par, int32_t stride,
+                            const int32_t* group_ptr, const int32_t* members, const int32_t* perm, int32_t k,
+                            int3* out_e, int32_t* out_n, int32_t cap, cudaStream_t s) {
+  k_ub_paths<<<k, 256, 0, s>>>(g, dist, par, stride, group_ptr, members, perm, out_e, out_n, cap);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_adam(int64_t n, float* p, const float* g, float* m, float* v, float lr, int32_t t, cudaStream_t s) {
+  double c1 = 1.0, c2 = 1.0;
+  for (int32_t i = 0; i < t; ++i) {
+    c1 *= 0.9;
+    c2 *= 0.999;
+  }
+  k_adam<<<grid_for(n, 256, 256), 256, 0, s>>>(n, p, g, m, v, lr, (float)(1.0 - c1), (float)(1.0 - c2));
+  return cudaGetLastError();
+}
+
+}  // namespace gst

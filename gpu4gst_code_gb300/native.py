@@ -1,4 +1,4 @@
-"""ctypes binding of libgst.so (include/gst.h, include/gst_gen.h).
+"""ctypes binding of libgst.so (include/gst.h, gst_gen.h, gst_learn.h, gst_debug.h).
 
 The library is the product: every solve runs the CUDA kernels in libgst.so.
 There is no Python or CPU fallback; if the library is missing this module
@@ -18,10 +18,14 @@ LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libgst.so"
 I32P = C.POINTER(C.c_int32)
 I64P = C.POINTER(C.c_int64)
 F64P = C.POINTER(C.c_double)
+F32P = C.POINTER(C.c_float)
 
 MAX_K = 16
 COST_LIMIT = 1073741823
 NOALLOC_MAX_VERTICES = 1 << 20
+SCORER_NUM_PARAMS = 25921
+SCORER_FEATURES = 16
+SCORER_HIDDEN = 64
 
 
 class Status(enum.IntEnum):
@@ -83,6 +87,23 @@ SIGNATURES = {
         [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int64, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p,
          C.c_void_p],
     ),
+    # learned proposal (include/gst_learn.h)
+    "gst_scorer_num_params": (C.c_int64, []),
+    "gst_scorer_create": (C.c_int, [F32P, C.POINTER(C.c_void_p)]),
+    "gst_scorer_free": (None, [C.c_void_p]),
+    "gst_scorer_get_params": (C.c_int, [C.c_void_p, F32P]),
+    "gst_scorer_scores": (C.c_int, [C.c_void_p, C.c_void_p, I32P, I32P, C.c_int32, C.c_int32, F32P]),
+    "gst_scorer_train_step": (
+        C.c_int,
+        [C.c_void_p, C.c_void_p, I32P, I32P, C.c_int32, I32P, C.c_int32, C.c_float, C.c_int32, F32P, F32P],
+    ),
+    "gst_propose": (C.c_int, [C.c_void_p, C.c_void_p, I32P, I32P, C.c_int32, C.POINTER(C.c_void_p)]),
+    "gst_solve_learned": (
+        C.c_int,
+        [C.c_void_p, C.c_void_p, I32P, I32P, C.c_int32, C.POINTER(Opts), C.POINTER(C.c_void_p)],
+    ),
+    "gst_result_upper_bound": (C.c_int32, [C.c_void_p]),
+    "gst_result_proposal_ms": (C.c_double, [C.c_void_p]),
     "gst_last_error": (C.c_char_p, []),
     "gst_version": (C.c_char_p, []),
     # generators (include/gst_gen.h)
@@ -155,6 +176,8 @@ class Result:
     launches: int = 0
     times_ms: tuple = (0.0, 0.0, 0.0, 0.0)
     stats: dict = field(default_factory=dict)
+    upper_bound: int = 0  # bound that pruned a learned solve (0: none)
+    proposal_ms: float = 0.0
 
     @property
     def feasible(self) -> bool:
@@ -189,6 +212,8 @@ def _read_result(r) -> Result:
         launches=int(L.gst_result_launches(r)),
         times_ms=tuple(t),
         stats=dict(zip(STAT_NAMES, list(s))),
+        upper_bound=int(L.gst_result_upper_bound(r)),
+        proposal_ms=float(L.gst_result_proposal_ms(r)),
     )
 
 
@@ -270,6 +295,40 @@ class Graph:
             res = Result(Status(st), -1, -1, np.zeros(0, np.int32), np.zeros((0, 3), np.int32), 0)
         return res
 
+    def _call_result(self, fn, *args, raise_on_error=True) -> Result:
+        r = C.c_void_p()
+        st = fn(*args, C.byref(r))
+        msg = last_error()
+        try:
+            res = _read_result(r) if r.value else None
+        finally:
+            if r.value:
+                lib().gst_result_free(r)
+        if st not in (Status.OK, Status.INFEASIBLE) and raise_on_error:
+            raise GSTError(st, msg)
+        if res is None:
+            res = Result(Status(st), -1, -1, np.zeros(0, np.int32), np.zeros((0, 3), np.int32), 0)
+        return res
+
+    def propose(self, scorer, group_ptr, members=None) -> Result:
+        """Feasible tree from the scorer's top vertex (scorer None: fixed feature score)."""
+        if members is None:
+            group_ptr, members = groups_to_csr(group_ptr)
+        gp, mem = _i32(group_ptr), _i32(members)
+        h = scorer._h if scorer is not None else None
+        return self._call_result(lib().gst_propose, self._h, h, _ptr(gp), _ptr(mem), len(gp) - 1)
+
+    def solve_learned(self, scorer, group_ptr, members=None, *, max_rounds=0, use_graph=True,
+                      collect_stats=False, dense_shift=0, raise_on_error=True) -> Result:
+        """Proposal, then the exact DP pruned by its cost (gst_solve_learned)."""
+        if members is None:
+            group_ptr, members = groups_to_csr(group_ptr)
+        gp, mem = _i32(group_ptr), _i32(members)
+        o = make_opts(0, max_rounds, use_graph, collect_stats, dense_shift)
+        h = scorer._h if scorer is not None else None
+        return self._call_result(lib().gst_solve_learned, self._h, h, _ptr(gp), _ptr(mem), len(gp) - 1, C.byref(o),
+                                 raise_on_error=raise_on_error)
+
     def debug_table(self, k: int) -> np.ndarray:
         """(V, 2^k) table of the last solve with k groups (gst_graph_debug_table)."""
         out = np.zeros(self.V * (1 << k), np.int32)
@@ -304,6 +363,66 @@ class Graph:
         if st not in (Status.OK, Status.INFEASIBLE):
             raise GSTError(st, msg)
         return res
+
+
+class Scorer:
+    """The proposal network's parameters on the current GPU (gst_scorer)."""
+
+    def __init__(self, params):
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        if p.shape != (SCORER_NUM_PARAMS,):
+            raise ValueError(f"expected {SCORER_NUM_PARAMS} parameters, got {p.shape}")
+        h = C.c_void_p()
+        st = lib().gst_scorer_create(_ptr(p, F32P), C.byref(h))
+        if st != Status.OK:
+            raise GSTError(st, last_error())
+        self._h = h
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().gst_scorer_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def params(self) -> np.ndarray:
+        out = np.zeros(SCORER_NUM_PARAMS, np.float32)
+        st = lib().gst_scorer_get_params(self._h, _ptr(out, F32P))
+        if st != Status.OK:
+            raise GSTError(st, last_error())
+        return out
+
+    def scores(self, graph: "Graph", group_ptr, members, *, fp32: bool = False) -> np.ndarray:
+        gp, mem = _i32(group_ptr), _i32(members)
+        out = np.zeros(graph.V, np.float32)
+        st = lib().gst_scorer_scores(graph._h, self._h, _ptr(gp), _ptr(mem), len(gp) - 1, int(fp32), _ptr(out, F32P))
+        if st != Status.OK:
+            raise GSTError(st, last_error())
+        return out
+
+    def train_step(self, graph: "Graph", group_ptr, members, tree_vertices, *, lr: float = 1e-3,
+                   apply: bool = True, want_grads: bool = False):
+        """One Adam step on one solved query; returns (loss, grads or None)."""
+        gp, mem = _i32(group_ptr), _i32(members)
+        tv = _i32(tree_vertices)
+        loss = C.c_float(0.0)
+        grads = np.zeros(SCORER_NUM_PARAMS, np.float32) if want_grads else None
+        st = lib().gst_scorer_train_step(graph._h, self._h, _ptr(gp), _ptr(mem), len(gp) - 1, _ptr(tv), len(tv),
+                                         float(lr), int(apply), C.byref(loss),
+                                         _ptr(grads, F32P) if grads is not None else None)
+        if st != Status.OK:
+            raise GSTError(st, last_error())
+        return float(loss.value), grads
 
 
 # ------------------------------------------------------------- generators --

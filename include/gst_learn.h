@@ -1,0 +1,84 @@
+/* Learned upper-bound proposal for the GB300 GST solver (libgst).
+ *
+ * No counterpart in the reference: an addition on top of the DPBF entry
+ * point of gst.h. A small message-passing network scores the vertices of a
+ * query; its top-scored vertex roots a feasible tree (a shortest path from
+ * the root to the nearest member of every group, then an MST repair over
+ * the tree's vertices with non-essential leaves removed). That tree's cost
+ * is a proven upper bound: gst_solve_learned runs the exact DP pruned by it
+ * (exact for any bound >= the optimum) and falls back to the unpruned DP
+ * whenever no proposal can be made. The optimal cost never depends on the
+ * network, only the time to reach it does.
+ *
+ * Network: 16 query features per vertex, h0 = relu(W0 x + b0), three
+ * layers h_l = relu(Ws_l h_{l-1} + Wn_l mean_{N(v)} h_{l-1} + b_l) of width
+ * 64, score = wo . h3 + bo. Parameters are one flat float vector:
+ *   W0[64][16], b0[64], then per layer Ws[64][64], Wn[64][64], b[64],
+ *   then wo[64], bo  (GST_SCORER_NUM_PARAMS floats).
+ * Inference runs in bf16 with fp32 accumulation; training (one query per
+ * step, listwise softmax loss against the vertices of a known optimal
+ * tree, Adam) runs fp32 forward and backward kernels on the device.
+ * Training requires a graph whose CSR lists both directions of every edge
+ * (the backward pass of the mean aggregation walks rows as columns).
+ */
+#ifndef GST_LEARN_H
+#define GST_LEARN_H
+
+#include "gst.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GST_SCORER_FEATURES 16
+#define GST_SCORER_HIDDEN 64
+#define GST_SCORER_LAYERS 3
+#define GST_SCORER_NUM_PARAMS 25921
+
+typedef struct gst_scorer gst_scorer;
+
+/* Parameter count (GST_SCORER_NUM_PARAMS). */
+int64_t gst_scorer_num_params(void);
+
+/* Copies params (GST_SCORER_NUM_PARAMS floats) to the current device. */
+gst_status gst_scorer_create(const float* params, gst_scorer** out);
+void gst_scorer_free(gst_scorer* s);
+/* Current parameters back to the host. */
+gst_status gst_scorer_get_params(const gst_scorer* s, float* out);
+
+/* Scores every vertex for a query (caller vertex IDs, V floats).
+ * precision 0 = bf16 inference path, 1 = fp32 training forward path. */
+gst_status gst_scorer_scores(gst_graph* g, gst_scorer* s, const int32_t* group_ptr, const int32_t* members, int32_t k,
+                             int32_t precision, float* scores);
+
+/* One training step on one query whose optimal tree has the n vertices
+ * tree_vertices (caller IDs). Writes the loss; with grads non-null also
+ * the gradient (GST_SCORER_NUM_PARAMS floats) before any update; with
+ * apply != 0 takes an Adam step of learning rate lr. */
+gst_status gst_scorer_train_step(gst_graph* g, gst_scorer* s, const int32_t* group_ptr, const int32_t* members,
+                                 int32_t k, const int32_t* tree_vertices, int32_t n, float lr, int32_t apply,
+                                 float* loss, float* grads);
+
+/* The proposal alone: a feasible tree (gst_result: cost, vertices, edges)
+ * rooted at the top-scored vertex, or, with s NULL, at the vertex chosen by
+ * a fixed feature score (most groups within 1, then 2, then 3 hops, then
+ * degree): the same pipeline without the network. */
+gst_status gst_propose(gst_graph* g, gst_scorer* s, const int32_t* group_ptr, const int32_t* members, int32_t k,
+                       gst_result** out);
+
+/* Proposal, then the exact DP pruned by the proposal's cost (opts as for
+ * gst_solve; its upper_bound is replaced by the proposal's cost). With s
+ * NULL the fixed feature score roots the proposal. */
+gst_status gst_solve_learned(gst_graph* g, gst_scorer* s, const int32_t* group_ptr, const int32_t* members, int32_t k,
+                             const gst_opts* opts, gst_result** out);
+
+/* Bound that pruned the solve (0 = none, the fallback ran) and the host
+ * wall time of the proposal in ms. */
+int32_t gst_result_upper_bound(const gst_result* r);
+double gst_result_proposal_ms(const gst_result* r);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GST_LEARN_H */

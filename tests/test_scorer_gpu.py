@@ -1,0 +1,112 @@
+"""GPU checks of the learned proposal through the C ABI (gst_learn.h):
+fp32 forward and gradients of the device training kernels against the
+numpy oracle, bf16 inference against the same, feasibility of the proposed
+tree, and exactness of the proposal-pruned solve."""
+import numpy as np
+import pytest
+
+import oracle
+from oracle import scorer_oracle as SO
+
+pytestmark = pytest.mark.gpu
+
+
+def ba_case(V=3000, k=4, seed=0):
+    from gpu4gst_code_gb300 import native as N
+
+    g = N.gen_barabasi_albert(V, 4, 1, 100, seed)
+    gp, mem = N.gen_groups_zipf_degree(g, k, 1.2, 5, 60, seed + 11)
+    return g, gp, mem
+
+
+def rel_err(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-12))
+
+
+@pytest.fixture(scope="module")
+def case():
+    from gpu4gst_code_gb300 import learn, native as N
+
+    g, gp, mem = ba_case()
+    p = learn.init_params(1)
+    with N.Graph(g.row_ptr, g.col, g.w) as dg:
+        tree = dg.solve(gp, mem).vertices
+    A = SO.adjacency(g.row_ptr, g.col)
+    x = SO.features(g.row_ptr, g.col, gp, mem)
+    return g, gp, mem, p, tree, A, x
+
+
+def test_fp32_scores_match_oracle(case):
+    from gpu4gst_code_gb300 import native as N
+
+    g, gp, mem, p, tree, A, x = case
+    want, _, _ = SO.forward(p.astype(np.float64), A, x)
+    with N.Graph(g.row_ptr, g.col, g.w) as dg, N.Scorer(p) as sc:
+        got = sc.scores(dg, gp, mem, fp32=True)
+    assert np.abs(got - want).max() <= 1e-4 * (1 + np.abs(want).max())
+
+
+def test_bf16_inference_tracks_oracle(case):
+    from gpu4gst_code_gb300 import native as N
+
+    g, gp, mem, p, tree, A, x = case
+    want, _, _ = SO.forward(p.astype(np.float64), A, x)
+    with N.Graph(g.row_ptr, g.col, g.w) as dg, N.Scorer(p) as sc:
+        got = sc.scores(dg, gp, mem)
+    # bf16 keeps 8 significant bits: errors stay within a few percent of the score range
+    assert np.abs(got - want).max() <= 0.03 * (np.abs(want).max() + 1e-6)
+    assert np.corrcoef(got, want)[0, 1] > 0.999
+
+
+def test_gradients_match_oracle(case):
+    from gpu4gst_code_gb300 import native as N
+
+    g, gp, mem, p, tree, A, x = case
+    want_loss, want = SO.loss_and_grad(p.astype(np.float64), A, x, tree)
+    with N.Graph(g.row_ptr, g.col, g.w) as dg, N.Scorer(p) as sc:
+        loss, got = sc.train_step(dg, gp, mem, tree, apply=False, want_grads=True)
+        assert np.array_equal(sc.params(), p)  # apply=False leaves the parameters
+    assert abs(loss - want_loss) <= 1e-4 * max(1.0, abs(want_loss))
+    gd, wd = SO.unpack(got), SO.unpack(want)
+    floor = 1e-5 * np.linalg.norm(want)  # d/d bo is exactly 0 (softmax sums to one): fp32 leaves ~1e-7
+    for name in wd:
+        err = np.linalg.norm(gd[name] - wd[name])
+        assert err <= 2e-3 * np.linalg.norm(wd[name]) + floor, (name, err)
+
+
+def test_adam_step_matches_numpy(case):
+    from gpu4gst_code_gb300 import native as N
+
+    g, gp, mem, p, tree, A, x = case
+    lr = 1e-3
+    with N.Graph(g.row_ptr, g.col, g.w) as dg, N.Scorer(p) as sc:
+        _, grad = sc.train_step(dg, gp, mem, tree, lr=lr, apply=True, want_grads=True)
+        got = sc.params()
+    grad = grad.astype(np.float64)
+    m = 0.1 * grad  # first step from zero moments
+    v = 0.001 * grad * grad
+    want = p - lr * (m / 0.1) / (np.sqrt(v / 0.001) + 1e-8)
+    assert np.abs(got - want).max() <= 1e-6
+
+
+@pytest.mark.parametrize("use_scorer", [False, True])
+def test_proposal_is_feasible_and_learned_solve_exact(use_scorer):
+    from gpu4gst_code_gb300 import learn, native as N
+
+    for seed in range(6):
+        k = 3 + seed % 4
+        g, gp, mem = ba_case(V=2000 + 500 * seed, k=k, seed=100 + seed)
+        with N.Graph(g.row_ptr, g.col, g.w) as dg, N.Scorer(learn.init_params(seed)) as sc:
+            s = sc if use_scorer else None
+            plain = dg.solve(gp, mem, use_graph=True)
+            prop = dg.propose(s, gp, mem)
+            assert prop.status == N.Status.OK
+            err = oracle.check_tree(g.row_ptr, g.col, g.w, gp, mem, prop.vertices, prop.edges, prop.cost)
+            assert err is None, err
+            assert prop.cost >= plain.cost
+            res = dg.solve_learned(s, gp, mem)
+            assert res.status == N.Status.OK
+            assert res.cost == plain.cost
+            assert res.upper_bound == prop.cost
+            err = oracle.check_tree(g.row_ptr, g.col, g.w, gp, mem, res.vertices, res.edges, res.cost)
+            assert err is None, err
