@@ -70,7 +70,8 @@ struct SolveParams {
   // overflow test. A cost that reaches the limit is reported (GST_OVERFLOW).
   int32_t ovf_limit;
   int32_t dense_shift;  // dense round when the previous one changed > V >> dense_shift
-  int32_t pad[2];
+  int32_t refine;       // lower ub between waves from partial trees (k_ub_refine)
+  int32_t pad;
 };
 
 // Growth-loop control of the current wave (reset before each wave).
@@ -143,6 +144,9 @@ cudaError_t launch_merge(const GraphDev& g, const LevelArgs& a, cudaStream_t str
 cudaError_t launch_grow_round(const GraphDev& g, const LevelArgs& a, int num_sms, cudaStream_t stream,
                               int64_t* launches);
 cudaError_t launch_seed(const GraphDev& g, const LevelArgs& a, int num_sms, cudaStream_t stream);
+// After wave a.level's growth: with params->refine set, lowers params->ub to
+// the cheapest T(v,S) + sum of T(v,{g}) over the groups g outside S.
+cudaError_t launch_ub_refine(const GraphDev& g, const LevelArgs& a, int num_sms, cudaStream_t stream);
 cudaError_t launch_argmin(const GraphDev& g, const int32_t* full_slice, int32_t stride, Counters* ctr,
                           cudaStream_t stream);
 cudaError_t launch_backtrack(const GraphDev& g, int64_t nnz, const int32_t* par, const MaskInfo* minfo,

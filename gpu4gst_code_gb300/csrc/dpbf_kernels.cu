@@ -12,6 +12,7 @@
 //                   (:259-282): one label-correcting round, pull form
 //   k_argmin        host min scan over T(v,full) (:712-721)
 //   k_backtrack     host BFS over parent records (:729-758)
+#include <climits>
 #include <cstdint>
 
 #include "dpbf.cuh"
@@ -899,6 +900,58 @@ __global__ void __launch_bounds__(kGrowThreads, (L >= 3 ? 3 : 4)) k_grow_group(G
   round_end(a, rs, acc, ba);
 }
 
+// ------------------------------------------------------------ bound update --
+// The cost of a feasible subgraph for every state: T(v,S) plus v's wave-1
+// states T(v,{g}) for the groups g outside S (each stored cost is that of
+// an actual tree or path, so the sum bounds the union's cost and hence the
+// optimum from above). The cheapest one lowers params->ub (0 = none yet).
+// The restatement, over all states of a wave at once, of PrunedDP++'s
+// update of its best solution (graph_v_of_v_idealID_PrunedDPPlusPlus.h:668-711).
+__global__ void __launch_bounds__(kGrowThreads) k_ub_refine(GraphDev g, LevelArgs a) {
+  if (!a.params->refine) return;
+  __shared__ long long sbest[kGrowThreads / 32];
+  long long best = LLONG_MAX;
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < g.V; v += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t* d = a.cost + v * a.stride1;
+    int32_t dd[16];
+#pragma unroll
+    for (int gg = 0; gg < 16; ++gg) dd[gg] = gg < a.k ? d[gg] : 0;
+    const int32_t* row = a.cost + a.base + v * a.stride;
+    for (int j = 0; j < a.m; ++j) {
+      const int32_t c = row[j];
+      if (c >= kInf) continue;
+      const uint32_t S = (uint32_t)__ldg(a.lmasks + j);
+      long long sum = c;
+      bool ok = true;
+#pragma unroll
+      for (int gg = 0; gg < 16; ++gg)
+        if (gg < a.k && !((S >> gg) & 1u)) {
+          ok &= dd[gg] < kInf;
+          sum += dd[gg];
+        }
+      if (ok && sum < best) best = sum;
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const long long x = __shfl_xor_sync(0xffffffffu, best, o);
+    best = x < best ? x : best;
+  }
+  if ((threadIdx.x & 31) == 0) sbest[threadIdx.x >> 5] = best;
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  for (int w = 1; w < (int)(blockDim.x >> 5); ++w) best = sbest[w] < best ? sbest[w] : best;
+  if (best >= (long long)kInf) return;
+  int32_t* ub = const_cast<int32_t*>(&a.params->ub);
+  const int32_t cand = (int32_t)best;
+  int32_t old = *reinterpret_cast<volatile int32_t*>(ub);
+  while (old <= 0 || cand < old) {
+    const int32_t prev = atomicCAS(ub, old, cand);
+    if (prev == old) break;
+    old = prev;
+  }
+}
+
 // ----------------------------------------------------------------- argmin --
 __global__ void k_argmin(int32_t V, const int32_t* __restrict__ full_slice, int32_t stride, Counters* ctr) {
   unsigned long long best = ~0ull;
@@ -1087,6 +1140,13 @@ cudaError_t launch_seed(const GraphDev& g, const LevelArgs& a, int num_sms, cuda
   int64_t blocks = ((int64_t)g.V + kGrowThreads - 1) / kGrowThreads;  // >= one warp per 32 vertices
   if (blocks > (int64_t)num_sms * 8) blocks = (int64_t)num_sms * 8;
   k_seed<<<(unsigned)blocks, kGrowThreads, 0, stream>>>(g, a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ub_refine(const GraphDev& g, const LevelArgs& a, int num_sms, cudaStream_t stream) {
+  int64_t blocks = ((int64_t)g.V + kGrowThreads - 1) / kGrowThreads;
+  if (blocks > (int64_t)num_sms * 8) blocks = (int64_t)num_sms * 8;
+  k_ub_refine<<<(unsigned)blocks, kGrowThreads, 0, stream>>>(g, a);
   return cudaGetLastError();
 }
 

@@ -80,6 +80,8 @@ int binom(int n, int r) {
 constexpr int32_t kTreePrefix = 4096;   // tree entries read back with the counters
 constexpr int kPollEvery = 8;           // host loop: rounds launched between polls
 constexpr int kEvents = 3 * GST_MAX_K + 8;
+constexpr int kProposeTop = 256;       // top-scored vertices offered to the proposal's repair
+constexpr int kProposeRounds = 12;     // growth rounds of the proposal's root distances
 }  // namespace
 
 // ---------------------------------------------------------------- objects --
@@ -139,6 +141,9 @@ struct LearnWs {
   float* hub_sum = nullptr;           // nbig x kHid
   float* scores = nullptr;            // V
   unsigned long long* best = nullptr;
+  uint32_t* hist = nullptr;           // kScoreBins
+  uint2* top = nullptr;               // (key, v) of the top-scored vertices
+  int32_t top_cap = 0;
   int3* pe = nullptr;                 // proposal path edges
   int32_t* pn = nullptr;              // [count, stopped, unreachable]
   int32_t pe_cap = 0;
@@ -179,6 +184,7 @@ struct gst_graph {
   int32_t* d_hub_of = nullptr;  // hub index of a vertex, -1 for the others
   std::vector<int32_t> h_row;   // host copy of the internal CSR (proposal repair)
   std::vector<int2> h_adj;
+  std::vector<int32_t> h_slot;  // V-sized scratch of the repair (all zero between uses)
   std::mutex mu;
   Workspace ws;
   LearnWs lw;
@@ -194,8 +200,9 @@ struct gst_result {
   int64_t launches = 0;  // kernels this solve launched
   double ms[4] = {0, 0, 0, 0};
   int64_t stats[kNumStats] = {};
-  int32_t ub = 0;          // bound that pruned the solve (learned path)
-  double propose_ms = 0;   // host wall time of the proposal
+  int32_t ub = 0;             // pruning bound at the last wave (0 = none)
+  int32_t proposal_cost = 0;  // cost of the learned path's proposed tree
+  double propose_ms = 0;      // host wall time of the proposal
 };
 
 struct gst_scorer {
@@ -245,6 +252,8 @@ void free_learn(LearnWs& lw) {
   dfree(lw.hub_sum);
   dfree(lw.scores);
   dfree(lw.best);
+  dfree(lw.hist);
+  dfree(lw.top);
   dfree(lw.pe);
   dfree(lw.pn);
   for (auto& p : lw.h) dfree(p);
@@ -486,6 +495,7 @@ gst_status enqueue_epilogue(gst_graph* g, int32_t k, cudaStream_t s, int64_t* la
   *launches += 2;
   const size_t pre = (size_t)std::min(kTreePrefix, ws.bt_cap);
   GST_CUDA(cudaMemcpyAsync(ws.h_ctr, ws.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, s));
+  GST_CUDA(cudaMemcpyAsync(ws.h_params, ws.d_params, sizeof(SolveParams), cudaMemcpyDeviceToHost, s));
   GST_CUDA(cudaMemcpyAsync(ws.h_stats, ws.stats, kNumStats * sizeof(long long), cudaMemcpyDeviceToHost, s));
   GST_CUDA(cudaMemcpyAsync(ws.h_out_v, ws.out_v, pre * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
   GST_CUDA(cudaMemcpyAsync(ws.h_out_e, ws.out_e, pre * sizeof(int3), cudaMemcpyDeviceToHost, s));
@@ -543,6 +553,8 @@ gst_status build_query_graph(gst_graph* g, int32_t k) {
     if (st == GST_OK && cudaEventRecord(ws.ev[3 * l + 1], s) != cudaSuccess)
       st = fail(GST_CUDA_ERROR, "event record");
     if (st == GST_OK && l < k) st = capture_growth_loop(g, a, s);
+    if (st == GST_OK && l < k && launch_ub_refine(graph_dev(g), a, g->num_sms, s) != cudaSuccess)
+      st = fail(GST_CUDA_ERROR, "bound refinement launch");
     if (st == GST_OK && cudaEventRecord(ws.ev[3 * l + 2], s) != cudaSuccess)
       st = fail(GST_CUDA_ERROR, "event record");
   }
@@ -681,6 +693,8 @@ gst_status run_host_loop(gst_graph* g, int32_t k, int64_t* launches, bool* timeo
         }
         if (ws.h_ctl->last_changed == 0) break;
       }
+      GST_CUDA(launch_ub_refine(gd, a, g->num_sms, s));
+      ++*launches;
     }
     GST_CUDA(cudaEventRecord(ws.ev[3 * l + 2], s));
   }
@@ -713,6 +727,7 @@ gst_status solve_one(gst_graph* g, const int32_t* group_ptr, const int32_t* memb
   ws.h_params->k = k;
   ws.h_params->ovf_limit = kInf - std::max<int32_t>(g->max_w, 1);
   ws.h_params->dense_shift = o.dense_shift > 0 && o.dense_shift < 31 ? o.dense_shift : kDefaultDenseShift;
+  ws.h_params->refine = o.refine_bound ? 1 : 0;
 
   GST_CUDA(cudaEventRecord(ws.ev[0], s));
   GST_CUDA(cudaMemcpyAsync(ws.d_params, ws.h_params, sizeof(SolveParams), cudaMemcpyHostToDevice, s));
@@ -734,7 +749,8 @@ gst_status solve_one(gst_graph* g, const int32_t* group_ptr, const int32_t* memb
   GST_CUDA(cudaEventRecord(ws.ev[2], s));
   GST_CUDA(cudaStreamSynchronize(s));
   const Counters& c = *ws.h_ctr;
-  if (use_graph) launches = 1 + k + (k - 1) + (int64_t)c.rounds_total * (g->nchunks > 0 ? 2 : 1) + 2;
+  if (use_graph) launches = 1 + k + 2 * (k - 1) + (int64_t)c.rounds_total * (g->nchunks > 0 ? 2 : 1) + 2;
+  r->ub = ws.h_params->ub;  // the bound as the last wave saw it (refined on the device)
   r->launches = launches;
   r->states = (int64_t)c.states;
   std::copy(ws.h_stats, ws.h_stats + kNumStats, r->stats);
@@ -772,6 +788,113 @@ gst_opts resolve_opts(const gst_opts* opts) {
 
 
 // ------------------------------------------------------- learned proposal --
+struct TreeEdge {
+  int32_t u, v, w;  // u < v, internal IDs
+  bool operator<(const TreeEdge& o) const { return u != o.u ? u < o.u : (v != o.v ? v < o.v : w < o.w); }
+};
+
+struct HostTree {
+  bool ok = false;
+  int64_t cost = 0;
+  std::vector<int32_t> vertices;  // internal IDs, sorted
+  std::vector<TreeEdge> edges;
+};
+
+// MST of the subgraph induced by `set` (internal IDs), kept to the
+// component of `root`, then leaves removed while every group keeps a
+// member in the tree. ok = the result covers all k groups.
+HostTree mst_repair(gst_graph* g, std::vector<int32_t> set, int32_t root,
+                    const std::unordered_map<int32_t, uint32_t>& gbits, int32_t k) {
+  HostTree out;
+  std::sort(set.begin(), set.end());
+  set.erase(std::unique(set.begin(), set.end()), set.end());
+  const size_t n = set.size();
+  auto idx = [&](int32_t v) -> int64_t {
+    auto it = std::lower_bound(set.begin(), set.end(), v);
+    return (it != set.end() && *it == v) ? it - set.begin() : -1;
+  };
+  // slot + 1 of every set vertex in a V-sized scratch array (zero outside)
+  std::vector<int32_t>& slot = g->h_slot;
+  if (slot.size() != (size_t)g->V) slot.assign((size_t)g->V, 0);
+  for (size_t i = 0; i < n; ++i) slot[(size_t)set[i]] = (int32_t)i + 1;
+  std::vector<std::pair<int32_t, std::pair<int32_t, int32_t>>> ind;  // (w, (i, j))
+  for (size_t i = 0; i < n; ++i) {
+    const int32_t v = set[i];
+    for (int32_t e = g->h_row[(size_t)v]; e < g->h_row[(size_t)v + 1]; ++e) {
+      const int2 x = g->h_adj[(size_t)e];
+      if (x.x <= v) continue;
+      const int32_t j = slot[(size_t)x.x] - 1;
+      if (j >= 0) ind.push_back({x.y, {(int32_t)i, j}});
+    }
+  }
+  for (size_t i = 0; i < n; ++i) slot[(size_t)set[i]] = 0;
+  std::sort(ind.begin(), ind.end());
+  std::vector<int32_t> dsu(n);
+  for (size_t i = 0; i < n; ++i) dsu[i] = (int32_t)i;
+  auto find = [&](int32_t a) {
+    while (dsu[(size_t)a] != a) {
+      dsu[(size_t)a] = dsu[(size_t)dsu[(size_t)a]];
+      a = dsu[(size_t)a];
+    }
+    return a;
+  };
+  std::vector<std::vector<std::pair<int32_t, int32_t>>> adj(n);  // (neighbour, w)
+  for (auto& e : ind) {
+    const int32_t a = find(e.second.first), b = find(e.second.second);
+    if (a == b) continue;
+    dsu[(size_t)a] = b;
+    adj[(size_t)e.second.first].push_back({e.second.second, e.first});
+    adj[(size_t)e.second.second].push_back({e.second.first, e.first});
+  }
+  if (n == 0) return out;
+  int64_t ri = idx(root);
+  if (ri < 0) ri = 0;  // the root was pruned by an earlier repair: any vertex's component
+  const int32_t rc = find((int32_t)ri);
+  std::vector<char> alive(n, 0);
+  std::vector<uint32_t> bits(n, 0u);
+  std::vector<int32_t> cover((size_t)k, 0), deg(n, 0);
+  size_t left = 0;
+  for (size_t i = 0; i < n; ++i) {
+    if (find((int32_t)i) != rc) continue;
+    alive[i] = 1;
+    ++left;
+    auto it = gbits.find(set[i]);
+    bits[i] = it == gbits.end() ? 0u : it->second;
+    for (int32_t gi = 0; gi < k; ++gi) cover[(size_t)gi] += (bits[i] >> gi) & 1u;
+    deg[i] = (int32_t)adj[i].size();
+  }
+  for (int32_t gi = 0; gi < k; ++gi)
+    if (cover[(size_t)gi] == 0) return out;  // the component misses a group
+  std::vector<size_t> stack;
+  for (size_t i = 0; i < n; ++i)
+    if (alive[i] && deg[i] <= 1) stack.push_back(i);
+  while (!stack.empty() && left > 1) {
+    const size_t i = stack.back();
+    stack.pop_back();
+    if (!alive[i] || deg[i] > 1) continue;
+    bool needed = false;
+    for (int32_t gi = 0; gi < k; ++gi)
+      if (((bits[i] >> gi) & 1u) && cover[(size_t)gi] <= 1) needed = true;
+    if (needed) continue;
+    alive[i] = 0;
+    --left;
+    for (int32_t gi = 0; gi < k; ++gi) cover[(size_t)gi] -= (bits[i] >> gi) & 1u;
+    for (auto& nb : adj[i])
+      if (alive[(size_t)nb.first] && --deg[(size_t)nb.first] <= 1) stack.push_back((size_t)nb.first);
+  }
+  for (size_t i = 0; i < n; ++i) {
+    if (!alive[i]) continue;
+    out.vertices.push_back(set[i]);
+    for (auto& nb : adj[i])
+      if ((size_t)nb.first > i && alive[(size_t)nb.first]) {
+        out.cost += nb.second;
+        out.edges.push_back({set[i], set[(size_t)nb.first], nb.second});
+      }
+  }
+  out.ok = true;
+  return out;
+}
+
 gst_status ensure_learn_infer(gst_graph* g) {
   LearnWs& lw = g->lw;
   if (lw.x) return GST_OK;
@@ -787,6 +910,9 @@ gst_status ensure_learn_infer(gst_graph* g) {
   GST_CUDA(cudaMalloc(&lw.hub_sum, std::max<size_t>(1, (size_t)g->nbig) * kHid * sizeof(float)));
   GST_CUDA(cudaMalloc(&lw.scores, V * sizeof(float)));
   GST_CUDA(cudaMalloc(&lw.best, sizeof(unsigned long long)));
+  GST_CUDA(cudaMalloc(&lw.hist, kScoreBins * sizeof(uint32_t)));
+  lw.top_cap = 1 << 16;
+  GST_CUDA(cudaMalloc(&lw.top, (size_t)lw.top_cap * sizeof(uint2)));
   lw.pe_cap = (int32_t)std::min<int64_t>((int64_t)GST_MAX_K * (g->V + 1), 1 << 22);
   GST_CUDA(cudaMalloc(&lw.pe, (size_t)lw.pe_cap * sizeof(int3)));
   GST_CUDA(cudaMalloc(&lw.pn, 4 * sizeof(int32_t)));
@@ -839,9 +965,9 @@ gst_status compute_features(gst_graph* g, int32_t k) {
   LearnWs& lw = g->lw;
   const GraphDev gd = graph_dev(g);
   cudaStream_t s = g->stream;
-  GST_CUDA(launch_reach(gd, g->ws.gmask, lw.r1, lw.mnb, s));
-  GST_CUDA(launch_reach(gd, lw.r1, lw.r2, nullptr, s));
-  GST_CUDA(launch_reach(gd, lw.r2, lw.r3, nullptr, s));
+  GST_CUDA(launch_reach(gd, g->d_hub_of, g->ws.gmask, lw.r1, lw.mnb, s));
+  GST_CUDA(launch_reach(gd, g->d_hub_of, lw.r1, lw.r2, nullptr, s));
+  GST_CUDA(launch_reach(gd, g->d_hub_of, lw.r2, lw.r3, nullptr, s));
   GST_CUDA(launch_features(gd, g->ws.gmask, lw.r1, lw.r2, lw.r3, lw.mnb, k, lw.x, s));
   return GST_OK;
 }
@@ -914,36 +1040,82 @@ gst_status propose_tree(gst_graph* g, const gst_scorer* sc, const int32_t* group
   LearnWs& lw = g->lw;
   Workspace& ws = g->ws;
   cudaStream_t s = g->stream;
+  // GST_TRACE=1: report the proposal's phases (host wall clock, synchronising)
+  static const bool trace = std::getenv("GST_TRACE") != nullptr;
+  auto tp = std::chrono::steady_clock::now();
+  auto phase = [&](const char* name) {
+    if (!trace) return;
+    cudaStreamSynchronize(s);
+    const auto now = std::chrono::steady_clock::now();
+    std::fprintf(stderr, "gst-trace proposal %s %.3f ms\n", name,
+                 std::chrono::duration<double, std::milli>(now - tp).count());
+    tp = now;
+  };
   gst_status st = ensure_learn_infer(g);
   if (st != GST_OK) return st;
   st = upload_groups(g, group_ptr, members, k);
   if (st != GST_OK) return st;
   st = compute_features(g, k);
   if (st != GST_OK) return st;
+  phase("features");
   if (sc) {
     st = infer_scores(g, sc);
     if (st != GST_OK) return st;
   } else {
     GST_CUDA(launch_feature_score(g->V, lw.x, lw.scores, s));
   }
+  phase("scores");
   GST_CUDA(cudaMemsetAsync(lw.best, 0, sizeof(unsigned long long), s));
   GST_CUDA(launch_argmax(g->V, lw.scores, lw.best, s));
+  GST_CUDA(cudaMemsetAsync(lw.hist, 0, kScoreBins * sizeof(uint32_t), s));
+  GST_CUDA(launch_score_hist(g->V, lw.scores, lw.hist, s));
   unsigned long long best = 0;
+  std::vector<uint32_t> hist(kScoreBins);
   GST_CUDA(cudaMemcpyAsync(&best, lw.best, sizeof(best), cudaMemcpyDeviceToHost, s));
+  GST_CUDA(cudaMemcpyAsync(hist.data(), lw.hist, kScoreBins * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
   GST_CUDA(cudaStreamSynchronize(s));
   if (best == 0) return fail(GST_INTERNAL, "no vertex scored");
   const int32_t root = (int32_t)(0xffffffffull - (best & 0xffffffffull));
+  // the kProposeTop top-scored vertices: the lowest histogram bin that
+  // holds them, then the vertices of that bin and above, sorted on the host
+  uint32_t bin_lo = kScoreBins - 1;
+  for (uint32_t acc = 0;; --bin_lo) {
+    acc += hist[bin_lo];
+    if (acc >= (uint32_t)kProposeTop || bin_lo == 0) break;
+  }
+  GST_CUDA(cudaMemsetAsync(lw.pn + 3, 0, sizeof(int32_t), s));
+  GST_CUDA(launch_score_select(g->V, lw.scores, bin_lo, lw.top, lw.pn + 3, lw.top_cap, s));
+  int32_t ntop = 0;
+  GST_CUDA(cudaMemcpyAsync(&ntop, lw.pn + 3, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  GST_CUDA(cudaStreamSynchronize(s));
+  ntop = std::min(ntop, lw.top_cap);
+  std::vector<uint2> cand((size_t)ntop);
+  if (ntop) GST_CUDA(cudaMemcpy(cand.data(), lw.top, cand.size() * sizeof(uint2), cudaMemcpyDeviceToHost));
+  std::sort(cand.begin(), cand.end(), [](const uint2& a, const uint2& b) { return a.x != b.x ? a.x > b.x : a.y < b.y; });
+  std::vector<int32_t> top;
+  for (size_t i = 0; i < cand.size() && (int)i < kProposeTop; ++i) top.push_back((int32_t)cand[i].y);
+  phase("top");
   // distances to the root: a two-group solve whose groups are both {root}
   // grows wave 1 to the full shortest-path fixpoint from the root (a
   // one-group solve would stop after its only, last, wave's merge); the
   // row of wave 1 has stride 4 either way
   const int32_t gp1[3] = {0, 1, 2};
   const int32_t mem1[2] = {g->inv[(size_t)root], g->inv[(size_t)root]};
+  // The growth is capped at kProposeRounds rounds: every finite distance
+  // is the length of an actual path even before the fixpoint, so the tree
+  // stays feasible; a group still out of reach drops the proposal.
   gst_opts o1 = o;
   o1.upper_bound = 0;
+  o1.refine_bound = 0;
+  o1.max_rounds = kProposeRounds;
   gst_result tmp;
   st = solve_one(g, gp1, mem1, 2, o1, &tmp);
+  if (st == GST_TIMEOUT) {
+    st = GST_OK;
+    g_last_error.clear();
+  }
   if (st != GST_OK) return st;
+  phase("root distances");
   // nearest member of every group and its path to the root
   const int64_t nmembers = group_ptr[k];
   GST_CUDA(cudaMemcpyAsync(ws.d_group_ptr, group_ptr, (size_t)(k + 1) * 4, cudaMemcpyHostToDevice, s));
@@ -959,116 +1131,59 @@ gst_status propose_tree(gst_graph* g, const gst_scorer* sc, const int32_t* group
   if (pn[1] || pn[0] > lw.pe_cap) return fail(GST_INTERNAL, "proposal path walk failed");
   std::vector<int3> pe((size_t)pn[0]);
   if (pn[0]) GST_CUDA(cudaMemcpy(pe.data(), lw.pe, pe.size() * sizeof(int3), cudaMemcpyDeviceToHost));
+  phase("paths");
 
   // union of the paths (a subtree of the shortest-path tree)
   std::vector<int32_t> tv{root};
-  std::vector<std::pair<std::pair<int32_t, int32_t>, int32_t>> te;
+  std::vector<TreeEdge> te;
   for (const int3& e : pe) {
     tv.push_back(e.x);
     tv.push_back(e.y);
-    te.push_back({{std::min(e.x, e.y), std::max(e.x, e.y)}, e.z});
+    te.push_back({std::min(e.x, e.y), std::max(e.x, e.y), e.z});
   }
   std::sort(tv.begin(), tv.end());
   tv.erase(std::unique(tv.begin(), tv.end()), tv.end());
   std::sort(te.begin(), te.end());
-  te.erase(std::unique(te.begin(), te.end(), [](auto& a, auto& b) { return a.first == b.first; }), te.end());
-  int64_t cost1 = 0;
-  for (auto& e : te) cost1 += e.second;
+  te.erase(std::unique(te.begin(), te.end(), [](const TreeEdge& a, const TreeEdge& b) { return a.u == b.u && a.v == b.v; }),
+           te.end());
+  HostTree pick;
+  pick.vertices = tv;
+  pick.edges = te;
+  pick.cost = 0;
+  for (auto& e : te) pick.cost += e.w;
 
-  // MST repair: a minimum spanning tree of the subgraph induced by the
-  // tree's vertices, then leaves whose groups other vertices still cover
-  // are removed while any remain
-  const size_t nv = tv.size();
-  auto idx = [&](int32_t v) -> int64_t {
-    auto it = std::lower_bound(tv.begin(), tv.end(), v);
-    return (it != tv.end() && *it == v) ? it - tv.begin() : -1;
-  };
-  std::vector<std::pair<int32_t, std::pair<int32_t, int32_t>>> ind;  // (w, (i, j))
-  for (size_t i = 0; i < nv; ++i) {
-    const int32_t v = tv[i];
-    for (int32_t e = g->h_row[(size_t)v]; e < g->h_row[(size_t)v + 1]; ++e) {
-      const int2 x = g->h_adj[(size_t)e];
-      if (x.x <= v) continue;
-      const int64_t j = idx(x.x);
-      if (j >= 0) ind.push_back({x.y, {(int32_t)i, (int32_t)j}});
-    }
-  }
-  std::sort(ind.begin(), ind.end());
-  std::vector<int32_t> dsu(nv);
-  for (size_t i = 0; i < nv; ++i) dsu[i] = (int32_t)i;
-  std::function<int32_t(int32_t)> find = [&](int32_t a) { return dsu[(size_t)a] == a ? a : dsu[(size_t)a] = find(dsu[(size_t)a]); };
-  std::vector<std::vector<std::pair<int32_t, int32_t>>> adj(nv);  // (neighbour, w)
-  for (auto& e : ind) {
-    const int32_t a = find(e.second.first), b = find(e.second.second);
-    if (a == b) continue;
-    dsu[(size_t)a] = b;
-    adj[(size_t)e.second.first].push_back({e.second.second, e.first});
-    adj[(size_t)e.second.second].push_back({e.second.first, e.first});
-  }
-  std::vector<uint32_t> bits(nv, 0u);
+  // repairs: an MST of the subgraph induced by a vertex set, restricted to
+  // the root's component, with non-essential leaves removed; tried on the
+  // path union, on the path union plus the top-scored vertices, and again
+  // on each result's own vertices
+  std::unordered_map<int32_t, uint32_t> gbits;
   for (int32_t gi = 0; gi < k; ++gi)
-    for (int32_t i = group_ptr[gi]; i < group_ptr[gi + 1]; ++i) {
-      const int64_t j = idx(g->perm[(size_t)members[i]]);
-      if (j >= 0) bits[(size_t)j] |= 1u << gi;
+    for (int32_t i = group_ptr[gi]; i < group_ptr[gi + 1]; ++i) gbits[g->perm[(size_t)members[i]]] |= 1u << gi;
+  std::vector<int32_t> with_top = tv;
+  with_top.insert(with_top.end(), top.begin(), top.end());
+  for (const std::vector<int32_t>* set : {&tv, &with_top}) {
+    HostTree t = mst_repair(g, *set, root, gbits, k);
+    for (int pass = 0; pass < 2 && t.ok; ++pass) {
+      if (t.cost < pick.cost) pick = t;
+      HostTree t2 = mst_repair(g, t.vertices, root, gbits, k);
+      if (!t2.ok || t2.cost >= t.cost) break;
+      t = std::move(t2);
     }
-  std::vector<int32_t> cover((size_t)k, 0);
-  for (size_t i = 0; i < nv; ++i)
-    for (int32_t gi = 0; gi < k; ++gi) cover[(size_t)gi] += (bits[i] >> gi) & 1u;
-  std::vector<char> alive(nv, 1);
-  std::vector<int32_t> deg(nv);
-  for (size_t i = 0; i < nv; ++i) deg[i] = (int32_t)adj[i].size();
-  size_t left = nv;
-  for (bool again = true; again && left > 1;) {
-    again = false;
-    for (size_t i = 0; i < nv && left > 1; ++i) {
-      if (!alive[i] || deg[i] > 1) continue;
-      bool needed = false;
-      for (int32_t gi = 0; gi < k; ++gi)
-        if (((bits[i] >> gi) & 1u) && cover[(size_t)gi] <= 1) needed = true;
-      if (needed) continue;
-      alive[i] = 0;
-      --left;
-      again = true;
-      for (int32_t gi = 0; gi < k; ++gi) cover[(size_t)gi] -= (bits[i] >> gi) & 1u;
-      for (auto& nb : adj[i])
-        if (alive[(size_t)nb.first]) --deg[(size_t)nb.first];
-    }
+    if (t.ok && t.cost < pick.cost) pick = t;
   }
-  int64_t cost2 = 0;
-  std::vector<std::pair<std::pair<int32_t, int32_t>, int32_t>> te2;
-  for (size_t i = 0; i < nv; ++i) {
-    if (!alive[i]) continue;
-    for (auto& nb : adj[i])
-      if ((size_t)nb.first > i && alive[(size_t)nb.first]) {
-        cost2 += nb.second;
-        te2.push_back({{tv[i], tv[(size_t)nb.first]}, nb.second});
-      }
-  }
-  bool connected = true;  // the MST spans the path union, which is connected
-  {
-    int32_t c = -1;
-    for (size_t i = 0; i < nv; ++i)
-      if (alive[i]) {
-        const int32_t ri = find((int32_t)i);
-        if (c < 0) c = ri;
-        connected &= ri == c;
-      }
-  }
-  const bool use2 = connected && cost2 < cost1;
+  phase("repair");
   r->vertices.clear();
   r->edges.clear();
-  for (size_t i = 0; i < nv; ++i)
-    if (!use2 || alive[i]) r->vertices.push_back(g->inv[(size_t)tv[i]]);
+  for (int32_t v : pick.vertices) r->vertices.push_back(g->inv[(size_t)v]);
   std::sort(r->vertices.begin(), r->vertices.end());
-  for (auto& e : use2 ? te2 : te) {
-    const int32_t a = g->inv[(size_t)e.first.first], b = g->inv[(size_t)e.first.second];
+  for (auto& e : pick.edges) {
+    const int32_t a = g->inv[(size_t)e.u], b = g->inv[(size_t)e.v];
     r->edges.push_back(std::min(a, b));
     r->edges.push_back(std::max(a, b));
-    r->edges.push_back(e.second);
+    r->edges.push_back(e.w);
   }
-  const int64_t c = use2 ? cost2 : cost1;
-  if (c >= GST_COST_LIMIT) return fail(GST_OVERFLOW, "proposal cost reached GST_COST_LIMIT");
-  r->cost = (int32_t)c;
+  if (pick.cost >= GST_COST_LIMIT) return fail(GST_OVERFLOW, "proposal cost reached GST_COST_LIMIT");
+  r->cost = (int32_t)pick.cost;
   r->root = g->inv[(size_t)root];
   r->status = GST_OK;
   return GST_OK;
@@ -1500,12 +1615,13 @@ gst_status gst_solve_learned(gst_graph* g, gst_scorer* sc, const int32_t* group_
   gst_result prop;
   const gst_status pst = propose_tree(g, sc, group_ptr, members, k, o, &prop);
   const double pms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  o.refine_bound = 1;
   if (pst == GST_OK && prop.cost > 0) {
     o.upper_bound = prop.cost;
     st = solve_one(g, group_ptr, members, k, o, r);
     if (st == GST_OK) {
       r->status = GST_OK;
-      r->ub = prop.cost;
+      r->proposal_cost = prop.cost;
       r->propose_ms = pms;
       return GST_OK;
     }
@@ -1525,6 +1641,7 @@ gst_status gst_solve_learned(gst_graph* g, gst_scorer* sc, const int32_t* group_
 }
 
 int32_t gst_result_upper_bound(const gst_result* r) { return r ? r->ub : 0; }
+int32_t gst_result_proposal_cost(const gst_result* r) { return r ? r->proposal_cost : 0; }
 double gst_result_proposal_ms(const gst_result* r) { return r ? r->propose_ms : 0.0; }
 
 const char* gst_last_error(void) { return g_last_error.c_str(); }

@@ -38,8 +38,8 @@ __host__ __device__ constexpr int64_t layer_off(int l) { return kOffL1 + (int64_
 // out[v] = in[v] | OR of in[u] over neighbours u (groups within one more
 // hop). With member_nbrs non-null, also counts neighbours that belong to
 // some group.
-cudaError_t launch_reach(const GraphDev& g, const uint32_t* in, uint32_t* out, int32_t* member_nbrs,
-                         cudaStream_t s);
+cudaError_t launch_reach(const GraphDev& g, const int32_t* hub_of, const uint32_t* in, uint32_t* out,
+                         int32_t* member_nbrs, cudaStream_t s);
 // x[v][0..15] from the group masks (see learn_kernels.cu for the list).
 cudaError_t launch_features(const GraphDev& g, const uint32_t* m0, const uint32_t* r1, const uint32_t* r2,
                             const uint32_t* r3, const int32_t* member_nbrs, int32_t k, float* x, cudaStream_t s);
@@ -61,6 +61,14 @@ cudaError_t launch_infer_layer(const GraphDev& g, const int32_t* hub_of, const f
 // The proposal's root without a network: most groups within 1 hop, then 2,
 // then 3, then degree (s = 1000 x3 + 100 x4 + 10 x5 + x1).
 cudaError_t launch_feature_score(int32_t V, const float* x, float* s, cudaStream_t st);
+// Top-scored vertices, in two passes: a histogram of the top 12 bits of
+// the order-preserving score keys (hist[4096], zeroed by the caller), then
+// the vertices whose key bin is >= bin_lo appended as (key, v) to out
+// (*count counts them, at most cap are written).
+constexpr int kScoreBins = 4096;
+cudaError_t launch_score_hist(int32_t V, const float* scores, uint32_t* hist, cudaStream_t s);
+cudaError_t launch_score_select(int32_t V, const float* scores, uint32_t bin_lo, uint2* out, int32_t* count,
+                                int32_t cap, cudaStream_t s);
 // argmax of scores (ties to the smaller ID) packed as an order-preserving
 // key: *best = (key(score) << 32) | (0xffffffff - v).
 cudaError_t launch_argmax(int32_t V, const float* scores, unsigned long long* best, cudaStream_t s);

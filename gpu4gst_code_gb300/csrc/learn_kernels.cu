@@ -28,24 +28,36 @@ int grid_for(int64_t items, int per_block, int cap = 152 * 16) {
 }
 
 // -------------------------------------------------------------- features --
-__global__ void k_reach(GraphDev g, const uint32_t* __restrict__ in, uint32_t* __restrict__ out,
-                        int32_t* __restrict__ member_nbrs) {
+// out (zeroed by the caller) = in | OR over neighbours. Hub rows go one
+// 32-entry chunk per warp (atomicOr); the other vertices a thread each.
+__global__ void k_reach(GraphDev g, const int32_t* __restrict__ hub_of, const uint32_t* __restrict__ in,
+                        uint32_t* __restrict__ out, int32_t* __restrict__ member_nbrs) {
   const int lane = threadIdx.x & 31;
-  for (int64_t v = gwarp(); v < g.V; v += nwarps()) {
+  for (int64_t c = gwarp(); c < g.nchunks; c += nwarps()) {
+    const int2 hc = g.hub_chunk[c];
+    const int32_t u = g.big[hc.x];
+    const int32_t e = hc.y + lane;
+    uint32_t m = 0;
+    if (e < g.row_ptr[u + 1]) m = in[g.adj[e].x];
+    const uint32_t acc = __reduce_or_sync(0xffffffffu, m);
+    const uint32_t cnt = __reduce_add_sync(0xffffffffu, m != 0u ? 1u : 0u);
+    if (lane == 0) {
+      atomicOr(out + u, acc | in[u]);
+      if (member_nbrs && cnt) atomicAdd(member_nbrs + u, (int32_t)cnt);
+    }
+  }
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < g.V; v += (int64_t)gridDim.x * blockDim.x) {
+    if (hub_of[v] >= 0) continue;
     const int32_t beg = g.row_ptr[v], end = g.row_ptr[v + 1];
-    uint32_t acc = 0;
+    uint32_t acc = in[v];
     int32_t cnt = 0;
-    for (int32_t e = beg + lane; e < end; e += 32) {
+    for (int32_t e = beg; e < end; ++e) {
       const uint32_t m = in[g.adj[e].x];
       acc |= m;
       cnt += m != 0u;
     }
-    acc = __reduce_or_sync(0xffffffffu, acc);
-    cnt = (int32_t)__reduce_add_sync(0xffffffffu, (uint32_t)cnt);
-    if (lane == 0) {
-      out[v] = acc | in[v];
-      if (member_nbrs) member_nbrs[v] = cnt;
-    }
+    out[v] = acc;
+    if (member_nbrs) member_nbrs[v] = cnt;
   }
 }
 
@@ -130,6 +142,16 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
   return *reinterpret_cast<const uint32_t*>(&b);
 }
 
+__device__ __forceinline__ void add_bf16x8(float (&a)[8], const uint4 x) {
+  const uint32_t w[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const float2 f = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&w[q]));
+    a[2 * q] += f.x;
+    a[2 * q + 1] += f.y;
+  }
+}
+
 // D += A * B for one m16n8k16 tile (bf16 in, fp32 accumulate)
 __device__ __forceinline__ void mma_bf16(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
                                          uint32_t b0, uint32_t b1) {
@@ -172,43 +194,40 @@ __global__ void __launch_bounds__(kInfWarps * 32) k_infer_layer(GraphDev g, cons
   const float bo = bo_ptr ? *bo_ptr : 0.0f;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int gq = lane >> 2, tq = lane & 3;
-  const __nv_bfloat162* h2 = reinterpret_cast<const __nv_bfloat162*>(hin);
   const int64_t ntiles = ((int64_t)g.V + 15) / 16;
   for (int64_t tile = (int64_t)blockIdx.x * kInfWarps + w; tile < ntiles; tile += (int64_t)gridDim.x * kInfWarps) {
-    for (int i = 0; i < 16; ++i) {
+    // stage A: a quarter warp per vertex, 8 channels (16 bytes) per lane
+    const int sub = lane >> 3, sl = lane & 7;
+    for (int i0 = 0; i0 < 16; i0 += 4) {
+      const int i = i0 + sub;
       const int64_t v = tile * 16 + i;
-      uint32_t hv = 0, av = 0;
+      uint4 hv = make_uint4(0, 0, 0, 0), av = make_uint4(0, 0, 0, 0);
       if (v < g.V) {
-        hv = *reinterpret_cast<const uint32_t*>(&h2[v * (kHid / 2) + lane]);
+        hv = reinterpret_cast<const uint4*>(hin + v * kHid)[sl];
         const int32_t beg = g.row_ptr[v], end = g.row_ptr[v + 1];
         const float inv = end > beg ? 1.0f / (float)(end - beg) : 0.0f;
-        float ax = 0.0f, ay = 0.0f;
+        float a[8] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
         const int32_t hb = hub_of[v];
         if (hb >= 0) {
-          ax = hub_sum[(int64_t)hb * kHid + 2 * lane];
-          ay = hub_sum[(int64_t)hb * kHid + 2 * lane + 1];
+          const float4* hs = reinterpret_cast<const float4*>(hub_sum + (int64_t)hb * kHid + 8 * sl);
+          const float4 p0 = hs[0], p1 = hs[1];
+          a[0] = p0.x; a[1] = p0.y; a[2] = p0.z; a[3] = p0.w;
+          a[4] = p1.x; a[5] = p1.y; a[6] = p1.z; a[7] = p1.w;
         } else {
           int32_t e = beg;
-          for (; e + 4 <= end; e += 4) {
-            float2 f[4];
-#pragma unroll
-            for (int j = 0; j < 4; ++j) f[j] = __bfloat1622float2(h2[(int64_t)g.adj[e + j].x * (kHid / 2) + lane]);
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-              ax += f[j].x;
-              ay += f[j].y;
-            }
+          for (; e + 2 <= end; e += 2) {
+            const uint4 x0 = reinterpret_cast<const uint4*>(hin + (int64_t)g.adj[e].x * kHid)[sl];
+            const uint4 x1 = reinterpret_cast<const uint4*>(hin + (int64_t)g.adj[e + 1].x * kHid)[sl];
+            add_bf16x8(a, x0);
+            add_bf16x8(a, x1);
           }
-          for (; e < end; ++e) {
-            const float2 f = __bfloat1622float2(h2[(int64_t)g.adj[e].x * (kHid / 2) + lane]);
-            ax += f.x;
-            ay += f.y;
-          }
+          if (e < end) add_bf16x8(a, reinterpret_cast<const uint4*>(hin + (int64_t)g.adj[e].x * kHid)[sl]);
         }
-        av = pack_bf16x2(ax * inv, ay * inv);
+        av = make_uint4(pack_bf16x2(a[0] * inv, a[1] * inv), pack_bf16x2(a[2] * inv, a[3] * inv),
+                        pack_bf16x2(a[4] * inv, a[5] * inv), pack_bf16x2(a[6] * inv, a[7] * inv));
       }
-      reinterpret_cast<uint32_t*>(&sA[w][i][0])[lane] = hv;
-      reinterpret_cast<uint32_t*>(&sA[w][i][kHid])[lane] = av;
+      reinterpret_cast<uint4*>(&sA[w][i][0])[sl] = hv;
+      reinterpret_cast<uint4*>(&sA[w][i][kHid])[sl] = av;
     }
     __syncwarp();
     float acc[kHid / 8][4];
@@ -272,6 +291,31 @@ __global__ void k_feature_score(int32_t V, const float* __restrict__ x, float* _
 __device__ __forceinline__ uint32_t order_key(float f) {
   const uint32_t u = __float_as_uint(f);
   return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+__global__ void k_score_hist(int32_t V, const float* __restrict__ s, uint32_t* __restrict__ hist) {
+  __shared__ uint32_t h[kScoreBins];
+  for (int i = threadIdx.x; i < kScoreBins; i += blockDim.x) h[i] = 0u;
+  __syncthreads();
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < V; v += (int64_t)gridDim.x * blockDim.x) {
+    const float f = s[v];
+    if (f == f) atomicAdd(&h[order_key(f) >> 20], 1u);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < kScoreBins; i += blockDim.x)
+    if (h[i]) atomicAdd(hist + i, h[i]);
+}
+
+__global__ void k_score_select(int32_t V, const float* __restrict__ s, uint32_t bin_lo, uint2* __restrict__ out,
+                               int32_t* count, int32_t cap) {
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < V; v += (int64_t)gridDim.x * blockDim.x) {
+    const float f = s[v];
+    if (f != f) continue;
+    const uint32_t key = order_key(f);
+    if ((key >> 20) < bin_lo) continue;
+    const int32_t i = atomicAdd(count, 1);
+    if (i < cap) out[i] = make_uint2(key, (uint32_t)v);
+  }
 }
 
 __global__ void k_argmax(int32_t V, const float* __restrict__ s, unsigned long long* best) {
@@ -554,9 +598,12 @@ __global__ void __launch_bounds__(256) k_ub_paths(GraphDev g, const int32_t* __r
 }  // namespace
 
 // -------------------------------------------------------------- launchers --
-cudaError_t launch_reach(const GraphDev& g, const uint32_t* in, uint32_t* out, int32_t* member_nbrs,
-                         cudaStream_t s) {
-  k_reach<<<grid_for((int64_t)g.V * 32, 256), 256, 0, s>>>(g, in, out, member_nbrs);
+cudaError_t launch_reach(const GraphDev& g, const int32_t* hub_of, const uint32_t* in, uint32_t* out,
+                         int32_t* member_nbrs, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(out, 0, (size_t)g.V * sizeof(uint32_t), s);
+  if (e == cudaSuccess && member_nbrs) e = cudaMemsetAsync(member_nbrs, 0, (size_t)g.V * sizeof(int32_t), s);
+  if (e != cudaSuccess) return e;
+  k_reach<<<grid_for(g.V, 256), 256, 0, s>>>(g, hub_of, in, out, member_nbrs);
   return cudaGetLastError();
 }
 
@@ -596,6 +643,17 @@ cudaError_t launch_infer_layer(const GraphDev& g, const int32_t* hub_of, const f
 
 cudaError_t launch_feature_score(int32_t V, const float* x, float* s, cudaStream_t st) {
   k_feature_score<<<grid_for(V, 256), 256, 0, st>>>(V, x, s);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_score_hist(int32_t V, const float* scores, uint32_t* hist, cudaStream_t s) {
+  k_score_hist<<<grid_for(V, 256, 152 * 2), 256, 0, s>>>(V, scores, hist);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_score_select(int32_t V, const float* scores, uint32_t bin_lo, uint2* out, int32_t* count,
+                                int32_t cap, cudaStream_t s) {
+  k_score_select<<<grid_for(V, 256, 152 * 4), 256, 0, s>>>(V, scores, bin_lo, out, count, cap);
   return cudaGetLastError();
 }
 

@@ -54,7 +54,8 @@ class Opts(C.Structure):
         ("use_graph", C.c_int32),
         ("collect_stats", C.c_int32),
         ("dense_shift", C.c_int32),
-        ("reserved", C.c_int32 * 10),
+        ("refine_bound", C.c_int32),
+        ("reserved", C.c_int32 * 9),
     ]
 
 
@@ -103,6 +104,7 @@ SIGNATURES = {
         [C.c_void_p, C.c_void_p, I32P, I32P, C.c_int32, C.POINTER(Opts), C.POINTER(C.c_void_p)],
     ),
     "gst_result_upper_bound": (C.c_int32, [C.c_void_p]),
+    "gst_result_proposal_cost": (C.c_int32, [C.c_void_p]),
     "gst_result_proposal_ms": (C.c_double, [C.c_void_p]),
     "gst_last_error": (C.c_char_p, []),
     "gst_version": (C.c_char_p, []),
@@ -176,7 +178,8 @@ class Result:
     launches: int = 0
     times_ms: tuple = (0.0, 0.0, 0.0, 0.0)
     stats: dict = field(default_factory=dict)
-    upper_bound: int = 0  # bound that pruned a learned solve (0: none)
+    upper_bound: int = 0  # pruning bound at the last wave (0: unpruned)
+    proposal_cost: int = 0  # learned path: cost of the proposed tree (0: none)
     proposal_ms: float = 0.0
 
     @property
@@ -213,12 +216,13 @@ def _read_result(r) -> Result:
         times_ms=tuple(t),
         stats=dict(zip(STAT_NAMES, list(s))),
         upper_bound=int(L.gst_result_upper_bound(r)),
+        proposal_cost=int(L.gst_result_proposal_cost(r)),
         proposal_ms=float(L.gst_result_proposal_ms(r)),
     )
 
 
 def make_opts(upper_bound: int = 0, max_rounds: int = 0, use_graph: bool = False, collect_stats: bool = False,
-              dense_shift: int = 0) -> Opts:
+              dense_shift: int = 0, refine_bound: bool = False) -> Opts:
     o = Opts()
     o.struct_size = C.sizeof(Opts)
     o.upper_bound = int(upper_bound)
@@ -226,6 +230,7 @@ def make_opts(upper_bound: int = 0, max_rounds: int = 0, use_graph: bool = False
     o.use_graph = int(bool(use_graph))
     o.collect_stats = int(bool(collect_stats))
     o.dense_shift = int(dense_shift)
+    o.refine_bound = int(bool(refine_bound))
     return o
 
 
@@ -274,13 +279,13 @@ class Graph:
         self.close()
 
     def solve(self, group_ptr, members=None, *, upper_bound=0, max_rounds=0, use_graph=False,
-              collect_stats=False, dense_shift=0, raise_on_error=True) -> Result:
+              collect_stats=False, dense_shift=0, refine_bound=False, raise_on_error=True) -> Result:
         """Solves one query. `group_ptr` may be a list of member lists."""
         if members is None:
             group_ptr, members = groups_to_csr(group_ptr)
         gp, mem = _i32(group_ptr), _i32(members)
         k = len(gp) - 1
-        o = make_opts(upper_bound, max_rounds, use_graph, collect_stats, dense_shift)
+        o = make_opts(upper_bound, max_rounds, use_graph, collect_stats, dense_shift, refine_bound)
         r = C.c_void_p()
         st = lib().gst_solve(self._h, _ptr(gp), _ptr(mem), k, C.byref(o), C.byref(r))
         msg = last_error()

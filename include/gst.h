@@ -73,7 +73,13 @@ typedef struct gst_opts {
    * V >> dense_shift vertices; 0 = the default (1). A tuning knob only:
    * results do not depend on it. */
   int32_t dense_shift;
-  int32_t reserved[10];
+  /* 1 = after every DP wave, lower the pruning bound to the cheapest
+   * feasible subgraph seen so far: a state T(v,S) plus v's shortest paths
+   * (wave-1 states) to the groups outside S, as PrunedDP++ updates its
+   * best solution (graph_v_of_v_idealID_PrunedDPPlusPlus.h:668-711). Turns
+   * pruning on from wave 2 even without an upper_bound. Exact either way. */
+  int32_t refine_bound;
+  int32_t reserved[9];
 } gst_opts;
 
 /* ---------------------------------------------------------------- graph -- */

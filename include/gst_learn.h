@@ -72,9 +72,12 @@ gst_status gst_propose(gst_graph* g, gst_scorer* s, const int32_t* group_ptr, co
 gst_status gst_solve_learned(gst_graph* g, gst_scorer* s, const int32_t* group_ptr, const int32_t* members, int32_t k,
                              const gst_opts* opts, gst_result** out);
 
-/* Bound that pruned the solve (0 = none, the fallback ran) and the host
- * wall time of the proposal in ms. */
+/* Pruning bound as the last DP wave saw it (after the refinements of
+ * gst_opts.refine_bound; 0 = the solve ran unpruned), the cost of the
+ * learned path's proposed tree (0 = no proposal, the fallback ran) and the
+ * host wall time of the proposal in ms. gst_solve_learned always refines. */
 int32_t gst_result_upper_bound(const gst_result* r);
+int32_t gst_result_proposal_cost(const gst_result* r);
 double gst_result_proposal_ms(const gst_result* r);
 
 #ifdef __cplusplus

@@ -106,6 +106,23 @@ def test_upper_bound_pruning_is_exact(golden, use_graph):
                 assert res.status == Status.INFEASIBLE
 
 
+@pytest.mark.parametrize("use_graph", MODES)
+def test_refined_bound_is_exact(golden, use_graph):
+    """refine_bound lowers the bound between waves from partial trees; the
+    cost stays exact with and without a starting bound, and the final bound
+    is a feasible cost (>= the optimum)."""
+    for case in golden["cases"][::7] + golden["cases"][200:]:
+        g, gp, mem = make_instance(case)
+        opt = case["dpbf"]
+        with native.Graph(g.row_ptr, g.col, g.w) as dg:
+            for ub in (0, opt, 2 * opt + 1):
+                res = dg.solve(gp, mem, upper_bound=ub, refine_bound=True, use_graph=use_graph)
+                _check(g.row_ptr, g.col, g.w, gp, mem, res, opt)
+                assert res.upper_bound == 0 or res.upper_bound >= opt
+                if ub:
+                    assert res.upper_bound <= ub
+
+
 def test_hub_rows_use_block_path():
     # star: hub 0 joined to 600 leaves (degree > 64 -> one CTA per row)
     V = 601

@@ -107,6 +107,33 @@ def test_proposal_is_feasible_and_learned_solve_exact(use_scorer):
             res = dg.solve_learned(s, gp, mem)
             assert res.status == N.Status.OK
             assert res.cost == plain.cost
-            assert res.upper_bound == prop.cost
+            assert res.proposal_cost == prop.cost
+            # the refined bound: a feasible cost, or 0 (= no bound) once a zero-cost tree is seen
+            assert res.upper_bound <= prop.cost and (res.upper_bound >= plain.cost or plain.cost == 0)
             err = oracle.check_tree(g.row_ptr, g.col, g.w, gp, mem, res.vertices, res.edges, res.cost)
             assert err is None, err
+
+
+def test_trained_network_gains_over_the_method_without_it():
+    """The committed weights (trained on DP-solved queries, see
+    gpu4gst_code_gb300/weights/scorer_ba.json) propose tighter bounds on
+    held-out queries than the same pipeline without a network (fixed
+    feature score) and than the untrained network; every solve stays exact."""
+    from gpu4gst_code_gb300 import learn, native as N
+
+    g = N.gen_barabasi_albert(100_000, 4, 1, 100, 4242)  # a graph not trained on
+    rng = np.random.default_rng(5)
+    ratios = {"trained": [], "none": [], "untrained": []}
+    with N.Graph(g.row_ptr, g.col, g.w) as dg, N.Scorer(learn.load_params()) as tr, \
+            N.Scorer(learn.init_params(0)) as un:
+        for q in range(24):
+            k = int(rng.choice([4, 5, 6]))
+            gp, mem = N.gen_groups_zipf_degree(g, k, 1.2, 5, 500, 90_000 + q)
+            opt = dg.solve(gp, mem, use_graph=True).cost
+            for name, sc in (("trained", tr), ("none", None), ("untrained", un)):
+                res = dg.solve_learned(sc, gp, mem)
+                assert res.cost == opt
+                assert res.proposal_cost >= opt
+                ratios[name].append(res.proposal_cost / opt)
+    mean = {k: float(np.mean(v)) for k, v in ratios.items()}
+    assert mean["trained"] < mean["none"] and mean["trained"] < mean["untrained"], mean
