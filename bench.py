@@ -1,19 +1,30 @@
 """Benchmark: exact GST queries/sec on one GB300 (DPBF, k=6, |V|=1M).
 
-A step is one exact query (one solve of the DP over all 2^6 group sets) on a
-resident synthetic graph: Barabasi-Albert m=4, |V|=1,000,000 (~4M edges),
-integer weights U[1,100]; k=6 groups with Zipf(1.2) sizes clipped to
-[5,500], members drawn proportionally to degree. Every step uses a
-different query (seeded), all on the same graph.
+A step is one exact query on a resident synthetic graph: Barabasi-Albert
+m=4, |V|=1,000,000 (~4M edges), integer weights U[1,100]; k=6 groups with
+Zipf(1.2) sizes clipped to [5,500], members drawn proportionally to degree.
+Every step uses a different seeded query on the same graph. The same K
+queries run through three exact methods, each through the C ABI:
+
+  plain     gst_solve: the DPBF of the reference, unpruned;
+  bounded   gst_solve with refine_bound: the bound is lowered after every
+            wave from partial trees (PrunedDP++'s best-solution update);
+  learned   gst_solve_learned with the committed trained scorer: proposal
+            tree from the network's top vertex, then the bounded DP.
+
+`value` is the learned method's throughput (the metric's method); the
+other two and the speedups ride along in the same line.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-Ours: the state table of a query (1M x 63 int32 costs + parents, 504 MB)
-exceeds L2 (129 MB), and L2 is additionally flushed (a 256 MiB device
-write) before every step; device time comes from CUDA events recorded on
-the solver's own stream. `e2e` is wall time of the C-ABI call with host
-group arrays in and the host tree out. The CPU baseline is the oracle's C
-restatement of the reference's CPU DPBF on one host core, one full query.
+Device time comes from CUDA events recorded on the solver's own stream
+(the learned method adds the proposal's host wall time, which includes its
+device work). The state table of a query (1M x 63 int32 costs + parents,
+504 MB) exceeds L2 (129 MB), and L2 is additionally flushed (a 256 MiB
+device write) before every step. `e2e` is the wall time of the C-ABI call
+with host group arrays in and the host tree out. The CPU baseline is the
+oracle's C restatement of the reference's CPU DPBF on one host core, one
+full query.
 
 Reference arm: the reference's CPU DPBF (its C restatement: the reference's
 own build needs a Boost it does not ship) on all host cores, one query per
@@ -40,6 +51,12 @@ METRIC = "GST queries/sec, k=6, |V|=1M, exact; learned-UB pruned vs plain DPBF s
 UNIT = "queries/s"
 FALLBACK_HBM_GBS = 6800.0
 
+METHOD_DESC = {
+    "plain": "plain DPBF (gst_solve, unpruned); exact",
+    "bounded": "pruned DPBF, bound refined between waves (gst_solve, refine_bound); exact",
+    "learned": "learned-bound pruned DPBF (gst_solve_learned, trained scorer, refined bound); exact",
+}
+
 WORKLOADS = {
     # name: (graph generator args, group generator, description)
     "ba1m_k6": dict(V=1_000_000, m=4, wmin=1, wmax=100, k=6, zipf=(1.2, 5, 500), graph_seed=2,
@@ -50,6 +67,9 @@ WORKLOADS = {
                            "sizes in [5,500], degree-proportional members"),
     "ba2m_k8": dict(V=2_000_000, m=8, wmin=1, wmax=1000, k=8, uniform=50, graph_seed=3,
                     desc="plain GPU DPBF, large mask: BA m=8, |V|=2,000,000, w U[1,1000], k=8 x 50 uniform"),
+    "ba4m_k7": dict(V=4_000_000, m=8, wmin=1, wmax=100, k=7, zipf=(1.2, 5, 500), graph_seed=5,
+                    desc="learned-bound evaluation graph: BA m=8, |V|=4,000,000, w U[1,100], k=7, Zipf(1.2) "
+                         "sizes in [5,500], degree-proportional members"),
     "rc1k_k3": dict(V=1000, E=5000, wmin=1, wmax=100, k=3, uniform=20, graph_seed=0,
                     desc="plain DPBF, single query: random connected |V|=1000 |E|=5000, w U[1,100], k=3 x 20"),
 }
@@ -94,7 +114,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self._t = threading.Thread(target=self._read, daemon=True)
             self._t.start()
         except OSError:
@@ -132,6 +152,23 @@ class ClockSampler:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
                 "samples": len(sm)}
+
+
+# DRAM bytes (read + write) of all growth-kernel launches of one plain
+# query, summed from one ncu capture per workload (profiles/); None where
+# no capture exists.
+TRAFFIC_PER_STEP = {"ba1m_k6": 9.87e9}  # profiles/grow_dram_ba1m_k6.md
+
+
+def table_bytes(V, k):
+    """cost + parent tables: V x sum over waves of the padded row stride, int32 each."""
+    from math import comb
+
+    return 8 * V * sum((comb(k, l) + 3) // 4 * 4 for l in range(1, k + 1))
+
+
+def traffic_per_step(wl):
+    return TRAFFIC_PER_STEP.get(wl.get("name"))
 
 
 def measured_hbm_peak():
@@ -187,16 +224,18 @@ def run_reference(args, wl):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="ba1m_k6", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--methods", default="plain,bounded,learned",
+                    help="comma-separated subset of plain,bounded,learned (profiling runs); value = the last")
     ap.add_argument("--driver", default="graph", choices=["graph", "host"],
                     help="graph: one captured CUDA graph per query; host: host-launched growth rounds")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
-    wl = WORKLOADS[args.workload]
+    wl = dict(WORKLOADS[args.workload], name=args.workload)
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -230,60 +269,105 @@ def main():
     dg = N.Graph(g.row_ptr, g.col, g.w)
     upload_ms = 1e3 * (time.perf_counter() - t)
 
-    def step(i, stats=True):
+    from gpu4gst_code_gb300 import learn
+
+    scorer = N.Scorer(learn.load_params())
+    use_graph = args.driver == "graph"
+
+    def step(i, method):
         flush.fill_(i & 0xFF)
         torch.cuda.synchronize()
         gp, mem = queries[i]
         t0 = time.perf_counter()
-        r = dg.solve(gp, mem, collect_stats=stats, use_graph=args.driver == "graph")
+        if method == "plain":
+            r = dg.solve(gp, mem, collect_stats=True, use_graph=use_graph)
+        elif method == "bounded":
+            r = dg.solve(gp, mem, refine_bound=True, use_graph=use_graph)
+        else:
+            r = dg.solve_learned(scorer, gp, mem, use_graph=use_graph)
         wall = time.perf_counter() - t0
         assert r.status == N.Status.OK, r.status
         return r, wall
 
-    for i in range(args.warmup):
-        step(i)
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    results = []
-    with ClockSampler(local_rank) as clk:
-        for i in range(args.warmup, n_total):
-            results.append(step(i))
-    torch.cuda.synchronize()
-    dev_ms = sum(r.times_ms[0] for r, _ in results)
-    wall_s = sum(w for _, w in results)
-    if dist:
-        tt = torch.tensor([dev_ms, wall_s], dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        dev_ms, wall_s = float(tt[0]), float(tt[1])
-    value = world * args.steps / (dev_ms / 1e3)
-    e2e = world * args.steps / wall_s
-    grow_ms = sum(r.times_ms[1] for r, _ in results)
-    grow_bytes = sum(r.stats["bytes"] for r, _ in results)
-    launches = sum(r.launches for r, _ in results)
+    def dev_ms(r, method):
+        return r.times_ms[0] + (r.proposal_ms if method == "learned" else 0.0)
+
+    arms = {}
+    clocks = None
+    methods = [m for m in ("plain", "bounded", "learned") if m in args.methods.split(",")]
+    for method in methods:
+        for i in range(args.warmup):
+            step(i, method)
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        res = []
+        with ClockSampler(local_rank) as clk:
+            for i in range(args.warmup, n_total):
+                res.append(step(i, method))
+        torch.cuda.synchronize()
+        if method == methods[-1]:
+            clocks = clk.summary()
+        d_ms = sum(dev_ms(r, method) for r, _ in res)
+        w_s = sum(w for _, w in res)
+        if dist:
+            tt = torch.tensor([d_ms, w_s], dtype=torch.float64)
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            d_ms, w_s = float(tt[0]), float(tt[1])
+        arms[method] = dict(results=res, dev_ms=d_ms, wall_s=w_s, qps=world * args.steps / (d_ms / 1e3),
+                            e2e=world * args.steps / w_s)
+    # Roofline pass of the growth kernels: the same plain queries through the
+    # host-launched driver, whose per-wave CUDA events (on the solver's
+    # stream) bracket only growth launches; algorithmic bytes from the
+    # kernels' own counters. Not part of `value`.
+    roof = [dg.solve(*queries[i], collect_stats=True, use_graph=False) for i in range(args.warmup, n_total)]
+    costs = {m: [r.cost for r, _ in a["results"]] for m, a in arms.items()}
+    assert all(c == [r.cost for r in roof] for c in costs.values()), costs
+    head = arms[methods[-1]]  # the metric's method: learned unless restricted
+    value = head["qps"]
+    grow_ms = sum(r.times_ms[1] for r in roof)
+    grow_bytes = sum(r.stats["bytes"] for r in roof)
+    launches = sum(r.launches for r, _ in head["results"])
     peak, peak_kind = measured_hbm_peak()
     achieved = grow_bytes / (grow_ms / 1e3) / 1e9 if grow_ms > 0 else 0.0
     h2d = int(np.mean([(len(q[0]) + len(q[1])) * 4 for q in queries[args.warmup:]]))
-    d2h = int(np.mean([64 + 4 * len(r.vertices) + 12 * len(r.edges) for r, _ in results]))
+    d2h = int(np.mean([64 + 4 * len(r.vertices) + 12 * len(r.edges) for r, _ in head["results"]]))
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
+        "warmup": args.warmup, "ms_per_step": head["dev_ms"] / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int32",
         "data": "synthetic (seeded generators; no public dataset)",
         "config": {
             "workload": args.workload, "desc": wl["desc"], "V": g.V, "nnz": g.nnz, "k": wl["k"],
-            "method": "plain DPBF (no pruning)", "driver": args.driver, "l2": "flushed before every step (256 MiB device write); "
-            "state table 504 MB > L2", "graph_upload_ms": upload_ms,
-            "costs": [r.cost for r, _ in results],
+            "method": METHOD_DESC[methods[-1]],
+            "driver": args.driver,
+            "l2": f"flushed before every step (256 MiB device write); state table "
+                  f"{table_bytes(g.V, wl['k']) / 1e6:.0f} MB > L2 (129 MB)",
+            "graph_upload_ms": upload_ms, "costs": costs[methods[-1]],
         },
-        "roofline": {"kernel": "k_grow", "bound": "hbm", "achieved": achieved, "peak": peak,
-                     "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+        "methods": {
+            m: {"value": a["qps"], "ms_per_step": a["dev_ms"] / args.steps, "e2e": a["e2e"]}
+            for m, a in arms.items()
+        },
+        "speedup_vs_plain": {m: a["qps"] / arms["plain"]["qps"] for m, a in arms.items()
+                             if m != "plain" and "plain" in arms},
+        "roofline": {"kernel": "growth kernels (k_grow_thread<MP>, k_grow_hubs), plain method, per step",
+                     "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_kind": peak_kind, "traffic": traffic_per_step(wl),
+                     "traffic_note": "DRAM bytes of the growth kernels per query, one ncu capture (profiles/)",
                      "algorithmic_bytes_per_step": grow_bytes / args.steps,
                      "grow_ms_per_step": grow_ms / args.steps},
-        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "e2e": {"value": head["e2e"], "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
-        "clocks": clk.summary(),
+        "clocks": clocks,
     }
+    if "learned" in arms:
+        lr = arms["learned"]["results"]
+        line["learned_detail"] = {
+            "proposal_ms_mean": float(np.mean([r.proposal_ms for r, _ in lr])),
+            "proposal_over_opt_mean": float(np.mean([r.proposal_cost / r.cost for r, _ in lr if r.cost > 0])),
+            "final_bound_over_opt_mean": float(np.mean([r.upper_bound / r.cost for r, _ in lr if r.cost > 0])),
+        }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         import oracle
 
@@ -294,9 +378,10 @@ def main():
         line["cpu_baseline"] = {"value": 1.0 / cpu_s, "unit": UNIT, "cores": 1, "kind": "port",
                                 "sample": "1 full query (the first timed one), 1 thread; the oracle's C "
                                           "restatement of the reference CPU DPBF"}
-        line["parity_first_query"] = bool(ref.cost == results[0][0].cost)
+        line["parity_first_query"] = bool(ref.cost == roof[0].cost)
     if rank == 0:
         print(json.dumps(line), flush=True)
+    scorer.close()
     dg.close()
     if dist:
         dist.destroy_process_group()

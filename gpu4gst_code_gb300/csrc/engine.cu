@@ -1058,12 +1058,16 @@ gst_status propose_tree(gst_graph* g, const gst_scorer* sc, const int32_t* group
   st = compute_features(g, k);
   if (st != GST_OK) return st;
   phase("features");
+  int64_t launches = 5;  // group masks, three reach passes, features
   if (sc) {
     st = infer_scores(g, sc);
     if (st != GST_OK) return st;
+    launches += 1 + kMpLayers * (g->nbig > 0 ? 2 : 1);
   } else {
     GST_CUDA(launch_feature_score(g->V, lw.x, lw.scores, s));
+    launches += 1;
   }
+  launches += 3;  // argmax, histogram, selection
   phase("scores");
   GST_CUDA(cudaMemsetAsync(lw.best, 0, sizeof(unsigned long long), s));
   GST_CUDA(launch_argmax(g->V, lw.scores, lw.best, s));
@@ -1113,8 +1117,11 @@ gst_status propose_tree(gst_graph* g, const gst_scorer* sc, const int32_t* group
   if (st == GST_TIMEOUT) {
     st = GST_OK;
     g_last_error.clear();
+    // a capped solve stops before its epilogue: the round loop's launches
+    tmp.launches = 1 + 2 + 2 * 1 + (int64_t)kProposeRounds * (g->nchunks > 0 ? 2 : 1);
   }
   if (st != GST_OK) return st;
+  launches += tmp.launches + 1;  // + the path walk
   phase("root distances");
   // nearest member of every group and its path to the root
   const int64_t nmembers = group_ptr[k];
@@ -1185,6 +1192,7 @@ gst_status propose_tree(gst_graph* g, const gst_scorer* sc, const int32_t* group
   if (pick.cost >= GST_COST_LIMIT) return fail(GST_OVERFLOW, "proposal cost reached GST_COST_LIMIT");
   r->cost = (int32_t)pick.cost;
   r->root = g->inv[(size_t)root];
+  r->launches = launches;
   r->status = GST_OK;
   return GST_OK;
 }
@@ -1623,6 +1631,7 @@ gst_status gst_solve_learned(gst_graph* g, gst_scorer* sc, const int32_t* group_
       r->status = GST_OK;
       r->proposal_cost = prop.cost;
       r->propose_ms = pms;
+      r->launches += prop.launches;
       return GST_OK;
     }
     if (st != GST_INFEASIBLE) {
@@ -1637,6 +1646,7 @@ gst_status gst_solve_learned(gst_graph* g, gst_scorer* sc, const int32_t* group_
   st = solve_one(g, group_ptr, members, k, o, r);
   r->status = st;
   r->propose_ms = pms;
+  r->launches += prop.launches;
   return st;
 }
 
