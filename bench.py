@@ -97,6 +97,24 @@ def make_query(wl, g, i):
     return N.gen_groups_uniform(g.V, wl["k"], wl["uniform"], seed)
 
 
+# ------------------------------------------------------------- replicas --
+def rank_query_ids(rank: int, n: int) -> range:
+    """Query seeds of one replica: every rank solves its own n queries."""
+    return range(rank * n, (rank + 1) * n)
+
+
+def max_over_ranks(values, dist=None):
+    """This rank's timed totals -> the max over ranks (an all-reduce on the
+    host process group); the slowest replica sets the job's time."""
+    if dist is None:
+        return [float(v) for v in values]
+    import torch
+
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(x) for x in t]
+
+
 # --------------------------------------------------------------- clocks --
 class ClockSampler:
     """nvidia-smi clocks / throttle reasons sampled during the timed region."""
@@ -263,8 +281,7 @@ def main():
     g = make_graph(wl)
     log(f"graph: V={g.V} nnz={g.nnz} ({time.perf_counter() - t:.1f}s)")
     n_total = args.warmup + args.steps
-    qbase = rank * n_total
-    queries = [make_query(wl, g, qbase + i) for i in range(n_total)]
+    queries = [make_query(wl, g, i) for i in rank_query_ids(rank, n_total)]
     t = time.perf_counter()
     dg = N.Graph(g.row_ptr, g.col, g.w)
     upload_ms = 1e3 * (time.perf_counter() - t)
@@ -308,12 +325,7 @@ def main():
         torch.cuda.synchronize()
         if method == methods[-1]:
             clocks = clk.summary()
-        d_ms = sum(dev_ms(r, method) for r, _ in res)
-        w_s = sum(w for _, w in res)
-        if dist:
-            tt = torch.tensor([d_ms, w_s], dtype=torch.float64)
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            d_ms, w_s = float(tt[0]), float(tt[1])
+        d_ms, w_s = max_over_ranks([sum(dev_ms(r, method) for r, _ in res), sum(w for _, w in res)], dist)
         arms[method] = dict(results=res, dev_ms=d_ms, wall_s=w_s, qps=world * args.steps / (d_ms / 1e3),
                             e2e=world * args.steps / w_s)
     # Roofline pass of the growth kernels: the same plain queries through the
