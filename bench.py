@@ -70,6 +70,9 @@ WORKLOADS = {
     "ba4m_k7": dict(V=4_000_000, m=8, wmin=1, wmax=100, k=7, zipf=(1.2, 5, 500), graph_seed=5,
                     desc="learned-bound evaluation graph: BA m=8, |V|=4,000,000, w U[1,100], k=7, Zipf(1.2) "
                          "sizes in [5,500], degree-proportional members"),
+    "serve256": dict(V=1_000_000, m=4, wmin=1, wmax=100, k=(3, 7), zipf=(1.2, 5, 500), graph_seed=2, batch=256,
+                     desc="batched serving: one resident BA m=4 |V|=1,000,000 graph, w U[1,100]; batches of 256 "
+                          "queries, k uniform in {3..7}, Zipf(1.2) sizes in [5,500], degree-proportional members"),
     "rc1k_k3": dict(V=1000, E=5000, wmin=1, wmax=100, k=3, uniform=20, graph_seed=0,
                     desc="plain DPBF, single query: random connected |V|=1000 |E|=5000, w U[1,100], k=3 x 20"),
 }
@@ -91,9 +94,12 @@ def make_query(wl, g, i):
     from gpu4gst_code_gb300 import native as N
 
     seed = 1000 + i
+    k = wl["k"]
+    if isinstance(k, tuple):  # k uniform in [lo, hi], seeded per query
+        k = int(np.random.default_rng(seed).integers(k[0], k[1] + 1))
     if "zipf" in wl:
         s, lo, hi = wl["zipf"]
-        return N.gen_groups_zipf_degree(g, wl["k"], s, lo, hi, seed)
+        return N.gen_groups_zipf_degree(g, k, s, lo, hi, seed)
     return N.gen_groups_uniform(g.V, wl["k"], wl["uniform"], seed)
 
 
@@ -238,6 +244,83 @@ def run_reference(args, wl):
     print(json.dumps(line), flush=True)
 
 
+# -------------------------------------------------------------- serving --
+def run_serving(args, wl, world, rank, local_rank, dist):
+    """Batched serving: a step is one gst_solve_batch of wl['batch'] queries
+    (concurrent solve contexts over one resident graph), wall-clocked with
+    the device synchronised on both sides; per-query latencies from the
+    results. Methods: plain and bounded (value = bounded)."""
+    import torch
+
+    from gpu4gst_code_gb300 import native as N
+
+    torch.cuda.set_device(0)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    g = make_graph(wl)
+    B = wl["batch"]
+    n_total = args.warmup + args.steps
+    ids = rank_query_ids(rank, n_total * B + 32)
+    queries = [make_query(wl, g, i) for i in ids]
+    sample, queries = queries[:32], queries[32:]
+    dg = N.Graph(g.row_ptr, g.col, g.w)
+    t = time.perf_counter()
+    lanes = dg.autotune(sample, refine_bound=True)
+    tune_s = time.perf_counter() - t
+    arms = {}
+    clocks = None
+    for method in ("plain", "bounded"):
+        refine = method == "bounded"
+        batches = [queries[i * B:(i + 1) * B] for i in range(n_total)]
+        for b in batches[:args.warmup]:
+            dg.solve_batch(b, use_graph=True, refine_bound=refine)
+        if dist:
+            dist.barrier()
+        walls, lat_own, lat_done, costs, launches = [], [], [], [], 0
+        with ClockSampler(local_rank) as clk:
+            for b in batches[args.warmup:]:
+                flush.fill_(len(walls) & 0xFF)
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                res = dg.solve_batch(b, use_graph=True, refine_bound=refine)
+                torch.cuda.synchronize()
+                walls.append(time.perf_counter() - t0)
+                for r in res:
+                    assert r.status == N.Status.OK, r.status
+                    lat_own.append(r.latency_ms[0])
+                    lat_done.append(r.latency_ms[1])
+                    costs.append(r.cost)
+                    launches += r.launches
+        if method == "bounded":
+            clocks = clk.summary()
+        (wall,) = max_over_ranks([sum(walls)], dist)
+        arms[method] = dict(qps=world * B * args.steps / wall, wall=wall, costs=costs, launches=launches,
+                            p50=float(np.percentile(lat_own, 50)), p99=float(np.percentile(lat_own, 99)),
+                            c50=float(np.percentile(lat_done, 50)), c99=float(np.percentile(lat_done, 99)))
+    assert arms["plain"]["costs"] == arms["bounded"]["costs"]
+    head = arms["bounded"]
+    h2d = int(np.mean([(len(q[0]) + len(q[1])) * 4 for q in queries]))
+    line = {
+        "metric": "GST queries/sec (batched serving, k in {3..7}, |V|=1M, exact)", "value": head["qps"],
+        "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * head["wall"] / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded generators; no public dataset)",
+        "config": {"workload": args.workload, "desc": wl["desc"], "batch": B, "lanes": lanes,
+                   "tuned_shift_by_k": "gst_autotune on 32 separate queries", "autotune_s": tune_s,
+                   "method": METHOD_DESC["bounded"], "driver": "graph",
+                   "l2": "flushed before every batch (256 MiB device write)"},
+        "methods": {m: {"value": a["qps"], "latency_ms_p50": a["p50"], "latency_ms_p99": a["p99"],
+                        "completion_ms_p50": a["c50"], "completion_ms_p99": a["c99"]} for m, a in arms.items()},
+        "speedup_vs_plain": {"bounded": head["qps"] / arms["plain"]["qps"]},
+        "latency_ms": {"p50": head["p50"], "p99": head["p99"], "note": "each query's own solve, wall clock"},
+        "e2e": {"value": head["qps"], "unit": UNIT, "h2d_bytes_per_step": h2d * B, "d2h_bytes_per_step": 400 * B},
+        "gpu_launches": head["launches"],
+        "clocks": clocks,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    dg.close()
+
+
 # ------------------------------------------------------------------ ours --
 def main():
     ap = argparse.ArgumentParser()
@@ -264,6 +347,16 @@ def main():
 
     if args.impl == "reference":
         return run_reference(args, wl)
+    if "batch" in wl:
+        dist = None
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.init_process_group("gloo")
+        run_serving(args, wl, world, rank, local_rank, dist)
+        if dist:
+            dist.destroy_process_group()
+        return
 
     import torch
 

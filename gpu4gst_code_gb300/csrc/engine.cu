@@ -32,6 +32,8 @@
 #include <cstring>
 #include <functional>
 #include <mutex>
+#include <thread>
+#include <atomic>
 #include <new>
 #include <string>
 #include <unordered_set>
@@ -82,6 +84,8 @@ constexpr int kPollEvery = 8;           // host loop: rounds launched between po
 constexpr int kEvents = 3 * GST_MAX_K + 8;
 constexpr int kProposeTop = 256;       // top-scored vertices offered to the proposal's repair
 constexpr int kProposeRounds = 12;     // growth rounds of the proposal's root distances
+constexpr int32_t kDefaultLanes = 4;   // concurrent solve contexts of a batch
+constexpr int32_t kMaxLanes = 8;
 }  // namespace
 
 // ---------------------------------------------------------------- objects --
@@ -188,6 +192,15 @@ struct gst_graph {
   std::mutex mu;
   Workspace ws;
   LearnWs lw;
+  // Serving lanes: extra solve contexts sharing this graph's device arrays
+  // (own workspace and streams), used by concurrent batches.
+  bool owns_device = true;
+  const gst_graph* parent = nullptr;
+  std::vector<gst_graph*> lanes;
+  // Tuning (gst_autotune): dense-round shift per k (0 = default) and the
+  // batch concurrency (0 = default).
+  int32_t tuned_shift[GST_MAX_K + 1] = {};
+  int32_t tuned_lanes = 0;
 };
 
 struct gst_result {
@@ -200,6 +213,7 @@ struct gst_result {
   int64_t launches = 0;  // kernels this solve launched
   double ms[4] = {0, 0, 0, 0};
   int64_t stats[kNumStats] = {};
+  double lat_ms[2] = {0, 0};  // batch: own solve wall time, completion since the batch began
   int32_t ub = 0;             // pruning bound at the last wave (0 = none)
   int32_t proposal_cost = 0;  // cost of the learned path's proposed tree
   double propose_ms = 0;      // host wall time of the proposal
@@ -726,7 +740,11 @@ gst_status solve_one(gst_graph* g, const int32_t* group_ptr, const int32_t* memb
   ws.h_params->stats_on = o.collect_stats ? 1 : 0;
   ws.h_params->k = k;
   ws.h_params->ovf_limit = kInf - std::max<int32_t>(g->max_w, 1);
-  ws.h_params->dense_shift = o.dense_shift > 0 && o.dense_shift < 31 ? o.dense_shift : kDefaultDenseShift;
+  const gst_graph* tg = g->parent ? g->parent : g;
+  const int32_t tuned = tg->tuned_shift[k];
+  ws.h_params->dense_shift = o.dense_shift > 0 && o.dense_shift < 31 ? o.dense_shift
+                             : tuned > 0                              ? tuned
+                                                                      : kDefaultDenseShift;
   ws.h_params->refine = o.refine_bound ? 1 : 0;
 
   GST_CUDA(cudaEventRecord(ws.ev[0], s));
@@ -1196,6 +1214,39 @@ gst_status propose_tree(gst_graph* g, const gst_scorer* sc, const int32_t* group
   r->status = GST_OK;
   return GST_OK;
 }
+// Serving lanes: n extra contexts that share g's device arrays.
+gst_status ensure_lanes(gst_graph* g, int32_t n) {
+  std::lock_guard<std::mutex> lock(g->mu);
+  while ((int32_t)g->lanes.size() < n) {
+    auto* l = new (std::nothrow) gst_graph;
+    if (!l) return fail(GST_OOM, "host allocation failed");
+    l->owns_device = false;
+    l->parent = g;
+    l->device = g->device;
+    l->num_sms = g->num_sms;
+    l->V = g->V;
+    l->nnz = g->nnz;
+    l->d_row_ptr = g->d_row_ptr;
+    l->d_adj = g->d_adj;
+    l->d_big = g->d_big;
+    l->nbig = g->nbig;
+    l->d_order = g->d_order;
+    l->d_hub_chunk = g->d_hub_chunk;
+    l->nchunks = g->nchunks;
+    l->max_w = g->max_w;
+    l->perm = g->perm;
+    l->inv = g->inv;
+    l->d_perm = g->d_perm;
+    l->d_hub_of = g->d_hub_of;
+    g->lanes.push_back(l);  // freed with g from here on
+    cudaError_t e;
+    if ((e = cudaStreamCreateWithFlags(&l->stream, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaStreamCreateWithFlags(&l->side, cudaStreamNonBlocking)) != cudaSuccess)
+      return fail(GST_CUDA_ERROR, std::string("lane streams: ") + cudaGetErrorString(e));
+  }
+  return GST_OK;
+}
+
 }  // namespace
 
 // ------------------------------------------------------------------ C ABI --
@@ -1318,19 +1369,23 @@ gst_status gst_graph_upload(const int32_t* row_ptr, const int32_t* col, const in
 
 void gst_graph_free(gst_graph* g) {
   if (!g) return;
+  for (gst_graph* l : g->lanes) gst_graph_free(l);
+  g->lanes.clear();
   int prev = -1;
   cudaGetDevice(&prev);
   cudaSetDevice(g->device);
   if (g->stream) cudaStreamSynchronize(g->stream);
   free_workspace(g->ws);
   free_learn(g->lw);
-  dfree(g->d_row_ptr);
-  dfree(g->d_perm);
-  dfree(g->d_hub_of);
-  dfree(g->d_adj);
-  dfree(g->d_big);
-  dfree(g->d_order);
-  dfree(g->d_hub_chunk);
+  if (g->owns_device) {
+    dfree(g->d_row_ptr);
+    dfree(g->d_perm);
+    dfree(g->d_hub_of);
+    dfree(g->d_adj);
+    dfree(g->d_big);
+    dfree(g->d_order);
+    dfree(g->d_hub_chunk);
+  }
   if (g->stream) cudaStreamDestroy(g->stream);
   if (g->side) cudaStreamDestroy(g->side);
   if (prev >= 0) cudaSetDevice(prev);
@@ -1371,22 +1426,154 @@ gst_status gst_solve_batch(gst_graph* g, int32_t nq, const int32_t* ks, const in
                            const int32_t* members, const gst_opts* opts, gst_result** out) {
   g_last_error.clear();
   if (!out || !g || nq < 0 || (nq > 0 && (!ks || !group_ptr))) return fail(GST_BAD_INPUT, "bad batch arguments");
-  gst_status first = GST_OK;
+  const gst_opts o = resolve_opts(opts);
+  // per-query group arrays, rebased
+  std::vector<std::vector<int32_t>> gps((size_t)nq);
+  std::vector<const int32_t*> mems((size_t)nq, nullptr);
+  std::vector<gst_status> pre((size_t)nq, GST_OK);
   int64_t gbase = 0;
   for (int32_t q = 0; q < nq; ++q) {
     out[q] = nullptr;
     if (ks[q] < 1 || ks[q] > GST_MAX_K) {
-      if (first == GST_OK) first = fail(GST_BAD_INPUT, "k out of range in batch");
+      pre[(size_t)q] = GST_BAD_INPUT;
       continue;
     }
-    std::vector<int32_t> gp((size_t)ks[q] + 1);
+    auto& gp = gps[(size_t)q];
+    gp.resize((size_t)ks[q] + 1);
     for (int32_t i = 0; i <= ks[q]; ++i) gp[(size_t)i] = group_ptr[gbase + i] - group_ptr[gbase];
-    const int32_t* mem = members ? members + group_ptr[gbase] : nullptr;
-    gst_status st = gst_solve(g, gp.data(), mem, ks[q], opts, &out[q]);
-    if (st != GST_OK && st != GST_INFEASIBLE && first == GST_OK) first = st;
+    mems[(size_t)q] = members ? members + group_ptr[gbase] : nullptr;
     gbase += ks[q];
   }
+  const int32_t want = o.concurrency > 0 ? o.concurrency : (g->tuned_lanes > 0 ? g->tuned_lanes : kDefaultLanes);
+  const int32_t nl = std::max(1, std::min({want, nq, kMaxLanes}));
+  gst_status st = ensure_lanes(g, nl - 1);
+  if (st != GST_OK) return st;
+  std::vector<gst_graph*> ctx{g};
+  for (int32_t i = 0; i + 1 < nl; ++i) ctx.push_back(g->lanes[(size_t)i]);
+  std::atomic<int32_t> next{0};
+  std::vector<std::string> errs((size_t)nq);
+  const auto t0 = std::chrono::steady_clock::now();
+  auto worker = [&](gst_graph* c) {
+    cudaSetDevice(c->device);
+    std::lock_guard<std::mutex> lock(c->mu);
+    for (int32_t q; (q = next.fetch_add(1)) < nq;) {
+      if (pre[(size_t)q] != GST_OK) {
+        errs[(size_t)q] = "k out of range in batch";
+        continue;
+      }
+      auto* r = new (std::nothrow) gst_result;
+      if (!r) {
+        errs[(size_t)q] = "host allocation failed";
+        continue;
+      }
+      out[q] = r;
+      const auto ts = std::chrono::steady_clock::now();
+      g_last_error.clear();
+      bool empty = false;
+      const int32_t k = ks[q];
+      gst_status s2 = validate_groups(c, gps[(size_t)q].data(), mems[(size_t)q], k, &empty);
+      if (s2 == GST_OK && empty) s2 = GST_INFEASIBLE;
+      if (s2 == GST_OK) {
+        cudaGetLastError();
+        s2 = solve_one(c, gps[(size_t)q].data(), mems[(size_t)q], k, o, r);
+      }
+      r->status = s2;
+      if (s2 != GST_OK && s2 != GST_INFEASIBLE) errs[(size_t)q] = g_last_error;
+      const auto te = std::chrono::steady_clock::now();
+      r->lat_ms[0] = std::chrono::duration<double, std::milli>(te - ts).count();
+      r->lat_ms[1] = std::chrono::duration<double, std::milli>(te - t0).count();
+    }
+  };
+  if (nl == 1) {
+    worker(g);
+  } else {
+    std::vector<std::thread> th;
+    for (gst_graph* c : ctx) th.emplace_back(worker, c);
+    for (auto& t : th) t.join();
+  }
+  gst_status first = GST_OK;
+  for (int32_t q = 0; q < nq; ++q) {
+    const gst_status sq = out[q] ? out[q]->status : pre[(size_t)q] != GST_OK ? pre[(size_t)q] : GST_OOM;
+    if (sq != GST_OK && sq != GST_INFEASIBLE && first == GST_OK) {
+      first = sq;
+      g_last_error = errs[(size_t)q];
+    }
+  }
   return first;
+}
+
+gst_status gst_autotune(gst_graph* g, int32_t nq, const int32_t* ks, const int32_t* group_ptr,
+                        const int32_t* members, const gst_opts* opts, int32_t* lanes_out) {
+  g_last_error.clear();
+  if (!g || nq < 1 || !ks || !group_ptr) return fail(GST_BAD_INPUT, "bad autotune arguments");
+  gst_opts o = resolve_opts(opts);
+  // 1. dense-round shift per k: up to two sample queries of that k each
+  std::vector<int64_t> offs((size_t)nq + 1, 0);
+  for (int32_t q = 0; q < nq; ++q) {
+    if (ks[q] < 1 || ks[q] > GST_MAX_K) return fail(GST_BAD_INPUT, "k out of range in autotune");
+    offs[(size_t)q + 1] = offs[(size_t)q] + ks[q];
+  }
+  for (int32_t k = 1; k <= GST_MAX_K; ++k) {
+    std::vector<int32_t> sample;
+    for (int32_t q = 0; q < nq && sample.size() < 2; ++q)
+      if (ks[q] == k) sample.push_back(q);
+    if (sample.empty()) continue;
+    double best_ms = 1e300;
+    int32_t best_shift = kDefaultDenseShift;
+    for (int32_t shift : {1, 2, 3, 4}) {
+      double ms = 0;
+      for (int rep = 0; rep < 2; ++rep)  // the first pass also captures the query graphs
+        for (int32_t q : sample) {
+          std::vector<int32_t> gp((size_t)k + 1);
+          for (int32_t i = 0; i <= k; ++i) gp[(size_t)i] = group_ptr[offs[(size_t)q] + i] - group_ptr[offs[(size_t)q]];
+          gst_opts oq = o;
+          oq.dense_shift = shift;
+          gst_result* r = nullptr;
+          const gst_status sq = gst_solve(g, gp.data(), members ? members + group_ptr[offs[(size_t)q]] : nullptr, k, &oq, &r);
+          if (sq != GST_OK && sq != GST_INFEASIBLE) {
+            gst_result_free(r);
+            return sq;
+          }
+          if (rep == 1) ms += r->ms[0];
+          gst_result_free(r);
+        }
+      if (ms < best_ms) {
+        best_ms = ms;
+        best_shift = shift;
+      }
+    }
+    g->tuned_shift[k] = best_shift;
+  }
+  // 2. batch concurrency: the sample as one batch per candidate, wall time
+  std::vector<gst_result*> res((size_t)nq, nullptr);
+  double best_s = 1e300;
+  int32_t best_l = 1;
+  for (int32_t l : {1, 2, 4, 8}) {
+    if (l > kMaxLanes) break;
+    gst_opts ob = o;
+    ob.concurrency = l;
+    for (int rep = 0; rep < 2; ++rep) {
+      const auto t0 = std::chrono::steady_clock::now();
+      const gst_status sb = gst_solve_batch(g, nq, ks, group_ptr, members, &ob, res.data());
+      const double sec = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+      for (auto*& r : res) {
+        gst_result_free(r);
+        r = nullptr;
+      }
+      if (sb != GST_OK && sb != GST_INFEASIBLE) return sb;
+      if (rep == 1 && sec < best_s) {
+        best_s = sec;
+        best_l = l;
+      }
+    }
+  }
+  g->tuned_lanes = best_l;
+  if (lanes_out) *lanes_out = best_l;
+  return GST_OK;
+}
+
+void gst_result_latency(const gst_result* r, double* ms2) {
+  if (r && ms2) std::copy(r->lat_ms, r->lat_ms + 2, ms2);
 }
 
 void gst_result_free(gst_result* r) { delete r; }

@@ -55,7 +55,8 @@ class Opts(C.Structure):
         ("collect_stats", C.c_int32),
         ("dense_shift", C.c_int32),
         ("refine_bound", C.c_int32),
-        ("reserved", C.c_int32 * 9),
+        ("concurrency", C.c_int32),
+        ("reserved", C.c_int32 * 8),
     ]
 
 
@@ -70,6 +71,8 @@ SIGNATURES = {
         C.c_int,
         [C.c_void_p, C.c_int32, I32P, I32P, I32P, C.POINTER(Opts), C.POINTER(C.c_void_p)],
     ),
+    "gst_autotune": (C.c_int, [C.c_void_p, C.c_int32, I32P, I32P, I32P, C.POINTER(Opts), I32P]),
+    "gst_result_latency": (None, [C.c_void_p, F64P]),
     "gst_result_free": (None, [C.c_void_p]),
     "gst_result_status": (C.c_int, [C.c_void_p]),
     "gst_result_cost": (C.c_int32, [C.c_void_p]),
@@ -178,6 +181,7 @@ class Result:
     launches: int = 0
     times_ms: tuple = (0.0, 0.0, 0.0, 0.0)
     stats: dict = field(default_factory=dict)
+    latency_ms: tuple = (0.0, 0.0)  # batch: own solve, completion since the batch began
     upper_bound: int = 0  # pruning bound at the last wave (0: unpruned)
     proposal_cost: int = 0  # learned path: cost of the proposed tree (0: none)
     proposal_ms: float = 0.0
@@ -205,6 +209,8 @@ def _read_result(r) -> Result:
     L.gst_result_times(r, t)
     s = (C.c_int64 * 8)()
     L.gst_result_stats(r, s)
+    lat = (C.c_double * 2)()
+    L.gst_result_latency(r, lat)
     return Result(
         status=st,
         cost=int(L.gst_result_cost(r)),
@@ -215,6 +221,7 @@ def _read_result(r) -> Result:
         launches=int(L.gst_result_launches(r)),
         times_ms=tuple(t),
         stats=dict(zip(STAT_NAMES, list(s))),
+        latency_ms=tuple(lat),
         upper_bound=int(L.gst_result_upper_bound(r)),
         proposal_cost=int(L.gst_result_proposal_cost(r)),
         proposal_ms=float(L.gst_result_proposal_ms(r)),
@@ -222,7 +229,7 @@ def _read_result(r) -> Result:
 
 
 def make_opts(upper_bound: int = 0, max_rounds: int = 0, use_graph: bool = False, collect_stats: bool = False,
-              dense_shift: int = 0, refine_bound: bool = False) -> Opts:
+              dense_shift: int = 0, refine_bound: bool = False, concurrency: int = 0) -> Opts:
     o = Opts()
     o.struct_size = C.sizeof(Opts)
     o.upper_bound = int(upper_bound)
@@ -231,6 +238,7 @@ def make_opts(upper_bound: int = 0, max_rounds: int = 0, use_graph: bool = False
     o.collect_stats = int(bool(collect_stats))
     o.dense_shift = int(dense_shift)
     o.refine_bound = int(bool(refine_bound))
+    o.concurrency = int(concurrency)
     return o
 
 
@@ -342,8 +350,8 @@ class Graph:
             raise GSTError(st, last_error())
         return out.reshape(self.V, 1 << k)
 
-    def solve_batch(self, queries, *, upper_bound=0, use_graph=False, collect_stats=False) -> list[Result]:
-        """queries: list of (group_ptr, members) or list of member-list lists."""
+    @staticmethod
+    def _pack_batch(queries):
         ks, gptr, mem = [], [0], []
         for q in queries:
             gp, m = q if isinstance(q, tuple) else groups_to_csr(q)
@@ -352,10 +360,25 @@ class Graph:
             base = len(mem)
             mem.extend(int(x) for x in m)
             gptr.extend(int(base + x) for x in gp[1:])
-        ks_a, gp_a, mem_a = _i32(ks), _i32(gptr), _i32(mem)
-        n = len(ks)
+        return _i32(ks), _i32(gptr), _i32(mem)
+
+    def autotune(self, queries, *, use_graph=True, refine_bound=False) -> int:
+        """gst_autotune on a sample of queries; returns the tuned concurrency."""
+        ks_a, gp_a, mem_a = self._pack_batch(queries)
+        o = make_opts(0, 0, use_graph, False, 0, refine_bound)
+        lanes = C.c_int32(0)
+        st = lib().gst_autotune(self._h, len(ks_a), _ptr(ks_a), _ptr(gp_a), _ptr(mem_a), C.byref(o), C.byref(lanes))
+        if st != Status.OK:
+            raise GSTError(st, last_error())
+        return int(lanes.value)
+
+    def solve_batch(self, queries, *, upper_bound=0, use_graph=False, collect_stats=False, refine_bound=False,
+                    concurrency=0) -> list[Result]:
+        """queries: list of (group_ptr, members) or list of member-list lists."""
+        ks_a, gp_a, mem_a = self._pack_batch(queries)
+        n = len(ks_a)
         outs = (C.c_void_p * n)()
-        o = make_opts(upper_bound, 0, use_graph, collect_stats)
+        o = make_opts(upper_bound, 0, use_graph, collect_stats, 0, refine_bound, concurrency)
         st = lib().gst_solve_batch(self._h, n, _ptr(ks_a), _ptr(gp_a), _ptr(mem_a), C.byref(o), outs)
         msg = last_error()
         res = []

@@ -79,7 +79,11 @@ typedef struct gst_opts {
    * best solution (graph_v_of_v_idealID_PrunedDPPlusPlus.h:668-711). Turns
    * pruning on from wave 2 even without an upper_bound. Exact either way. */
   int32_t refine_bound;
-  int32_t reserved[9];
+  /* gst_solve_batch: solve contexts run concurrently, each with its own
+   * workspace and streams over the one resident graph; 0 = the tuned value
+   * (gst_autotune), else 4. Capped at 8. */
+  int32_t concurrency;
+  int32_t reserved[8];
 } gst_opts;
 
 /* ---------------------------------------------------------------- graph -- */
@@ -123,9 +127,21 @@ gst_status gst_solve(gst_graph *g, const int32_t *group_ptr, const int32_t *memb
 gst_status gst_solve_batch(gst_graph *g, int32_t nq, const int32_t *ks, const int32_t *group_ptr,
                            const int32_t *members, const gst_opts *opts, gst_result **out);
 
+/* Tunes the graph for a sample of queries (laid out as for
+ * gst_solve_batch): for every k present, the dense-round shift (1..4) that
+ * solves its sample fastest; then the batch concurrency (1, 2, 4 or 8) that
+ * solves the whole sample fastest. Later solves with dense_shift 0 and
+ * batches with concurrency 0 use the tuned values. Results never depend on
+ * tuning. No counterpart in the reference. */
+gst_status gst_autotune(gst_graph *g, int32_t nq, const int32_t *ks, const int32_t *group_ptr,
+                        const int32_t *members, const gst_opts *opts, int32_t *lanes_out);
+
 /* --------------------------------------------------------------- result -- */
 
 void gst_result_free(gst_result *r);
+/* Batch results: ms2[0] = the query's own solve (host wall time),
+ * ms2[1] = its completion since the batch began. */
+void gst_result_latency(const gst_result *r, double *ms2);
 gst_status gst_result_status(const gst_result *r);
 /* Optimal cost (DPBF_GPU's *real_cost), -1 if infeasible. */
 int32_t gst_result_cost(const gst_result *r);

@@ -226,3 +226,36 @@ def test_stats_and_launch_count(use_graph):
         # each state evaluates its unordered splits, except states of cost 0
         assert 0 < st["splits"] <= 20000 * (3**5 - 2**6 + 1) // 2
         assert res.launches >= 1 + 5 + st["rounds"] + 2
+
+
+def _ba_queries(V, n, seed):
+    g = native.gen_barabasi_albert(V, 4, 1, 100, seed)
+    rng = np.random.default_rng(seed)
+    qs = [native.gen_groups_zipf_degree(g, int(rng.integers(3, 7)), 1.2, 5, 60, seed * 1000 + i) for i in range(n)]
+    return g, qs
+
+
+@pytest.mark.parametrize("concurrency", [1, 3, 0])
+def test_concurrent_batch_matches_single(concurrency):
+    """gst_solve_batch runs queries on concurrent solve contexts (lanes)
+    over one resident graph: every result equals the single solve."""
+    g, qs = _ba_queries(20_000, 12, 31)
+    with native.Graph(g.row_ptr, g.col, g.w) as dg:
+        want = [dg.solve(gp, mem, use_graph=True).cost for gp, mem in qs]
+        for refine in (False, True):
+            got = dg.solve_batch(qs, use_graph=True, refine_bound=refine, concurrency=concurrency)
+            assert [r.cost for r in got] == want
+            for (gp, mem), r in zip(qs, got):
+                _check(g.row_ptr, g.col, g.w, gp, mem, r, r.cost)
+                assert r.latency_ms[0] > 0 and r.latency_ms[1] >= r.latency_ms[0] * 0.999
+
+
+def test_autotune_keeps_results_exact():
+    g, qs = _ba_queries(20_000, 16, 37)
+    with native.Graph(g.row_ptr, g.col, g.w) as dg:
+        want = [dg.solve(gp, mem).cost for gp, mem in qs]
+        lanes = dg.autotune(qs[:8], refine_bound=True)
+        assert lanes in (1, 2, 4, 8)
+        got = dg.solve_batch(qs, use_graph=True, refine_bound=True)
+        assert [r.cost for r in got] == want
+        assert [dg.solve(gp, mem, use_graph=True).cost for gp, mem in qs] == want
