@@ -12,8 +12,9 @@ queries run through three exact methods, each through the C ABI:
   learned   gst_solve_learned with the committed trained scorer: proposal
             tree from the network's top vertex, then the bounded DP.
 
-`value` is the learned method's throughput (the metric's method); the
-other two and the speedups ride along in the same line.
+`value` is the bound-refined method's throughput (the fastest exact method
+on this workload); the plain and learned methods and their speedups over
+plain ride along in the same line (`methods`, `speedup_vs_plain`).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -330,8 +331,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="ba1m_k6", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--methods", default="plain,bounded,learned",
-                    help="comma-separated subset of plain,bounded,learned (profiling runs); value = the last")
+    ap.add_argument("--methods", default="plain,learned,bounded",
+                    help="comma-separated subset of plain,learned,bounded (profiling runs); value = the last of "
+                         "plain, learned, bounded present")
     ap.add_argument("--driver", default="graph", choices=["graph", "host"],
                     help="graph: one captured CUDA graph per query; host: host-launched growth rounds")
     args = ap.parse_args()
@@ -404,7 +406,8 @@ def main():
 
     arms = {}
     clocks = None
-    methods = [m for m in ("plain", "bounded", "learned") if m in args.methods.split(",")]
+    # the last method is the line's `value`: the bound-refined DP, the fastest exact method here
+    methods = [m for m in ("plain", "learned", "bounded") if m in args.methods.split(",")]
     for method in methods:
         for i in range(args.warmup):
             step(i, method)
