@@ -26,7 +26,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-r
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC"]
 
 CU_SOURCES = ["dpbf_kernels.cu", "learn_kernels.cu", "engine.cu", "noalloc.cu"]
-CXX_SOURCES = ["gen.cpp"]
+CXX_SOURCES = ["gen.cpp", "dataset.cpp"]
 
 
 def nvcc() -> str:
@@ -42,7 +42,7 @@ def toolkit_available() -> bool:
 
 def _inputs() -> list[Path]:
     files = [CSRC / s for s in CU_SOURCES + CXX_SOURCES]
-    files += sorted(CSRC.glob("*.cuh")) + sorted(CSRC.glob("*.h")) + sorted(INCLUDE.glob("*.h"))
+    files += sorted(CSRC.glob("*.cuh")) + sorted(CSRC.glob("*.h")) + sorted(CSRC.glob("*.hpp")) + sorted(INCLUDE.glob("*.h"))
     files.append(Path(__file__))
     return files
 

@@ -1249,6 +1249,10 @@ gst_status ensure_lanes(gst_graph* g, int32_t n) {
 
 }  // namespace
 
+namespace gst {
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+}  // namespace gst
+
 // ------------------------------------------------------------------ C ABI --
 extern "C" {
 

@@ -1,5 +1,6 @@
 // Seeded synthetic GST instances (host only); see include/gst_gen.h.
 #include "gst_gen.h"
+#include "host_types.hpp"
 
 #include <algorithm>
 #include <cmath>
@@ -9,15 +10,6 @@
 #include <utility>
 #include <vector>
 
-struct gst_host_graph {
-  int32_t V = 0;
-  std::vector<int32_t> row_ptr, col, w;
-};
-
-struct gst_host_groups {
-  int32_t k = 0;
-  std::vector<int32_t> group_ptr, members;
-};
 
 namespace {
 

@@ -1,4 +1,4 @@
-"""ctypes binding of libgst.so (include/gst.h, gst_gen.h, gst_learn.h, gst_debug.h).
+"""ctypes binding of libgst.so (include/gst.h, gst_gen.h, gst_io.h, gst_learn.h, gst_debug.h).
 
 The library is the product: every solve runs the CUDA kernels in libgst.so.
 There is no Python or CPU fallback; if the library is missing this module
@@ -127,6 +127,11 @@ SIGNATURES = {
     "gst_host_groups_num_members": (C.c_int64, [C.c_void_p]),
     "gst_host_groups_copy": (None, [C.c_void_p, I32P, I32P]),
     "gst_host_groups_free": (None, [C.c_void_p]),
+    # dataset readers (include/gst_io.h)
+    "gst_read_graph_file": (C.c_int, [C.c_char_p, C.POINTER(C.c_void_p), I32P]),
+    "gst_read_groups_file": (C.c_int, [C.c_char_p, C.POINTER(C.c_void_p)]),
+    "gst_read_queries_file": (C.c_int, [C.c_char_p, C.c_int32, C.POINTER(C.c_void_p)]),
+    "gst_read_gstp_instance": (C.c_int, [C.c_char_p, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]),
 }
 
 _LIB = None
@@ -518,3 +523,71 @@ def gen_groups_zipf_degree(g: CSR, k: int, s: float, size_min: int, size_max: in
     return _take_groups(
         lib().gst_gen_groups_zipf_degree(_ptr(rp), _ptr(col), g.V, g.nnz, k, s, size_min, size_max, seed)
     )
+
+
+# ---------------------------------------------------------------- datasets --
+def _fs(path) -> bytes:
+    return str(path).encode()
+
+
+def read_graph_file(path) -> tuple[CSR, int]:
+    """<name>.in (the reference's read_input_graph) -> (CSR, number of communities)."""
+    h = C.c_void_p()
+    c = C.c_int32(0)
+    st = lib().gst_read_graph_file(_fs(path), C.byref(h), C.byref(c))
+    if st != Status.OK:
+        raise GSTError(st, last_error())
+    return _take_graph(h.value), int(c.value)
+
+
+def _take_lists(h) -> tuple[np.ndarray, np.ndarray]:
+    L = lib()
+    try:
+        k = L.gst_host_groups_k(h)
+        n = L.gst_host_groups_num_members(h)
+        gp = np.zeros(k + 1, np.int32)
+        mem = np.zeros(n, np.int32)
+        L.gst_host_groups_copy(h, _ptr(gp), _ptr(mem))
+    finally:
+        L.gst_host_groups_free(h)
+    return gp, mem
+
+
+def read_groups_file(path) -> tuple[np.ndarray, np.ndarray]:
+    """<name>.g (read_Group) -> every group of the dataset as (group_ptr, members)."""
+    h = C.c_void_p()
+    st = lib().gst_read_groups_file(_fs(path), C.byref(h))
+    if st != Status.OK:
+        raise GSTError(st, last_error())
+    return _take_lists(h.value)
+
+
+def read_queries_file(path, V: int) -> list[list[int]]:
+    """<name>.gK (read_inquire) -> per query, its group indices (value - V)."""
+    h = C.c_void_p()
+    st = lib().gst_read_queries_file(_fs(path), int(V), C.byref(h))
+    if st != Status.OK:
+        raise GSTError(st, last_error())
+    qp, ids = _take_lists(h.value)
+    return [ids[qp[i]:qp[i + 1]].tolist() for i in range(len(qp) - 1)]
+
+
+def read_gstp_instance(path) -> tuple[CSR, np.ndarray, np.ndarray]:
+    """A GSTP instance text (graph_hash_of_mixed_weighted_save_for_GSTP) -> (CSR, group_ptr, members)."""
+    hg, hq = C.c_void_p(), C.c_void_p()
+    st = lib().gst_read_gstp_instance(_fs(path), C.byref(hg), C.byref(hq))
+    if st != Status.OK:
+        raise GSTError(st, last_error())
+    g = _take_graph(hg.value)
+    gp, mem = _take_lists(hq.value)
+    return g, gp, mem
+
+
+def query_groups(all_groups: tuple[np.ndarray, np.ndarray], ids) -> tuple[np.ndarray, np.ndarray]:
+    """The (group_ptr, members) of one query from the dataset's groups."""
+    gp_all, mem_all = all_groups
+    gp, mem = [0], []
+    for i in ids:
+        mem.extend(mem_all[gp_all[i]:gp_all[i + 1]].tolist())
+        gp.append(len(mem))
+    return _i32(gp), _i32(mem)

@@ -259,3 +259,24 @@ def test_autotune_keeps_results_exact():
         got = dg.solve_batch(qs, use_graph=True, refine_bound=True)
         assert [r.cost for r in got] == want
         assert [dg.solve(gp, mem, use_graph=True).cost for gp, mem in qs] == want
+
+
+def test_dataset_files_solve_like_the_reference_harness(tmp_path):
+    """A dataset in the reference's file formats (.in/.g/.g7), read with the
+    gst_io readers and solved query by query (rucgraph/test_gpu.h:115-215)."""
+    from test_dataset_cpu import write_in
+
+    g = native.gen_random_connected(400, 1600, 1, 100, 21)
+    write_in(tmp_path / "d.in", g)
+    groups = [native.gen_groups_uniform(g.V, 1, 6, 900 + i)[1].tolist() for i in range(6)]
+    (tmp_path / "d.g").write_text("".join(f"g{i + 1}:{' '.join(map(str, m))}\n" for i, m in enumerate(groups)))
+    (tmp_path / "d.g7").write_text(f"{g.V} {g.V + 3} {g.V + 5} \n{g.V + 1} {g.V + 2} {g.V + 4} \n")
+    h, _ = native.read_graph_file(tmp_path / "d.in")
+    all_groups = native.read_groups_file(tmp_path / "d.g")
+    queries = native.read_queries_file(tmp_path / "d.g7", h.V)
+    assert queries == [[0, 3, 5], [1, 2, 4]]
+    with native.Graph(h.row_ptr, h.col, h.w) as dg:
+        for ids in queries:
+            gp, mem = native.query_groups(all_groups, ids)
+            want = oracle.dpbf(h.row_ptr, h.col, h.w, gp, mem).cost
+            _check(h.row_ptr, h.col, h.w, gp, mem, dg.solve(gp, mem, use_graph=True), want)
