@@ -643,23 +643,38 @@ __device__ __forceinline__ void thread_vertex(const GraphDev& g, const LevelArgs
   ++acc[kAccVert];
   acc[kAccEnt] += end - beg;
   if (!live) return;
+  // software pipeline: the next batch's CSR entries (and, in sparse rounds,
+  // their change flags) are loaded while this batch's rows are gathered
+  int32_t nv[U], nw[U];
+  bool act[U];
+#pragma unroll
+  for (int i = 0; i < U; ++i) {
+    act[i] = beg + i < end;
+    nv[i] = 0;
+    nw[i] = 0;
+    if (act[i]) {
+      const int2 x = g.adj[beg + i];
+      nv[i] = x.x;
+      nw[i] = x.y;
+    }
+  }
+  if (!rs.dense) {
+#pragma unroll
+    for (int i = 0; i < U; ++i) act[i] = act[i] && rs.cur_flag[nv[i]] != 0;
+  }
   for (int32_t e0 = beg; e0 < end; e0 += U) {
-    int32_t nv[U], nw[U];
-    bool act[U];
+    int32_t nv2[U], nw2[U];
+    bool act2[U];
 #pragma unroll
     for (int i = 0; i < U; ++i) {
-      act[i] = e0 + i < end;
-      nv[i] = 0;
-      nw[i] = 0;
-      if (act[i]) {
-        const int2 x = g.adj[e0 + i];
-        nv[i] = x.x;
-        nw[i] = x.y;
+      act2[i] = e0 + U + i < end;
+      nv2[i] = 0;
+      nw2[i] = 0;
+      if (act2[i]) {
+        const int2 x = g.adj[e0 + U + i];
+        nv2[i] = x.x;
+        nw2[i] = x.y;
       }
-    }
-    if (!rs.dense) {
-#pragma unroll
-      for (int i = 0; i < U; ++i) act[i] = act[i] && rs.cur_flag[nv[i]] != 0;
     }
     int32_t rows[U][MP];
 #pragma unroll
@@ -694,6 +709,16 @@ __device__ __forceinline__ void thread_vertex(const GraphDev& g, const LevelArgs
         const int sh = 8 * (j & 3);
         code[j >> 2] = lt ? ((code[j >> 2] & ~(0xffu << sh)) | (rel << sh)) : code[j >> 2];
       }
+    }
+    if (!rs.dense) {
+#pragma unroll
+      for (int i = 0; i < U; ++i) act2[i] = act2[i] && rs.cur_flag[nv2[i]] != 0;
+    }
+#pragma unroll
+    for (int i = 0; i < U; ++i) {
+      nv[i] = nv2[i];
+      nw[i] = nw2[i];
+      act[i] = act2[i];
     }
   }
   bool any = false;
