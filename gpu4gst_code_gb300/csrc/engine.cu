@@ -214,6 +214,7 @@ struct gst_result {
   double ms[4] = {0, 0, 0, 0};
   int64_t stats[kNumStats] = {};
   double lat_ms[2] = {0, 0};  // batch: own solve wall time, completion since the batch began
+  int32_t replica = -1;       // pool: replica that solved the query
   int32_t ub = 0;             // pruning bound at the last wave (0 = none)
   int32_t proposal_cost = 0;  // cost of the learned path's proposed tree
   double propose_ms = 0;      // host wall time of the proposal
@@ -1575,6 +1576,95 @@ gst_status gst_autotune(gst_graph* g, int32_t nq, const int32_t* ks, const int32
   if (lanes_out) *lanes_out = best_l;
   return GST_OK;
 }
+
+struct gst_pool {
+  std::vector<gst_graph*> replicas;
+};
+
+gst_status gst_pool_create(const int32_t* row_ptr, const int32_t* col, const int32_t* w, int32_t V, int64_t nnz,
+                           const int32_t* devices, int32_t num_devices, gst_pool** out) {
+  g_last_error.clear();
+  if (!out || !devices || num_devices < 1) return fail(GST_BAD_INPUT, "devices / out missing");
+  *out = nullptr;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess) return fail(GST_CUDA_ERROR, "cudaGetDeviceCount failed");
+  for (int32_t i = 0; i < num_devices; ++i)
+    if (devices[i] < 0 || devices[i] >= count) return fail(GST_BAD_INPUT, "device index out of range");
+  auto* p = new (std::nothrow) gst_pool;
+  if (!p) return fail(GST_OOM, "host allocation failed");
+  int prev = -1;
+  cudaGetDevice(&prev);
+  for (int32_t i = 0; i < num_devices; ++i) {
+    cudaSetDevice(devices[i]);
+    gst_graph* g = nullptr;
+    const gst_status st = gst_graph_upload(row_ptr, col, w, V, nnz, &g);
+    if (st != GST_OK) {
+      const std::string msg = g_last_error;
+      gst_pool_free(p);
+      if (prev >= 0) cudaSetDevice(prev);
+      return fail(st, "replica " + std::to_string(i) + ": " + msg);
+    }
+    p->replicas.push_back(g);
+  }
+  if (prev >= 0) cudaSetDevice(prev);
+  *out = p;
+  return GST_OK;
+}
+
+void gst_pool_free(gst_pool* p) {
+  if (!p) return;
+  for (gst_graph* g : p->replicas) gst_graph_free(g);
+  delete p;
+}
+
+int32_t gst_pool_num_replicas(const gst_pool* p) { return p ? (int32_t)p->replicas.size() : 0; }
+
+gst_status gst_pool_solve_batch(gst_pool* p, int32_t nq, const int32_t* ks, const int32_t* group_ptr,
+                                const int32_t* members, const gst_opts* opts, gst_result** out) {
+  g_last_error.clear();
+  if (!p || p->replicas.empty() || !out || nq < 0 || (nq > 0 && (!ks || !group_ptr)))
+    return fail(GST_BAD_INPUT, "bad pool batch arguments");
+  // where each query's groups start
+  std::vector<int64_t> gofs((size_t)nq + 1, 0);
+  for (int32_t q = 0; q < nq; ++q) {
+    if (ks[q] < 1 || ks[q] > GST_MAX_K) return fail(GST_BAD_INPUT, "k out of range in batch");
+    gofs[(size_t)q + 1] = gofs[(size_t)q] + ks[q];
+  }
+  const int32_t chunk = std::max(1, std::min(16, nq / (4 * (int32_t)p->replicas.size()) + 1));
+  std::atomic<int32_t> next{0};
+  std::vector<gst_status> sts(p->replicas.size(), GST_OK);
+  std::vector<std::string> errs(p->replicas.size());
+  auto worker = [&](size_t ri) {
+    gst_graph* g = p->replicas[ri];
+    cudaSetDevice(g->device);
+    for (int32_t q0; (q0 = next.fetch_add(chunk)) < nq;) {
+      const int32_t n = std::min(chunk, nq - q0);
+      // the chunk's groups as their own batch (group_ptr rebased to its first group)
+      const int64_t g0 = gofs[(size_t)q0], g1 = gofs[(size_t)q0 + n];
+      std::vector<int32_t> gp((size_t)(g1 - g0 + 1));
+      for (int64_t i = 0; i <= g1 - g0; ++i) gp[(size_t)i] = group_ptr[g0 + i] - group_ptr[g0];
+      const gst_status st = gst_solve_batch(g, n, ks + q0, gp.data(), members ? members + group_ptr[g0] : nullptr,
+                                            opts, out + q0);
+      for (int32_t i = 0; i < n; ++i)
+        if (out[q0 + i]) out[q0 + i]->replica = (int32_t)ri;
+      if (st != GST_OK && st != GST_INFEASIBLE && sts[ri] == GST_OK) {
+        sts[ri] = st;
+        errs[ri] = g_last_error;
+      }
+    }
+  };
+  std::vector<std::thread> th;
+  for (size_t ri = 0; ri < p->replicas.size(); ++ri) th.emplace_back(worker, ri);
+  for (auto& t : th) t.join();
+  for (size_t ri = 0; ri < sts.size(); ++ri)
+    if (sts[ri] != GST_OK) {
+      g_last_error = errs[ri];
+      return sts[ri];
+    }
+  return GST_OK;
+}
+
+int32_t gst_result_replica(const gst_result* r) { return r ? r->replica : -1; }
 
 void gst_result_latency(const gst_result* r, double* ms2) {
   if (r && ms2) std::copy(r->lat_ms, r->lat_ms + 2, ms2);

@@ -72,6 +72,14 @@ SIGNATURES = {
         [C.c_void_p, C.c_int32, I32P, I32P, I32P, C.POINTER(Opts), C.POINTER(C.c_void_p)],
     ),
     "gst_autotune": (C.c_int, [C.c_void_p, C.c_int32, I32P, I32P, I32P, C.POINTER(Opts), I32P]),
+    "gst_pool_create": (C.c_int, [I32P, I32P, I32P, C.c_int32, C.c_int64, I32P, C.c_int32, C.POINTER(C.c_void_p)]),
+    "gst_pool_free": (None, [C.c_void_p]),
+    "gst_pool_num_replicas": (C.c_int32, [C.c_void_p]),
+    "gst_pool_solve_batch": (
+        C.c_int,
+        [C.c_void_p, C.c_int32, I32P, I32P, I32P, C.POINTER(Opts), C.POINTER(C.c_void_p)],
+    ),
+    "gst_result_replica": (C.c_int32, [C.c_void_p]),
     "gst_result_latency": (None, [C.c_void_p, F64P]),
     "gst_result_free": (None, [C.c_void_p]),
     "gst_result_status": (C.c_int, [C.c_void_p]),
@@ -187,6 +195,7 @@ class Result:
     times_ms: tuple = (0.0, 0.0, 0.0, 0.0)
     stats: dict = field(default_factory=dict)
     latency_ms: tuple = (0.0, 0.0)  # batch: own solve, completion since the batch began
+    replica: int = -1  # pool: replica that solved the query
     upper_bound: int = 0  # pruning bound at the last wave (0: unpruned)
     proposal_cost: int = 0  # learned path: cost of the proposed tree (0: none)
     proposal_ms: float = 0.0
@@ -227,6 +236,7 @@ def _read_result(r) -> Result:
         times_ms=tuple(t),
         stats=dict(zip(STAT_NAMES, list(s))),
         latency_ms=tuple(lat),
+        replica=int(L.gst_result_replica(r)),
         upper_bound=int(L.gst_result_upper_bound(r)),
         proposal_cost=int(L.gst_result_proposal_cost(r)),
         proposal_ms=float(L.gst_result_proposal_ms(r)),
@@ -385,6 +395,59 @@ class Graph:
         outs = (C.c_void_p * n)()
         o = make_opts(upper_bound, 0, use_graph, collect_stats, 0, refine_bound, concurrency)
         st = lib().gst_solve_batch(self._h, n, _ptr(ks_a), _ptr(gp_a), _ptr(mem_a), C.byref(o), outs)
+        msg = last_error()
+        res = []
+        for i in range(n):
+            if outs[i]:
+                res.append(_read_result(outs[i]))
+                lib().gst_result_free(outs[i])
+            else:
+                res.append(None)
+        if st not in (Status.OK, Status.INFEASIBLE):
+            raise GSTError(st, msg)
+        return res
+
+
+class Pool:
+    """Replicas of one graph on several devices (gst_pool); a device may repeat."""
+
+    def __init__(self, row_ptr, col, w, devices):
+        rp, c, ww = _i32(row_ptr), _i32(col), _i32(w)
+        dev = _i32(devices)
+        h = C.c_void_p()
+        st = lib().gst_pool_create(_ptr(rp), _ptr(c), _ptr(ww), len(rp) - 1, len(c), _ptr(dev), len(dev),
+                                   C.byref(h))
+        if st != Status.OK:
+            raise GSTError(st, last_error())
+        self._h = h
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().gst_pool_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def replicas(self) -> int:
+        return int(lib().gst_pool_num_replicas(self._h))
+
+    def solve_batch(self, queries, *, use_graph=True, refine_bound=False, concurrency=0) -> list[Result]:
+        ks_a, gp_a, mem_a = Graph._pack_batch(queries)
+        n = len(ks_a)
+        outs = (C.c_void_p * n)()
+        o = make_opts(0, 0, use_graph, False, 0, refine_bound, concurrency)
+        st = lib().gst_pool_solve_batch(self._h, n, _ptr(ks_a), _ptr(gp_a), _ptr(mem_a), C.byref(o), outs)
         msg = last_error()
         res = []
         for i in range(n):

@@ -136,12 +136,31 @@ gst_status gst_solve_batch(gst_graph *g, int32_t nq, const int32_t *ks, const in
 gst_status gst_autotune(gst_graph *g, int32_t nq, const int32_t *ks, const int32_t *group_ptr,
                         const int32_t *members, const gst_opts *opts, int32_t *lanes_out);
 
+/* ---------------------------------------------------------------- pool -- */
+
+/* Replicas of one graph on several devices (query-level scaling: a query's
+ * DP does not partition, independent queries do). gst_pool_solve_batch
+ * hands chunks of queries to one host thread per replica (work stealing);
+ * each replica runs them as gst_solve_batch does. A device may appear more
+ * than once (two replicas on one GPU). No counterpart in the reference. */
+typedef struct gst_pool gst_pool;
+gst_status gst_pool_create(const int32_t *row_ptr, const int32_t *col, const int32_t *w, int32_t V, int64_t nnz,
+                           const int32_t *devices, int32_t num_devices, gst_pool **out);
+void gst_pool_free(gst_pool *p);
+int32_t gst_pool_num_replicas(const gst_pool *p);
+/* As gst_solve_batch; out[q] also records which replica solved query q
+ * (gst_result_replica). */
+gst_status gst_pool_solve_batch(gst_pool *p, int32_t nq, const int32_t *ks, const int32_t *group_ptr,
+                                const int32_t *members, const gst_opts *opts, gst_result **out);
+
 /* --------------------------------------------------------------- result -- */
 
 void gst_result_free(gst_result *r);
 /* Batch results: ms2[0] = the query's own solve (host wall time),
  * ms2[1] = its completion since the batch began. */
 void gst_result_latency(const gst_result *r, double *ms2);
+/* Pool results: index of the replica that solved the query (-1 otherwise). */
+int32_t gst_result_replica(const gst_result *r);
 gst_status gst_result_status(const gst_result *r);
 /* Optimal cost (DPBF_GPU's *real_cost), -1 if infeasible. */
 int32_t gst_result_cost(const gst_result *r);

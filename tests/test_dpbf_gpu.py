@@ -280,3 +280,19 @@ def test_dataset_files_solve_like_the_reference_harness(tmp_path):
             gp, mem = native.query_groups(all_groups, ids)
             want = oracle.dpbf(h.row_ptr, h.col, h.w, gp, mem).cost
             _check(h.row_ptr, h.col, h.w, gp, mem, dg.solve(gp, mem, use_graph=True), want)
+
+
+def test_replica_pool_matches_single():
+    """gst_pool: replicas of the graph (here two on device 0; on a multi-GPU
+    node one per device) share a batch by work stealing; results equal the
+    single solves and both replicas take queries."""
+    g, qs = _ba_queries(20_000, 24, 41)
+    with native.Graph(g.row_ptr, g.col, g.w) as dg:
+        want = [dg.solve(gp, mem).cost for gp, mem in qs]
+    with native.Pool(g.row_ptr, g.col, g.w, [0, 0]) as pool:
+        assert pool.replicas == 2
+        got = pool.solve_batch(qs, refine_bound=True, concurrency=2)
+        assert [r.cost for r in got] == want
+        assert {r.replica for r in got} == {0, 1}
+        for (gp, mem), r in zip(qs, got):
+            _check(g.row_ptr, g.col, g.w, gp, mem, r, r.cost)
