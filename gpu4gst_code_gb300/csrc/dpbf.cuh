@@ -24,7 +24,7 @@ namespace gst {
 
 constexpr int32_t kInf = 0x3FFFFFFF;  // == GST_COST_LIMIT; finite costs stay below
 constexpr int32_t kLeaf = INT32_MIN;
-constexpr int kDegBig = 64;        // rows longer than this go to a CTA of their own
+constexpr int kDegBig = 32;  // longer rows are hubs: relaxed in 32-entry chunks by any warp
 constexpr int kGrowThreads = 256;  // block size of growth / merge kernels
 constexpr int kMaxThreadMasks = 24;  // waves with stride <= this: a thread per vertex
 // Sparse rounds scan candidate flags in tiles of this many consecutive

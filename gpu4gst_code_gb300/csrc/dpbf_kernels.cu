@@ -118,7 +118,11 @@ __global__ void __launch_bounds__(kGrowThreads) k_merge(GraphDev g, LevelArgs a)
     if (j < a.m) {
       const uint32_t S = (uint32_t)__ldg(a.lmasks + j);
       if ((__ldg(a.gmask + v) & S) == S) best = 0;
-      if (a.level >= 2 && best != 0) {
+      // under a bound, a state whose lower bound alone exceeds it is dead:
+      // no split needs enumerating
+      const int32_t cap = (ub > 0 && a.level >= 2) ? prune_cap(a, ub, v, S) : kInf;
+      if (cap < 0) best = kInf;
+      if (a.level >= 2 && best != 0 && cap >= 0) {
         const uint32_t low = S & (0u - S), rest = S ^ low;
         for (uint32_t sub = (rest - 1u) & rest;; sub = (sub - 1u) & rest) {
           const uint32_t s1 = sub | low, s2 = S ^ s1;
@@ -142,7 +146,7 @@ __global__ void __launch_bounds__(kGrowThreads) k_merge(GraphDev g, LevelArgs a)
           if (sub == 0u) break;
         }
       }
-      if (ub > 0 && best < kInf && a.level >= 2 && best > prune_cap(a, ub, v, S)) {
+      if (best < kInf && best > cap) {
         best = kInf;
         code = kLeaf;
       }

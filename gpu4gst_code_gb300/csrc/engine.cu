@@ -699,9 +699,21 @@ gst_status run_host_loop(gst_graph* g, int32_t k, int64_t* launches, bool* timeo
         }
         GST_CUDA(cudaMemcpyAsync(ws.h_ctl, ws.ctl, sizeof(GrowCtl), cudaMemcpyDeviceToHost, s));
         GST_CUDA(cudaStreamSynchronize(s));
-        if (trace)
-          std::fprintf(stderr, "gst-trace wave %d round %d changed %d  %.3f ms\n", l, ws.h_ctl->round - 1,
+        if (trace) {
+          std::fprintf(stderr, "gst-trace wave %d round %d changed %d  %.3f ms", l, ws.h_ctl->round - 1,
                        ws.h_ctl->last_changed, elapsed(ws.ev[kEvents - 2], ws.ev[kEvents - 1]));
+          if (ws.h_params->stats_on) {  // this round's share of the counters
+            static long long prev[kNumStats];
+            long long cur[kNumStats];
+            GST_CUDA(cudaMemcpy(cur, ws.stats, sizeof(cur), cudaMemcpyDeviceToHost));
+            if (ws.h_ctl->round == 1) std::fill(prev, prev + kNumStats, 0LL);
+            std::fprintf(stderr, "  vertices %lld entries %lld rows %lld improved %lld", cur[kStatVertices] - prev[kStatVertices],
+                         cur[kStatEntries] - prev[kStatEntries], cur[kStatRows] - prev[kStatRows],
+                         cur[kStatImproved] - prev[kStatImproved]);
+            std::copy(cur, cur + kNumStats, prev);
+          }
+          std::fprintf(stderr, "\n");
+        }
         if (ws.h_ctl->timeout) {
           *timeout = true;
           return GST_OK;
