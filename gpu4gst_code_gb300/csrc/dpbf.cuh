@@ -24,13 +24,17 @@ namespace gst {
 
 constexpr int32_t kInf = 0x3FFFFFFF;  // == GST_COST_LIMIT; finite costs stay below
 constexpr int32_t kLeaf = INT32_MIN;
-constexpr int kDegBig = 32;  // longer rows are hubs: relaxed in 32-entry chunks by any warp
+// Rows longer than GraphDev::deg_big entries are hubs, relaxed in 32-entry
+// chunks by any warp; deg_big = 4 x the average degree, clamped to
+// [kDegBigMin, kDegBigMax] (parent codes of other rows fit a byte).
+constexpr int kDegBigMin = 32;
+constexpr int kDegBigMax = 64;
 constexpr int kGrowThreads = 256;  // block size of growth / merge kernels
 constexpr int kMaxThreadMasks = 24;  // waves with stride <= this: a thread per vertex
 // Sparse rounds scan candidate flags in tiles of this many consecutive
 // vertex IDs (one warp each). The graph is relabelled at upload so that
 // every tile holds a mix of degrees (see gst_graph_upload).
-constexpr int kCandTile = 512;
+constexpr int kCandTile = 256;
 // Dense rounds when the previous round changed more than V >> this
 // (sparse rounds with marking stay cheaper up to about half the graph).
 constexpr int kDefaultDenseShift = 1;
@@ -103,7 +107,8 @@ struct GraphDev {
   int32_t V;
   const int32_t* row_ptr;  // V+1
   const int2* adj;         // (col, w) per CSR entry
-  const int32_t* big;      // vertices with degree > kDegBig
+  int32_t deg_big;         // hub threshold (see kDegBigMin)
+  const int32_t* big;      // vertices with degree > deg_big
   int32_t nbig;
   const int32_t* order;    // the other vertices by decreasing degree
   int32_t nsmall;          // V - nbig

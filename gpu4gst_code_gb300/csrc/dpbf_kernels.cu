@@ -190,7 +190,7 @@ __global__ void __launch_bounds__(kGrowThreads) k_merge(GraphDev g, LevelArgs a)
 //   k_grow_group<G,L>  wider waves: G lanes per vertex, lane j holding masks
 //                      j, j+G, ... (L per lane), neighbour rows gathered four
 //                      at a time;
-//   hubs (degree > kDegBig) in both: 32-entry chunks of hub rows taken by
+//   hubs (degree > g.deg_big) in both: 32-entry chunks of hub rows taken by
 //                      any warp, minima folded into a per-hub scratch row,
 //                      applied by the warp that finishes the hub's last chunk.
 // The last block to finish publishes the round's change count, advances
@@ -446,7 +446,7 @@ __device__ __forceinline__ void group_relax(const GraphDev& g, const LevelArgs& 
   }
 }
 
-// Hub rows (degree > kDegBig) are cut into 32-entry chunks that any warp
+// Hub rows (degree > g.deg_big) are cut into 32-entry chunks that any warp
 // may take. A warp relaxes its chunk for every mask (lane j holds masks
 // j, j+32, ...), folds each lane's minimum into the hub's scratch row with
 // a 64-bit atomicMin of (cost << 32 | CSR entry), and counts the chunk as
@@ -554,7 +554,7 @@ __device__ __forceinline__ void hub_mark(const GraphDev& g, const LevelArgs& a, 
 // (within their bound) become round 0's candidates. Hub rows are walked a
 // 32-entry chunk per warp; the other vertices 32 at a time per warp, which
 // finds those with a light state by ballot and walks each one's (at most
-// kDegBig) neighbours with its 32 lanes.
+// g.deg_big) neighbours with its 32 lanes.
 __global__ void __launch_bounds__(kGrowThreads) k_seed(GraphDev g, LevelArgs a) {
   GrowCtl* ctl = a.ctl;
   if (ctl->changed[2] > (g.V >> a.params->dense_shift)) {
@@ -589,7 +589,7 @@ __global__ void __launch_bounds__(kGrowThreads) k_seed(GraphDev g, LevelArgs a) 
   for (int64_t vbase = warp * 32; vbase < g.V; vbase += nwarps * 32) {
     const int64_t vl = vbase + lane;
     bool light = false;
-    if (vl < g.V && g.row_ptr[vl + 1] - g.row_ptr[vl] <= kDegBig) {
+    if (vl < g.V && g.row_ptr[vl + 1] - g.row_ptr[vl] <= g.deg_big) {
       const int32_t* hv = a.cost + a.base + vl * s;
       for (int j = 0; j < a.m; ++j) light |= light_or_inf(hv[j], ub_light) < kInf;
     }
@@ -626,11 +626,11 @@ __device__ __forceinline__ void thread_vertex(const GraphDev& g, const LevelArgs
   constexpr int U = MP <= 8 ? 4 : 2;
   constexpr int Q = MP / 4;
   const int32_t beg = g.row_ptr[u], end = g.row_ptr[u + 1];
-  if (end - beg > kDegBig) return;  // hub: handled in 32-entry chunks
+  if (end - beg > g.deg_big) return;  // hub: handled in 32-entry chunks
   int4* rowc = reinterpret_cast<int4*>(a.cost + a.base + (int64_t)u * MP);
   int32_t best[MP];
   // parent of entry j as (CSR entry - beg), one byte each (rows are at most
-  // kDegBig long); 0xff = unchanged
+  // kDegBigMax long); 0xff = unchanged
   uint32_t code[Q];
 #pragma unroll
   for (int q = 0; q < Q; ++q) {
@@ -805,21 +805,21 @@ __global__ void __launch_bounds__(kGrowThreads, (MP <= 16 ? 3 : 2)) k_grow_threa
     for (int64_t i = t0; i < g.nsmall; i += nthreads)
       thread_vertex<MP>(g, a, rs, g.order[(rs.r & 1) ? g.nsmall - 1 - i : i], acc);
   } else {
-    // candidates only: a warp reads 512 candidate bytes at a time (16 per
-    // lane, one int4), compacts the set ones in shared memory and its lanes
-    // take them in turn
+    // candidates only: a warp reads kCandTile candidate bytes at a time (8
+    // per lane), compacts the set ones in shared memory and its lanes take
+    // them in turn
     __shared__ int32_t tile[kGrowThreads / 32][kCandTile];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int64_t warp = t0 >> 5, nwarps = nthreads >> 5;
-    static_assert(kCandTile == 16 * 32, "a lane reads 16 flag bytes");
+    static_assert(kCandTile == 8 * 32, "a lane reads 8 flag bytes");
     for (int64_t base = warp * kCandTile; base < g.V; base += nwarps * kCandTile) {
-      const int64_t v0 = base + 16 * lane;
-      uint4 f = make_uint4(0, 0, 0, 0);
-      if (v0 < g.V) f = *reinterpret_cast<const uint4*>(rs.cand_cur + v0);  // arrays padded to 16 bytes
-      const uint32_t w4[4] = {f.x, f.y, f.z, f.w};
+      const int64_t v0 = base + 8 * lane;
+      uint2 f = make_uint2(0u, 0u);
+      if (v0 < g.V) f = *reinterpret_cast<const uint2*>(rs.cand_cur + v0);  // arrays padded to 16 bytes
+      const uint32_t w2[2] = {f.x, f.y};
       int cnt = 0;
 #pragma unroll
-      for (int b = 0; b < 16; ++b) cnt += ((w4[b >> 2] >> (8 * (b & 3))) & 0xffu) != 0;
+      for (int b = 0; b < 8; ++b) cnt += ((w2[b >> 2] >> (8 * (b & 3))) & 0xffu) != 0;
       int pre = cnt;  // inclusive prefix over lanes
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
@@ -829,8 +829,8 @@ __global__ void __launch_bounds__(kGrowThreads, (MP <= 16 ? 3 : 2)) k_grow_threa
       const int total = __shfl_sync(0xffffffffu, pre, 31);
       int pos = pre - cnt;
 #pragma unroll
-      for (int b = 0; b < 16; ++b)
-        if (((w4[b >> 2] >> (8 * (b & 3))) & 0xffu) != 0) tile[wib][pos++] = (int32_t)(v0 + b);
+      for (int b = 0; b < 8; ++b)
+        if (((w2[b >> 2] >> (8 * (b & 3))) & 0xffu) != 0) tile[wib][pos++] = (int32_t)(v0 + b);
       __syncwarp();
       for (int i = lane; i < total; i += 32) thread_vertex<MP>(g, a, rs, tile[wib][i], acc);
       __syncwarp();
@@ -881,7 +881,7 @@ __global__ void __launch_bounds__(kGrowThreads, (L >= 3 ? 3 : 4)) k_grow_group(G
         const int32_t u = (int32_t)(vbase + __ffs(cm) - 1);
         for (int i = 0; i < NGW && cm; ++i) cm &= cm - 1u;
         const int32_t beg = g.row_ptr[u], end = g.row_ptr[u + 1];
-        if (end - beg > kDegBig) continue;  // handled in 32-entry chunks
+        if (end - beg > g.deg_big) continue;  // handled in 32-entry chunks
         const int64_t rowu = a.base + (int64_t)u * s;
         bool imp_any = false;
         for (int jc = 0; jc < s; jc += CH) {

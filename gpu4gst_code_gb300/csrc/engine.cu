@@ -178,7 +178,8 @@ struct gst_graph {
   int2* d_adj = nullptr;
   int32_t* d_big = nullptr;
   int32_t nbig = 0;
-  int32_t* d_order = nullptr;  // vertices of degree <= kDegBig, by decreasing degree
+  int32_t deg_big = kDegBigMin;  // hub threshold of this graph
+  int32_t* d_order = nullptr;  // vertices of degree <= deg_big, by decreasing degree
   int2* d_hub_chunk = nullptr;  // (hub index, first CSR entry) per 32-entry chunk of a hub row
   int64_t nchunks = 0;
   int32_t max_w = 0;  // largest edge weight
@@ -237,6 +238,7 @@ GraphDev graph_dev(const gst_graph* g) {
   d.row_ptr = g->d_row_ptr;
   d.adj = g->d_adj;
   d.big = g->d_big;
+  d.deg_big = g->deg_big;
   d.nbig = g->nbig;
   d.order = g->d_order;
   d.nsmall = g->V - g->nbig;
@@ -1242,6 +1244,7 @@ gst_status ensure_lanes(gst_graph* g, int32_t n) {
     l->d_row_ptr = g->d_row_ptr;
     l->d_adj = g->d_adj;
     l->d_big = g->d_big;
+    l->deg_big = g->deg_big;
     l->nbig = g->nbig;
     l->d_order = g->d_order;
     l->d_hub_chunk = g->d_hub_chunk;
@@ -1338,7 +1341,8 @@ gst_status gst_graph_upload(const int32_t* row_ptr, const int32_t* col, const in
   // windows of kOrderWindow consecutive IDs, so the 32 lanes of a warp walk
   // rows of similar length while a window's rows stay close in memory.
   std::vector<int32_t> big, order;
-  for (int32_t v = 0; v < V; ++v) (row_ptr[v + 1] - row_ptr[v] > kDegBig ? big : order).push_back(v);
+  g->deg_big = (int32_t)std::min<int64_t>(kDegBigMax, std::max<int64_t>(kDegBigMin, (4 * nnz + V - 1) / V));
+  for (int32_t v = 0; v < V; ++v) (row_ptr[v + 1] - row_ptr[v] > g->deg_big ? big : order).push_back(v);
   constexpr size_t kOrderWindow = 1024;
   for (size_t w0 = 0; w0 < order.size(); w0 += kOrderWindow) {
     const size_t w1 = std::min(order.size(), w0 + kOrderWindow);
