@@ -82,8 +82,8 @@ int binom(int n, int r) {
 constexpr int32_t kTreePrefix = 4096;   // tree entries read back with the counters
 constexpr int kPollEvery = 8;           // host loop: rounds launched between polls
 constexpr int kEvents = 3 * GST_MAX_K + 8;
-constexpr int kProposeTop = 256;       // top-scored vertices offered to the proposal's repair
-constexpr int kProposeRounds = 12;     // growth rounds of the proposal's root distances
+constexpr int kProposeTop = 64;        // top-scored vertices offered to the proposal's repair
+constexpr int kProposeRounds = 8;      // growth rounds of the proposal's root distances
 constexpr int32_t kDefaultLanes = 4;   // concurrent solve contexts of a batch
 constexpr int32_t kMaxLanes = 8;
 }  // namespace
@@ -141,7 +141,7 @@ struct LearnWs {
   uint32_t* r3 = nullptr;
   int32_t* mnb = nullptr;
   float* x = nullptr;                 // V x kFeat
-  __nv_bfloat16* hb[2] = {nullptr, nullptr};  // V x kHid each
+  __nv_bfloat16* hb[3] = {nullptr, nullptr, nullptr};  // V x kHid each: two activations, the neighbour mean
   float* hub_sum = nullptr;           // nbig x kHid
   float* scores = nullptr;            // V
   unsigned long long* best = nullptr;
@@ -266,6 +266,7 @@ void free_learn(LearnWs& lw) {
   dfree(lw.x);
   dfree(lw.hb[0]);
   dfree(lw.hb[1]);
+  dfree(lw.hb[2]);
   dfree(lw.hub_sum);
   dfree(lw.scores);
   dfree(lw.best);
@@ -940,6 +941,7 @@ gst_status ensure_learn_infer(gst_graph* g) {
   GST_CUDA(cudaMalloc(&lw.x, V * kFeat * sizeof(float)));
   GST_CUDA(cudaMalloc(&lw.hb[0], V * kHid * sizeof(__nv_bfloat16)));
   GST_CUDA(cudaMalloc(&lw.hb[1], V * kHid * sizeof(__nv_bfloat16)));
+  GST_CUDA(cudaMalloc(&lw.hb[2], V * kHid * sizeof(__nv_bfloat16)));
   GST_CUDA(cudaMalloc(&lw.hub_sum, std::max<size_t>(1, (size_t)g->nbig) * kHid * sizeof(float)));
   GST_CUDA(cudaMalloc(&lw.scores, V * sizeof(float)));
   GST_CUDA(cudaMalloc(&lw.best, sizeof(unsigned long long)));
@@ -1018,8 +1020,9 @@ gst_status infer_scores(gst_graph* g, const gst_scorer* sc) {
       GST_CUDA(launch_hub_sum_bf16(gd, hin, lw.hub_sum, s));
     }
     const bool last = l == kMpLayers;
-    GST_CUDA(launch_infer_layer(gd, g->d_hub_of, lw.hub_sum, hin, sc->wcat + (size_t)(l - 1) * kHid * 2 * kHid,
-                                sc->params, l, last ? nullptr : lw.hb[l & 1], last ? lw.scores : nullptr, s));
+    GST_CUDA(launch_infer_layer(gd, g->d_hub_of, lw.hub_sum, hin, lw.hb[2],
+                                sc->wcat + (size_t)(l - 1) * kHid * 2 * kHid, sc->params, l,
+                                last ? nullptr : lw.hb[l & 1], last ? lw.scores : nullptr, s));
   }
   return GST_OK;
 }
@@ -1095,7 +1098,7 @@ gst_status propose_tree(gst_graph* g, const gst_scorer* sc, const int32_t* group
   if (sc) {
     st = infer_scores(g, sc);
     if (st != GST_OK) return st;
-    launches += 1 + kMpLayers * (g->nbig > 0 ? 2 : 1);
+    launches += 1 + kMpLayers * (g->nbig > 0 ? 3 : 2);
   } else {
     GST_CUDA(launch_feature_score(g->V, lw.x, lw.scores, s));
     launches += 1;

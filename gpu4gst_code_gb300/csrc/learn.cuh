@@ -53,11 +53,12 @@ cudaError_t launch_infer_l0(int32_t V, const float* x, const float* params, __nv
 // Hub rows' neighbour sums for one layer, fp32, one 32-entry chunk per warp
 // (hub_sum[nbig][kHid], zeroed by the caller).
 cudaError_t launch_hub_sum_bf16(const GraphDev& g, const __nv_bfloat16* hin, float* hub_sum, cudaStream_t s);
-// One message-passing layer (l = 1..3). On the last layer, with scores
-// non-null, writes scores instead of activations.
+// One message-passing layer (l = 1..3): the neighbour mean into agg
+// (V x kHid bf16 scratch), then the tensor-core layer over [h | agg]. On the
+// last layer, with scores non-null, writes scores instead of activations.
 cudaError_t launch_infer_layer(const GraphDev& g, const int32_t* hub_of, const float* hub_sum,
-                               const __nv_bfloat16* hin, const __nv_bfloat16* wcat_l, const float* params, int l,
-                               __nv_bfloat16* hout, float* scores, cudaStream_t s);
+                               const __nv_bfloat16* hin, __nv_bfloat16* agg, const __nv_bfloat16* wcat_l,
+                               const float* params, int l, __nv_bfloat16* hout, float* scores, cudaStream_t s);
 // The proposal's root without a network: most groups within 1 hop, then 2,
 // then 3, then degree (s = 1000 x3 + 100 x4 + 10 x5 + x1).
 cudaError_t launch_feature_score(int32_t V, const float* x, float* s, cudaStream_t st);

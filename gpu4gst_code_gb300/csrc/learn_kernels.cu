@@ -89,6 +89,21 @@ __global__ void k_features(GraphDev g, const uint32_t* __restrict__ m0, const ui
 }
 
 // ------------------------------------------------------------- inference --
+__device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
+  const __nv_bfloat162 b = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<const uint32_t*>(&b);
+}
+
+__device__ __forceinline__ void add_bf16x8(float (&a)[8], const uint4 x) {
+  const uint32_t w[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const float2 f = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&w[q]));
+    a[2 * q] += f.x;
+    a[2 * q + 1] += f.y;
+  }
+}
+
 __global__ void k_pack_bf16(const float* __restrict__ p, __nv_bfloat16* __restrict__ wcat) {
   const int64_t n = (int64_t)kMpLayers * kHid * 2 * kHid;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -101,21 +116,78 @@ __global__ void k_pack_bf16(const float* __restrict__ p, __nv_bfloat16* __restri
   }
 }
 
-// block: 4 vertices x 64 outputs
+// Thread per vertex: all 64 outputs of h0 = relu(W0 x + b0) from W0 in
+// shared memory (broadcast reads), the 16 features in registers, the row
+// written as eight 16-byte stores.
 __global__ void __launch_bounds__(256) k_infer_l0(int32_t V, const float* __restrict__ x, const float* __restrict__ p,
                                                   __nv_bfloat16* __restrict__ h) {
-  __shared__ float sw[kHid][kFeat + 1];
+  __shared__ float sw[kHid][kFeat];
   __shared__ float sb[kHid];
   for (int i = threadIdx.x; i < kHid * kFeat; i += blockDim.x) sw[i / kFeat][i % kFeat] = p[kOffW0 + i];
   if (threadIdx.x < kHid) sb[threadIdx.x] = p[kOffB0 + threadIdx.x];
   __syncthreads();
-  const int o = threadIdx.x & (kHid - 1), vi = threadIdx.x >> 6;
-  for (int64_t v = (int64_t)blockIdx.x * 4 + vi; v < V; v += (int64_t)gridDim.x * 4) {
-    const float* xv = x + v * kFeat;
-    float acc = sb[o];
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < V; v += (int64_t)gridDim.x * blockDim.x) {
+    float f[kFeat];
+    const float4* xv = reinterpret_cast<const float4*>(x + v * kFeat);
 #pragma unroll
-    for (int c = 0; c < kFeat; ++c) acc = fmaf(sw[o][c], xv[c], acc);
-    h[v * kHid + o] = __float2bfloat16_rn(fmaxf(acc, 0.0f));
+    for (int q = 0; q < kFeat / 4; ++q) {
+      const float4 t = xv[q];
+      f[4 * q] = t.x;
+      f[4 * q + 1] = t.y;
+      f[4 * q + 2] = t.z;
+      f[4 * q + 3] = t.w;
+    }
+    uint4* out = reinterpret_cast<uint4*>(h + v * kHid);
+#pragma unroll 1
+    for (int o8 = 0; o8 < kHid / 8; ++o8) {
+      float y[8];
+#pragma unroll
+      for (int t = 0; t < 8; ++t) {
+        float acc = sb[o8 * 8 + t];
+#pragma unroll
+        for (int c = 0; c < kFeat; ++c) acc = fmaf(sw[o8 * 8 + t][c], f[c], acc);
+        y[t] = fmaxf(acc, 0.0f);
+      }
+      out[o8] = make_uint4(pack_bf16x2(y[0], y[1]), pack_bf16x2(y[2], y[3]), pack_bf16x2(y[4], y[5]),
+                           pack_bf16x2(y[6], y[7]));
+    }
+  }
+}
+
+// The neighbour mean of one layer's input, bf16 in and out: eight threads
+// per vertex, 16 bytes (8 channels) each, fp32 accumulation; hub rows take
+// their sums from hub_sum. No shared memory, so many warps are resident to
+// cover the gathers' latency.
+__global__ void __launch_bounds__(256) k_mean_bf16(GraphDev g, const int32_t* __restrict__ hub_of,
+                                                   const float* __restrict__ hub_sum,
+                                                   const __nv_bfloat16* __restrict__ hin,
+                                                   __nv_bfloat16* __restrict__ agg) {
+  const int sl = threadIdx.x & 7;
+  for (int64_t v = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 3; v < g.V;
+       v += ((int64_t)gridDim.x * blockDim.x) >> 3) {
+    const int32_t beg = g.row_ptr[v], end = g.row_ptr[v + 1];
+    const float inv = end > beg ? 1.0f / (float)(end - beg) : 0.0f;
+    float a[8] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    const int32_t hb = hub_of[v];
+    if (hb >= 0) {
+      const float4* hs = reinterpret_cast<const float4*>(hub_sum + (int64_t)hb * kHid + 8 * sl);
+      const float4 p0 = hs[0], p1 = hs[1];
+      a[0] = p0.x; a[1] = p0.y; a[2] = p0.z; a[3] = p0.w;
+      a[4] = p1.x; a[5] = p1.y; a[6] = p1.z; a[7] = p1.w;
+    } else {
+      int32_t e = beg;
+      for (; e + 4 <= end; e += 4) {
+        uint4 r[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) r[j] = reinterpret_cast<const uint4*>(hin + (int64_t)g.adj[e + j].x * kHid)[sl];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) add_bf16x8(a, r[j]);
+      }
+      for (; e < end; ++e) add_bf16x8(a, reinterpret_cast<const uint4*>(hin + (int64_t)g.adj[e].x * kHid)[sl]);
+    }
+    reinterpret_cast<uint4*>(agg + v * kHid)[sl] =
+        make_uint4(pack_bf16x2(a[0] * inv, a[1] * inv), pack_bf16x2(a[2] * inv, a[3] * inv),
+                   pack_bf16x2(a[4] * inv, a[5] * inv), pack_bf16x2(a[6] * inv, a[7] * inv));
   }
 }
 
@@ -137,20 +209,7 @@ __global__ void k_hub_sum_bf16(GraphDev g, const __nv_bfloat16* __restrict__ hin
   }
 }
 
-__device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
-  const __nv_bfloat162 b = __floats2bfloat162_rn(lo, hi);
-  return *reinterpret_cast<const uint32_t*>(&b);
-}
 
-__device__ __forceinline__ void add_bf16x8(float (&a)[8], const uint4 x) {
-  const uint32_t w[4] = {x.x, x.y, x.z, x.w};
-#pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    const float2 f = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&w[q]));
-    a[2 * q] += f.x;
-    a[2 * q + 1] += f.y;
-  }
-}
 
 // D += A * B for one m16n8k16 tile (bf16 in, fp32 accumulate)
 __device__ __forceinline__ void mma_bf16(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
@@ -170,8 +229,7 @@ constexpr int kRowPad = 2 * kHid + 8;  // bf16 per shared row: 68 words, so frag
 // multiplies it by [Ws | Wn]^T (128 x 64) with 8 x 8 mma tiles, adds the
 // bias, applies the ReLU and stores bf16 activations, or on the last
 // layer reduces them against wo into scores.
-__global__ void __launch_bounds__(kInfWarps * 32) k_infer_layer(GraphDev g, const int32_t* __restrict__ hub_of,
-                                                                const float* __restrict__ hub_sum,
+__global__ void __launch_bounds__(kInfWarps * 32) k_infer_layer(GraphDev g, const __nv_bfloat16* __restrict__ agg,
                                                                 const __nv_bfloat16* __restrict__ hin,
                                                                 const __nv_bfloat16* __restrict__ wcat,
                                                                 const float* __restrict__ bias,
@@ -196,35 +254,17 @@ __global__ void __launch_bounds__(kInfWarps * 32) k_infer_layer(GraphDev g, cons
   const int gq = lane >> 2, tq = lane & 3;
   const int64_t ntiles = ((int64_t)g.V + 15) / 16;
   for (int64_t tile = (int64_t)blockIdx.x * kInfWarps + w; tile < ntiles; tile += (int64_t)gridDim.x * kInfWarps) {
-    // stage A: a quarter warp per vertex, 8 channels (16 bytes) per lane
+    // stage A = [h | mean]: both rows streamed (the mean comes from
+    // k_mean_bf16), a quarter warp per vertex, 16 bytes per lane
     const int sub = lane >> 3, sl = lane & 7;
+#pragma unroll
     for (int i0 = 0; i0 < 16; i0 += 4) {
       const int i = i0 + sub;
       const int64_t v = tile * 16 + i;
       uint4 hv = make_uint4(0, 0, 0, 0), av = make_uint4(0, 0, 0, 0);
       if (v < g.V) {
         hv = reinterpret_cast<const uint4*>(hin + v * kHid)[sl];
-        const int32_t beg = g.row_ptr[v], end = g.row_ptr[v + 1];
-        const float inv = end > beg ? 1.0f / (float)(end - beg) : 0.0f;
-        float a[8] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
-        const int32_t hb = hub_of[v];
-        if (hb >= 0) {
-          const float4* hs = reinterpret_cast<const float4*>(hub_sum + (int64_t)hb * kHid + 8 * sl);
-          const float4 p0 = hs[0], p1 = hs[1];
-          a[0] = p0.x; a[1] = p0.y; a[2] = p0.z; a[3] = p0.w;
-          a[4] = p1.x; a[5] = p1.y; a[6] = p1.z; a[7] = p1.w;
-        } else {
-          int32_t e = beg;
-          for (; e + 2 <= end; e += 2) {
-            const uint4 x0 = reinterpret_cast<const uint4*>(hin + (int64_t)g.adj[e].x * kHid)[sl];
-            const uint4 x1 = reinterpret_cast<const uint4*>(hin + (int64_t)g.adj[e + 1].x * kHid)[sl];
-            add_bf16x8(a, x0);
-            add_bf16x8(a, x1);
-          }
-          if (e < end) add_bf16x8(a, reinterpret_cast<const uint4*>(hin + (int64_t)g.adj[e].x * kHid)[sl]);
-        }
-        av = make_uint4(pack_bf16x2(a[0] * inv, a[1] * inv), pack_bf16x2(a[2] * inv, a[3] * inv),
-                        pack_bf16x2(a[4] * inv, a[5] * inv), pack_bf16x2(a[6] * inv, a[7] * inv));
+        av = reinterpret_cast<const uint4*>(agg + v * kHid)[sl];
       }
       reinterpret_cast<uint4*>(&sA[w][i][0])[sl] = hv;
       reinterpret_cast<uint4*>(&sA[w][i][kHid])[sl] = av;
@@ -619,7 +659,7 @@ cudaError_t launch_pack_bf16(const float* params, __nv_bfloat16* wcat, cudaStrea
 }
 
 cudaError_t launch_infer_l0(int32_t V, const float* x, const float* params, __nv_bfloat16* h0, cudaStream_t s) {
-  k_infer_l0<<<grid_for(V, 4), 256, 0, s>>>(V, x, params, h0);
+  k_infer_l0<<<grid_for(V, 256), 256, 0, s>>>(V, x, params, h0);
   return cudaGetLastError();
 }
 
@@ -630,14 +670,15 @@ cudaError_t launch_hub_sum_bf16(const GraphDev& g, const __nv_bfloat16* hin, flo
 }
 
 cudaError_t launch_infer_layer(const GraphDev& g, const int32_t* hub_of, const float* hub_sum,
-                               const __nv_bfloat16* hin, const __nv_bfloat16* wcat_l, const float* params, int l,
-                               __nv_bfloat16* hout, float* scores, cudaStream_t s) {
+                               const __nv_bfloat16* hin, __nv_bfloat16* agg, const __nv_bfloat16* wcat_l,
+                               const float* params, int l, __nv_bfloat16* hout, float* scores, cudaStream_t s) {
   const float* bias = params + layer_off(l) + 2 * kHid * kHid;
   const float* wo = scores ? params + kOffWo : nullptr;
   const float* bo = scores ? params + kOffBo : nullptr;
+  k_mean_bf16<<<grid_for((int64_t)g.V * 8, 256, 152 * 32), 256, 0, s>>>(g, hub_of, hub_sum, hin, agg);
   const int64_t tiles = ((int64_t)g.V + 15) / 16;
-  k_infer_layer<<<grid_for(tiles, kInfWarps, 152 * 12), kInfWarps * 32, 0, s>>>(g, hub_of, hub_sum, hin, wcat_l,
-                                                                                bias, wo, bo, hout, scores);
+  k_infer_layer<<<grid_for(tiles, kInfWarps, 152 * 12), kInfWarps * 32, 0, s>>>(g, agg, hin, wcat_l, bias, wo, bo,
+                                                                                hout, scores);
   return cudaGetLastError();
 }
 
