@@ -83,7 +83,7 @@ constexpr int32_t kTreePrefix = 4096;   // tree entries read back with the count
 constexpr int kPollEvery = 8;           // host loop: rounds launched between polls
 constexpr int kEvents = 3 * GST_MAX_K + 8;
 constexpr int kProposeTop = 64;        // top-scored vertices offered to the proposal's repair
-constexpr int kProposeRounds = 6;      // growth rounds of the proposal's root distances
+constexpr int kProposeRounds = 8;      // growth rounds of the proposal's root distances
 constexpr int32_t kDefaultLanes = 4;   // concurrent solve contexts of a batch
 constexpr int32_t kMaxLanes = 8;
 }  // namespace
