@@ -135,15 +135,34 @@ struct LevelArgs {
   Counters* ctr;
   long long* stats;
   const SolveParams* params;
+  // merge split table of this level (k <= kMergeTabK): for mask rank j,
+  // splits [msplit_ptr[j], msplit_ptr[j+1]) of msplits, each
+  // ((level1 << 24) | rank1, (level2 << 24) | rank2) with S1 holding S's
+  // lowest group
+  const int32_t* msplit_ptr;
+  const int2* msplits;
+  int32_t nsplits;
   cudaGraphConditionalHandle cond;  // while-loop handle when captured
   int32_t use_cond;
+};
+
+// Queries with at most kMergeTabK groups merge a vertex per thread from
+// per-level split tables (k_merge_vertex); larger k use k_merge.
+constexpr int kMergeTabK = 10;
+
+// Where each level's rows live, for k_merge_vertex.
+struct MergeLevels {
+  int64_t off[kMergeTabK + 1];     // base_l * V
+  int32_t stride[kMergeTabK + 1];  // row stride of level l
+  int32_t mbase[kMergeTabK + 1];   // base_l: level l's masks start at lmasks_all[mbase[l]]
+  const int32_t* lmasks_all;
 };
 
 // Launchers (dpbf_kernels.cu). All asynchronous on `stream`.
 // members are caller IDs; perm maps them to internal IDs
 cudaError_t launch_group_masks(const int32_t* group_ptr, const int32_t* members, const int32_t* perm, int32_t k,
                                uint32_t* gmask, cudaStream_t stream);
-cudaError_t launch_merge(const GraphDev& g, const LevelArgs& a, cudaStream_t stream);
+cudaError_t launch_merge(const GraphDev& g, const LevelArgs& a, const MergeLevels& ml, cudaStream_t stream);
 // One growth round: a hub-relaxation kernel (when the graph has hubs) and
 // the round kernel proper. Adds the kernels launched to *launches.
 cudaError_t launch_grow_round(const GraphDev& g, const LevelArgs& a, int num_sms, cudaStream_t stream,

@@ -95,6 +95,31 @@ __global__ void k_group_masks(const int32_t* __restrict__ group_ptr, const int32
   }
 }
 
+// One-label bound of vertex v, loaded once: dd[g] = min(T(v,{g}), ub/2+1)
+// for the k groups, 0 for absent groups (wave 1 is not written while waves
+// >= 2 grow). Rows of wave 1 are 16-byte aligned.
+__device__ __forceinline__ void load_label_bound(const LevelArgs& a, int32_t ub, int32_t v, int32_t (&dd)[16]) {
+  const int4* d4 = reinterpret_cast<const int4*>(a.cost + (int64_t)v * a.stride1);
+  const int32_t beyond = ub / 2 + 1;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    int4 t = make_int4(0, 0, 0, 0);
+    if (4 * q < a.k) t = __ldg(d4 + q);
+    dd[4 * q] = 4 * q < a.k ? min(t.x, beyond) : 0;
+    dd[4 * q + 1] = 4 * q + 1 < a.k ? min(t.y, beyond) : 0;
+    dd[4 * q + 2] = 4 * q + 2 < a.k ? min(t.z, beyond) : 0;
+    dd[4 * q + 3] = 4 * q + 3 < a.k ? min(t.w, beyond) : 0;
+  }
+}
+
+// max over groups outside S of dd (the bound on completing S to the full set)
+__device__ __forceinline__ int32_t label_bound(const int32_t (&dd)[16], uint32_t S) {
+  int32_t lb = 0;
+#pragma unroll
+  for (int gg = 0; gg < 16; ++gg) lb = max(lb, ((S >> gg) & 1u) ? 0 : dd[gg]);
+  return lb;
+}
+
 // ------------------------------------------------------------------ merge --
 // One thread per (v, slot) of the level's rows: T(v,S) = 0 when S is inside
 // groups(v), else the best split T(v,S1) + T(v,S^S1) over S1 holding the
@@ -157,6 +182,97 @@ __global__ void __launch_bounds__(kGrowThreads) k_merge(GraphDev g, LevelArgs a)
       flag2[v] = 1;
       ++acc[0];
     }
+  }
+  block_sum(acc);
+  if (threadIdx.x == 0) {
+    if (acc[0]) {
+      atomicAdd(&a.ctl->changed[2], (int32_t)acc[0]);
+      atomicAdd(&a.ctr->states, (unsigned long long)acc[0]);
+    }
+    if (a.params->stats_on) add_stat(a.stats, kStatSplits, acc[1]);
+    if (acc[2]) atomicExch(&a.ctr->overflow, 1);
+  }
+}
+
+// One thread per vertex (k <= kMergeTabK): the same states as k_merge, row
+// by row. The level's split table sits in shared memory, so a split costs
+// its two row loads; the vertex's group mask and one-label bound are
+// loaded once; the row is written 16 bytes at a time.
+__global__ void __launch_bounds__(kGrowThreads) k_merge_vertex(GraphDev g, LevelArgs a, MergeLevels ml) {
+  extern __shared__ int32_t msm[];
+  int32_t* sp = msm;                                                // m + 1
+  int2* ss = reinterpret_cast<int2*>(msm + ((a.m + 2) & ~1));      // nsplits (8-byte aligned)
+  for (int i = threadIdx.x; i <= a.m; i += blockDim.x) sp[i] = a.msplit_ptr[i];
+  for (int i = threadIdx.x; i < a.nsplits; i += blockDim.x) ss[i] = a.msplits[i];
+  __syncthreads();
+  const int32_t ub = (a.level >= 2) ? a.params->ub : 0;
+  const int32_t ub_light = a.params->ub;
+  const int32_t ovf_limit = a.params->ovf_limit;
+  const bool light_parts = a.level < a.k;
+  uint8_t* flag2 = a.flags + 2 * (int64_t)a.vpad;
+  long long acc[3] = {0, 0, 0};  // finite states, splits, overflow
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < g.V; v += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t gm = __ldg(a.gmask + v);
+    int32_t dd[16];
+    if (ub > 0) load_label_bound(a, ub, (int32_t)v, dd);
+    int4* rowc = reinterpret_cast<int4*>(a.cost + a.base + v * a.stride);
+    int4* rowp = reinterpret_cast<int4*>(a.par + a.base + v * a.stride);
+    bool any = false;
+    for (int j0 = 0; j0 < a.stride; j0 += 4) {
+      int32_t b4[4], c4[4];
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        const int j = j0 + t;
+        int32_t best = kInf, code = kLeaf;
+        if (j < a.m) {
+          const uint32_t S = (uint32_t)__ldg(a.lmasks + j);
+          if ((gm & S) == S) best = 0;
+          const int32_t cap = ub > 0 ? ub - label_bound(dd, S) : kInf;
+          if (cap < 0) {
+            best = kInf;
+          } else if (best != 0) {
+            int win = -1;
+            for (int i = sp[j]; i < sp[j + 1]; ++i) {
+              const int2 x = ss[i];
+              const int l1 = x.x >> 24, l2 = x.y >> 24;
+              int32_t c1 = a.cost[ml.off[l1] + v * ml.stride[l1] + (x.x & 0xffffff)];
+              int32_t c2 = a.cost[ml.off[l2] + v * ml.stride[l2] + (x.y & 0xffffff)];
+              if (light_parts) {
+                c1 = light_or_inf(c1, ub_light);
+                c2 = light_or_inf(c2, ub_light);
+              }
+              if (c1 < kInf && c2 < kInf) {
+                const int32_t c = c1 + c2;  // both < 2^30: no wrap
+                if (c >= ovf_limit)
+                  acc[2] = 1;
+                else if (c < best) {
+                  best = c;
+                  win = i;
+                }
+              }
+            }
+            acc[1] += sp[j + 1] - sp[j];
+            if (win >= 0) {
+              const int2 x = ss[win];
+              code = -__ldg(ml.lmasks_all + ml.mbase[x.x >> 24] + (x.x & 0xffffff));
+            }
+          }
+          if (best < kInf && best > cap) {
+            best = kInf;
+            code = kLeaf;
+          }
+        }
+        b4[t] = best;
+        c4[t] = code;
+        if (best < kInf) {
+          any = true;
+          ++acc[0];
+        }
+      }
+      rowc[j0 >> 2] = make_int4(b4[0], b4[1], b4[2], b4[3]);
+      rowp[j0 >> 2] = make_int4(c4[0], c4[1], c4[2], c4[3]);
+    }
+    if (any) flag2[v] = 1;
   }
   block_sum(acc);
   if (threadIdx.x == 0) {
@@ -245,31 +361,6 @@ __device__ __forceinline__ bool round_begin(const GraphDev& g, const LevelArgs& 
 __device__ __forceinline__ void mark_candidate(uint8_t* cand, int32_t v, uint32_t (&acc)[kAccN]) {
   cand[v] = 1;
   ++acc[kAccMarks];
-}
-
-// One-label bound of vertex v, loaded once: dd[g] = min(T(v,{g}), ub/2+1)
-// for the k groups, 0 for absent groups (wave 1 is not written while waves
-// >= 2 grow). Rows of wave 1 are 16-byte aligned.
-__device__ __forceinline__ void load_label_bound(const LevelArgs& a, int32_t ub, int32_t v, int32_t (&dd)[16]) {
-  const int4* d4 = reinterpret_cast<const int4*>(a.cost + (int64_t)v * a.stride1);
-  const int32_t beyond = ub / 2 + 1;
-#pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    int4 t = make_int4(0, 0, 0, 0);
-    if (4 * q < a.k) t = __ldg(d4 + q);
-    dd[4 * q] = 4 * q < a.k ? min(t.x, beyond) : 0;
-    dd[4 * q + 1] = 4 * q + 1 < a.k ? min(t.y, beyond) : 0;
-    dd[4 * q + 2] = 4 * q + 2 < a.k ? min(t.z, beyond) : 0;
-    dd[4 * q + 3] = 4 * q + 3 < a.k ? min(t.w, beyond) : 0;
-  }
-}
-
-// max over groups outside S of dd (the bound on completing S to the full set)
-__device__ __forceinline__ int32_t label_bound(const int32_t (&dd)[16], uint32_t S) {
-  int32_t lb = 0;
-#pragma unroll
-  for (int gg = 0; gg < 16; ++gg) lb = max(lb, ((S >> gg) & 1u) ? 0 : dd[gg]);
-  return lb;
 }
 
 // Does some entry j of vals (light-filtered costs of the marking vertex,
@@ -1088,7 +1179,18 @@ cudaError_t launch_group_masks(const int32_t* group_ptr, const int32_t* members,
   return cudaGetLastError();
 }
 
-cudaError_t launch_merge(const GraphDev& g, const LevelArgs& a, cudaStream_t stream) {
+cudaError_t launch_merge(const GraphDev& g, const LevelArgs& a, const MergeLevels& ml, cudaStream_t stream) {
+  if (a.k <= kMergeTabK && a.msplit_ptr) {
+    const size_t smem = (size_t)((a.m + 2) & ~1) * sizeof(int32_t) + (size_t)a.nsplits * sizeof(int2);
+    if (smem > 48 * 1024) {  // k = 9, 10: up to ~60 KB (set on the current device every time)
+      const cudaError_t e = cudaFuncSetAttribute(k_merge_vertex, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+    }
+    int64_t blocks = ((int64_t)g.V + kGrowThreads - 1) / kGrowThreads;
+    if (blocks > (1 << 20)) blocks = 1 << 20;
+    k_merge_vertex<<<(unsigned)blocks, kGrowThreads, smem, stream>>>(g, a, ml);
+    return cudaGetLastError();
+  }
   const int64_t total = (int64_t)g.V * a.stride;
   int64_t blocks = (total + kGrowThreads - 1) / kGrowThreads;
   if (blocks > (1 << 20)) blocks = 1 << 20;

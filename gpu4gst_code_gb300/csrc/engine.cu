@@ -82,6 +82,8 @@ int binom(int n, int r) {
 constexpr int32_t kTreePrefix = 4096;   // tree entries read back with the counters
 constexpr int kPollEvery = 8;           // host loop: rounds launched between polls
 constexpr int kEvents = 3 * GST_MAX_K + 8;
+// splits of every level for k = kMergeTabK: (3^k - 2^(k+1) + 1) / 2
+constexpr int64_t kMaxMergeSplits = 28501;
 constexpr int kProposeTop = 64;        // top-scored vertices offered to the proposal's repair
 constexpr int kProposeRounds = 8;      // growth rounds of the proposal's root distances
 constexpr int32_t kDefaultLanes = 4;   // concurrent solve contexts of a batch
@@ -108,6 +110,9 @@ struct Workspace {
   long long* stats = nullptr;
   MaskInfo* minfo = nullptr;  // 2^GST_MAX_K
   int32_t* lmasks = nullptr;  // 2^GST_MAX_K
+  int32_t* msplit_ptr = nullptr;  // merge split tables of every level (k <= kMergeTabK)
+  int2* msplits = nullptr;
+  std::vector<int32_t> h_msp_off, h_ms_off, h_ms_n;  // per level: offsets into the two, split count
   int32_t tables_k = 0;       // k the mask tables describe
   int32_t* d_group_ptr = nullptr;
   int32_t* d_members = nullptr;
@@ -301,6 +306,8 @@ void free_workspace(Workspace& ws) {
   dfree(ws.stats);
   dfree(ws.minfo);
   dfree(ws.lmasks);
+  dfree(ws.msplit_ptr);
+  dfree(ws.msplits);
   dfree(ws.d_group_ptr);
   dfree(ws.d_members);
   dfree(ws.qa);
@@ -353,6 +360,8 @@ gst_status ensure_workspace(gst_graph* g, int32_t k, int64_t nmembers) {
     GST_CUDA(cudaMalloc(&ws.stats, kNumStats * sizeof(long long)));
     GST_CUDA(cudaMalloc(&ws.minfo, sizeof(MaskInfo) << GST_MAX_K));
     GST_CUDA(cudaMalloc(&ws.lmasks, sizeof(int32_t) << GST_MAX_K));
+    GST_CUDA(cudaMalloc(&ws.msplit_ptr, ((size_t(1) << kMergeTabK) + kMergeTabK + 2) * sizeof(int32_t)));
+    GST_CUDA(cudaMalloc(&ws.msplits, kMaxMergeSplits * sizeof(int2)));
     GST_CUDA(cudaMallocHost(&ws.h_ctr, sizeof(Counters)));
     GST_CUDA(cudaMallocHost(&ws.h_ctl, sizeof(GrowCtl)));
     GST_CUDA(cudaMallocHost(&ws.h_params, sizeof(SolveParams)));
@@ -424,6 +433,39 @@ gst_status ensure_tables(gst_graph* g, int32_t k) {
     base += ws.h_lvl_stride[l];
   }
   info[0] = MaskInfo{0, 0, 0, 0};
+  // merge split tables (k <= kMergeTabK): per level, per mask in rank order,
+  // every split S1 | S2 = S with S1 holding S's lowest group
+  std::vector<int32_t> msp;
+  std::vector<int2> ms;
+  ws.h_msp_off.assign((size_t)k + 2, 0);
+  ws.h_ms_off.assign((size_t)k + 2, 0);
+  ws.h_ms_n.assign((size_t)k + 2, 0);
+  if (k <= kMergeTabK) {
+    for (int l = 1; l <= k; ++l) {
+      ws.h_msp_off[l] = (int32_t)msp.size();
+      ws.h_ms_off[l] = (int32_t)ms.size();
+      for (int32_t rank = 0; rank < ws.h_lvl_m[l]; ++rank) {
+        msp.push_back((int32_t)ms.size() - ws.h_ms_off[l]);
+        const uint32_t S = (uint32_t)lm[(size_t)(ws.h_lvl_base[l] + rank)];
+        if (l < 2) continue;
+        const uint32_t low = S & (0u - S), rest = S ^ low;
+        for (uint32_t sub = (rest - 1u) & rest;; sub = (sub - 1u) & rest) {
+          const uint32_t s1 = sub | low, s2 = S ^ s1;
+          const MaskInfo& i1 = info[s1];
+          const MaskInfo& i2 = info[s2];
+          ms.push_back(make_int2((i1.level << 24) | i1.rank, (i2.level << 24) | i2.rank));
+          if (sub == 0u) break;
+        }
+      }
+      msp.push_back((int32_t)ms.size() - ws.h_ms_off[l]);
+      ws.h_ms_n[l] = (int32_t)ms.size() - ws.h_ms_off[l];
+    }
+    if (ms.size() > (size_t)kMaxMergeSplits) return fail(GST_INTERNAL, "merge split table overflow");
+    GST_CUDA(cudaMemcpyAsync(ws.msplit_ptr, msp.data(), msp.size() * sizeof(int32_t), cudaMemcpyHostToDevice,
+                             g->stream));
+    if (!ms.empty())
+      GST_CUDA(cudaMemcpyAsync(ws.msplits, ms.data(), ms.size() * sizeof(int2), cudaMemcpyHostToDevice, g->stream));
+  }
   GST_CUDA(cudaMemcpyAsync(ws.minfo, info.data(), info.size() * sizeof(MaskInfo), cudaMemcpyHostToDevice,
                            g->stream));
   GST_CUDA(cudaMemcpyAsync(ws.lmasks, lm.data(), lm.size() * sizeof(int32_t), cudaMemcpyHostToDevice, g->stream));
@@ -468,8 +510,23 @@ LevelArgs level_args(gst_graph* g, int32_t k, int32_t l) {
   a.ctr = ws.ctr;
   a.stats = ws.stats;
   a.params = ws.d_params;
+  a.msplit_ptr = k <= kMergeTabK ? ws.msplit_ptr + ws.h_msp_off[l] : nullptr;
+  a.msplits = k <= kMergeTabK ? ws.msplits + ws.h_ms_off[l] : nullptr;
+  a.nsplits = k <= kMergeTabK ? ws.h_ms_n[l] : 0;
   a.use_cond = 0;
   return a;
+}
+
+MergeLevels merge_levels(const gst_graph* g, int32_t k) {
+  const Workspace& ws = g->ws;
+  MergeLevels ml{};
+  for (int l = 1; l <= std::min(k, kMergeTabK); ++l) {
+    ml.off[l] = (int64_t)ws.h_lvl_base[l] * g->V;
+    ml.stride[l] = ws.h_lvl_stride[l];
+    ml.mbase[l] = ws.h_lvl_base[l];
+  }
+  ml.lmasks_all = ws.lmasks;
+  return ml;
 }
 
 // Work before the waves: group masks and counters.
@@ -493,7 +550,7 @@ gst_status enqueue_merge(gst_graph* g, const LevelArgs& a, cudaStream_t s, int64
   Workspace& ws = g->ws;
   GST_CUDA(cudaMemsetAsync(ws.flags, 0, 6 * (size_t)vpad_of(g->V), s));
   GST_CUDA(cudaMemsetAsync(ws.ctl, 0, sizeof(GrowCtl), s));
-  GST_CUDA(launch_merge(graph_dev(g), a, s));
+  GST_CUDA(launch_merge(graph_dev(g), a, merge_levels(g, a.k), s));
   ++*launches;
   if (a.level < a.k) {  // how round 0 of the wave starts
     GST_CUDA(launch_seed(graph_dev(g), a, g->num_sms, s));
