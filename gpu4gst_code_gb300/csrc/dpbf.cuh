@@ -113,6 +113,7 @@ struct GraphDev {
   const int32_t* order;    // the other vertices by decreasing degree
   int32_t nsmall;          // V - nbig
   const int2* hub_chunk;   // (hub index, first CSR entry) per 32-entry chunk
+  const int32_t* chunk_vtx;  // the hub vertex of each chunk
   int64_t nchunks;
   unsigned long long* hub_min;  // per hub: hub_stride packed (cost, entry) minima
   int32_t* hub_cnt;             // per hub: chunks finished this round

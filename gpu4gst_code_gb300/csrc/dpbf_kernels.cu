@@ -557,9 +557,9 @@ __device__ __forceinline__ void hub_relax(const GraphDev& g, const LevelArgs& a,
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   const int32_t s = a.stride;
   for (int64_t c = warp; c < g.nchunks; c += nwarps) {
-    const int2 hc = g.hub_chunk[c];  // (hub index, first CSR entry of the chunk)
-    const int32_t u = g.big[hc.x];
+    const int32_t u = g.chunk_vtx[c];  // the flag test needs one dependent load
     if (!rs.all_cand && !rs.cand_cur[u]) continue;
+    const int2 hc = g.hub_chunk[c];  // (hub index, first CSR entry of the chunk)
     const int32_t beg = g.row_ptr[u], end = g.row_ptr[u + 1];
     const int32_t cend = min(end, hc.y + G);
     unsigned long long* hm = g.hub_min + (int64_t)hc.x * g.hub_stride;
@@ -622,9 +622,9 @@ __device__ __forceinline__ void hub_mark(const GraphDev& g, const LevelArgs& a, 
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   const int32_t s = a.stride;
   for (int64_t c = warp; c < g.nchunks; c += nwarps) {
-    const int2 hc = g.hub_chunk[c];
-    const int32_t u = g.big[hc.x];
+    const int32_t u = g.chunk_vtx[c];
     if (!rs.next_flag[u]) continue;
+    const int2 hc = g.hub_chunk[c];
     const int32_t e = hc.y + lane;
     if (e >= g.row_ptr[u + 1]) continue;
     const int2 x = g.adj[e];

@@ -186,6 +186,7 @@ struct gst_graph {
   int32_t deg_big = kDegBigMin;  // hub threshold of this graph
   int32_t* d_order = nullptr;  // vertices of degree <= deg_big, by decreasing degree
   int2* d_hub_chunk = nullptr;  // (hub index, first CSR entry) per 32-entry chunk of a hub row
+  int32_t* d_chunk_vtx = nullptr;  // the hub vertex of each chunk
   int64_t nchunks = 0;
   int32_t max_w = 0;  // largest edge weight
   // Internal vertex IDs: perm[caller ID] and its inverse (see gst_graph_upload)
@@ -248,6 +249,7 @@ GraphDev graph_dev(const gst_graph* g) {
   d.order = g->d_order;
   d.nsmall = g->V - g->nbig;
   d.hub_chunk = g->d_hub_chunk;
+  d.chunk_vtx = g->d_chunk_vtx;
   d.nchunks = g->nchunks;
   d.hub_min = g->ws.hub_min;
   d.hub_cnt = g->ws.hub_cnt;
@@ -1308,6 +1310,7 @@ gst_status ensure_lanes(gst_graph* g, int32_t n) {
     l->nbig = g->nbig;
     l->d_order = g->d_order;
     l->d_hub_chunk = g->d_hub_chunk;
+    l->d_chunk_vtx = g->d_chunk_vtx;
     l->nchunks = g->nchunks;
     l->max_w = g->max_w;
     l->perm = g->perm;
@@ -1414,8 +1417,12 @@ gst_status gst_graph_upload(const int32_t* row_ptr, const int32_t* col, const in
   std::vector<int32_t> hub_of((size_t)V, -1);
   for (int32_t h = 0; h < g->nbig; ++h) hub_of[(size_t)big[(size_t)h]] = h;
   std::vector<int2> chunks;
+  std::vector<int32_t> chunk_vtx;
   for (int32_t h = 0; h < g->nbig; ++h)
-    for (int32_t e = row_ptr[big[(size_t)h]]; e < row_ptr[big[(size_t)h] + 1]; e += 32) chunks.push_back(make_int2(h, e));
+    for (int32_t e = row_ptr[big[(size_t)h]]; e < row_ptr[big[(size_t)h] + 1]; e += 32) {
+      chunks.push_back(make_int2(h, e));
+      chunk_vtx.push_back(big[(size_t)h]);
+    }
   g->nchunks = (int64_t)chunks.size();
   auto cleanup = [&](gst_status s) {
     gst_graph_free(g);
@@ -1439,6 +1446,7 @@ gst_status gst_graph_upload(const int32_t* row_ptr, const int32_t* col, const in
       (e = up((void**)&g->d_big, big.data(), big.size() * 4)) != cudaSuccess ||
       (e = up((void**)&g->d_order, order.data(), order.size() * 4)) != cudaSuccess ||
       (e = up((void**)&g->d_hub_chunk, chunks.data(), chunks.size() * sizeof(int2))) != cudaSuccess ||
+      (e = up((void**)&g->d_chunk_vtx, chunk_vtx.data(), chunk_vtx.size() * sizeof(int32_t))) != cudaSuccess ||
       (e = cudaStreamSynchronize(g->stream)) != cudaSuccess)
     return cleanup(fail(e == cudaErrorMemoryAllocation ? GST_OOM : GST_CUDA_ERROR,
                         std::string("graph upload: ") + cudaGetErrorString(e)));
@@ -1466,6 +1474,7 @@ void gst_graph_free(gst_graph* g) {
     dfree(g->d_big);
     dfree(g->d_order);
     dfree(g->d_hub_chunk);
+    dfree(g->d_chunk_vtx);
   }
   if (g->stream) cudaStreamDestroy(g->stream);
   if (g->side) cudaStreamDestroy(g->side);
