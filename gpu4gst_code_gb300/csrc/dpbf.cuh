@@ -89,6 +89,7 @@ struct GrowCtl {
   int32_t dense[3];     // round ran dense (all vertices, no candidate marks)
   int32_t last_changed; // changes of the last completed round
   int32_t timeout;      // stopped by max_rounds with changes pending
+  uint32_t work[3];     // rotating per-round work counters (vertex batches / candidate tiles taken)
 };
 
 // Device-side counters of one solve.

@@ -314,6 +314,7 @@ __global__ void __launch_bounds__(kGrowThreads) k_merge_vertex(GraphDev g, Level
 namespace {
 
 constexpr int kGatherUnroll = 4;
+constexpr int kDenseGrab = 64;  // sweep positions a warp takes at a time in dense rounds
 
 struct RoundState {
   int32_t r;
@@ -463,6 +464,7 @@ __device__ __forceinline__ void round_end(const LevelArgs& a, const RoundState& 
   ctl->dense[rs.r % 3] = rs.dense ? 1 : 0;
   ctl->last_changed = total;
   ctl->changed[(rs.r + 1) % 3] = 0;
+  ctl->work[(rs.r + 1) % 3] = 0u;
   ctl->done = 0u;
   ctl->round = rs.r + 1;
   atomicAdd(&a.ctr->rounds_total, 1);
@@ -890,20 +892,39 @@ __global__ void __launch_bounds__(kGrowThreads, (MP <= 16 ? 3 : 2)) k_grow_threa
     hub_relax<(MP + 31) / 32>(g, a, rs, acc);
   else
     hub_mark(g, a, rs, acc);
+  // warps take their work from the round's counter, so blocks that draw
+  // cheap vertices (or tiles without candidates) take more of them and no
+  // SM idles while another finishes a fixed share
+  const int lane = threadIdx.x & 31;
+  uint32_t* work = &a.ctl->work[rs.r % 3];
   if (rs.all_cand) {
-    // every vertex; odd rounds sweep backwards, so in-place updates also
-    // carry along the order in the other direction within one round
-    for (int64_t i = t0; i < g.nsmall; i += nthreads)
-      thread_vertex<MP>(g, a, rs, g.order[(rs.r & 1) ? g.nsmall - 1 - i : i], acc);
+    // every vertex, kDenseGrab sweep positions per take; odd rounds sweep
+    // backwards, so in-place updates also carry along the order in the
+    // other direction within one round
+    for (;;) {
+      uint32_t base = 0;
+      if (lane == 0) base = atomicAdd(work, (uint32_t)kDenseGrab);
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if ((int64_t)base >= g.nsmall) break;
+#pragma unroll 1
+      for (int j = lane; j < kDenseGrab; j += 32) {
+        const int64_t i = (int64_t)base + j;
+        if (i < g.nsmall) thread_vertex<MP>(g, a, rs, g.order[(rs.r & 1) ? g.nsmall - 1 - i : i], acc);
+      }
+    }
   } else {
     // candidates only: a warp reads kCandTile candidate bytes at a time (8
     // per lane), compacts the set ones in shared memory and its lanes take
     // them in turn
     __shared__ int32_t tile[kGrowThreads / 32][kCandTile];
-    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const int64_t warp = t0 >> 5, nwarps = nthreads >> 5;
+    const int wib = threadIdx.x >> 5;
     static_assert(kCandTile == 8 * 32, "a lane reads 8 flag bytes");
-    for (int64_t base = warp * kCandTile; base < g.V; base += nwarps * kCandTile) {
+    for (;;) {
+      uint32_t ti = 0;
+      if (lane == 0) ti = atomicAdd(work, 1u);
+      ti = __shfl_sync(0xffffffffu, ti, 0);
+      const int64_t base = (int64_t)ti * kCandTile;
+      if (base >= g.V) break;
       const int64_t v0 = base + 8 * lane;
       uint2 f = make_uint2(0u, 0u);
       if (v0 < g.V) f = *reinterpret_cast<const uint2*>(rs.cand_cur + v0);  // arrays padded to 16 bytes
