@@ -314,7 +314,7 @@ __global__ void __launch_bounds__(kGrowThreads) k_merge_vertex(GraphDev g, Level
 namespace {
 
 constexpr int kGatherUnroll = 4;
-constexpr int kDenseGrab = 64;  // sweep positions a warp takes at a time in dense rounds
+constexpr int kDenseGrab = 32;  // sweep positions a warp takes at a time in dense rounds (one per lane)
 
 struct RoundState {
   int32_t r;
@@ -901,16 +901,14 @@ __global__ void __launch_bounds__(kGrowThreads, (MP <= 16 ? 3 : 2)) k_grow_threa
     // every vertex, kDenseGrab sweep positions per take; odd rounds sweep
     // backwards, so in-place updates also carry along the order in the
     // other direction within one round
+    static_assert(kDenseGrab == 32, "one sweep position per lane");
     for (;;) {
       uint32_t base = 0;
       if (lane == 0) base = atomicAdd(work, (uint32_t)kDenseGrab);
       base = __shfl_sync(0xffffffffu, base, 0);
       if ((int64_t)base >= g.nsmall) break;
-#pragma unroll 1
-      for (int j = lane; j < kDenseGrab; j += 32) {
-        const int64_t i = (int64_t)base + j;
-        if (i < g.nsmall) thread_vertex<MP>(g, a, rs, g.order[(rs.r & 1) ? g.nsmall - 1 - i : i], acc);
-      }
+      const int64_t i = (int64_t)base + lane;
+      if (i < g.nsmall) thread_vertex<MP>(g, a, rs, g.order[(rs.r & 1) ? g.nsmall - 1 - i : i], acc);
     }
   } else {
     // candidates only: a warp reads kCandTile candidate bytes at a time (8
@@ -982,9 +980,13 @@ __global__ void __launch_bounds__(kGrowThreads, (L >= 3 ? 3 : 4)) k_grow_group(G
     constexpr int NGW = 32 / G;
     const int gw = lane / G;
     const int32_t s = a.stride;
-    const int64_t wid = ((int64_t)blockIdx.x * blockDim.x + tid) >> 5;
-    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t vbase = wid * 32; vbase < g.V; vbase += nwarps * 32) {
+    uint32_t* work = &a.ctl->work[rs.r % 3];
+    for (;;) {  // 32 consecutive vertices per take from the round's counter
+      uint32_t wt = 0;
+      if (lane == 0) wt = atomicAdd(work, 1u);
+      wt = __shfl_sync(0xffffffffu, wt, 0);
+      const int64_t vbase = (int64_t)wt * 32;
+      if (vbase >= g.V) break;
       const int64_t vl = vbase + lane;
       const bool cnd = vl < g.V && (rs.all_cand || rs.cand_cur[vl] != 0);
       unsigned cm = __ballot_sync(0xffffffffu, cnd);
