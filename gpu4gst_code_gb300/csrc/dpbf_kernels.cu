@@ -358,6 +358,18 @@ __device__ __forceinline__ bool round_begin(const GraphDev& g, const LevelArgs& 
   return true;
 }
 
+// Zeroes the change flags of two rounds back and the candidate flags of the
+// last round (vpad bytes each, 16-byte aligned) with 16-byte stores.
+__device__ __forceinline__ void clear_flags(const LevelArgs& a, const RoundState& rs, int64_t t0, int64_t nthreads) {
+  uint4* f = reinterpret_cast<uint4*>(rs.clear_flag);
+  uint4* c = reinterpret_cast<uint4*>(rs.cand_clear);
+  const uint4 z = make_uint4(0u, 0u, 0u, 0u);
+  for (int64_t i = t0; i < ((int64_t)a.vpad >> 4); i += nthreads) {
+    f[i] = z;
+    c[i] = z;
+  }
+}
+
 // Makes v a candidate of the next round (an idempotent byte store).
 __device__ __forceinline__ void mark_candidate(uint8_t* cand, int32_t v, uint32_t (&acc)[kAccN]) {
   cand[v] = 1;
@@ -550,64 +562,80 @@ __device__ __forceinline__ void group_relax(const GraphDev& g, const LevelArgs& 
 // round kernel, which then marks the changed hubs' neighbours chunk by
 // chunk (hub_mark), so no single warp walks a whole hub row.
 template <int L>
-__device__ __forceinline__ void hub_relax(const GraphDev& g, const LevelArgs& a, const RoundState& rs,
-                                          uint32_t (&acc)[kAccN]) {
+__device__ __forceinline__ void hub_chunk_relax(const GraphDev& g, const LevelArgs& a, const RoundState& rs,
+                                                int64_t c, uint32_t (&acc)[kAccN]) {
   constexpr int G = 32;
   constexpr int CH = G * L;
   const int lane = threadIdx.x & 31;
+  const int32_t s = a.stride;
+  const int32_t u = g.chunk_vtx[c];
+  const int2 hc = g.hub_chunk[c];  // (hub index, first CSR entry of the chunk)
+  const int32_t beg = g.row_ptr[u], end = g.row_ptr[u + 1];
+  const int32_t cend = min(end, hc.y + G);
+  unsigned long long* hm = g.hub_min + (int64_t)hc.x * g.hub_stride;
+  for (int jc = 0; jc < s; jc += CH) {
+    int32_t best[L], code[L];
+#pragma unroll
+    for (int t = 0; t < L; ++t) {
+      best[t] = kInf;
+      code[t] = -1;
+    }
+    group_relax<G, L>(g, a, rs, hc.y, cend, jc, lane, 0, 0xffffffffu, 0xffffffffu, best, code, acc);
+#pragma unroll
+    for (int t = 0; t < L; ++t) {
+      const int j = jc + lane + t * G;
+      if (j < s && best[t] < kInf)
+        atomicMin(hm + j, ((unsigned long long)(uint32_t)best[t] << 32) | (uint32_t)code[t]);
+    }
+  }
+  if (lane == 0) acc[kAccEnt] += cend - hc.y;
+  __threadfence();
+  int last = 0;
+  if (lane == 0) last = atomicAdd(g.hub_cnt + hc.x, 1) == (end - beg + G - 1) / G - 1;
+  last = __shfl_sync(0xffffffffu, last, 0);
+  if (!last) return;
+  __threadfence();
+  const int64_t rowu = a.base + (int64_t)u * s;
+  bool imp = false;
+  for (int j = lane; j < s; j += G) {
+    const unsigned long long r = atomicExch(hm + j, ~0ull);  // read and clear
+    if (j >= a.m || r == ~0ull) continue;
+    const int32_t c2 = (int32_t)(r >> 32);
+    const int32_t own = a.cost[rowu + j];
+    if (c2 >= own) continue;
+    if (rs.ub > 0 && c2 > prune_cap(a, rs.ub, u, (uint32_t)__ldg(a.lmasks + j))) continue;
+    a.cost[rowu + j] = c2;
+    a.par[rowu + j] = (int32_t)(uint32_t)(r & 0xffffffffull);
+    imp = true;
+    ++acc[kAccImproved];
+  }
+  if (lane == 0) {
+    atomicExch(g.hub_cnt + hc.x, 0);
+    ++acc[kAccVert];
+  }
+  if (__ballot_sync(0xffffffffu, imp) && lane == 0) {
+    rs.next_flag[u] = 1;
+    ++acc[kAccChanged];
+  }
+}
+
+// A warp takes chunks warp, warp + W, warp + 2W, ... (W warps in the
+// grid); its lanes test 32 of them for candidacy at once and the warp
+// relaxes the candidate ones in turn.
+template <int L>
+__device__ __forceinline__ void hub_relax(const GraphDev& g, const LevelArgs& a, const RoundState& rs,
+                                          uint32_t (&acc)[kAccN]) {
+  const int lane = threadIdx.x & 31;
   const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  const int32_t s = a.stride;
-  for (int64_t c = warp; c < g.nchunks; c += nwarps) {
-    const int32_t u = g.chunk_vtx[c];  // the flag test needs one dependent load
-    if (!rs.all_cand && !rs.cand_cur[u]) continue;
-    const int2 hc = g.hub_chunk[c];  // (hub index, first CSR entry of the chunk)
-    const int32_t beg = g.row_ptr[u], end = g.row_ptr[u + 1];
-    const int32_t cend = min(end, hc.y + G);
-    unsigned long long* hm = g.hub_min + (int64_t)hc.x * g.hub_stride;
-    for (int jc = 0; jc < s; jc += CH) {
-      int32_t best[L], code[L];
-#pragma unroll
-      for (int t = 0; t < L; ++t) {
-        best[t] = kInf;
-        code[t] = -1;
-      }
-      group_relax<G, L>(g, a, rs, hc.y, cend, jc, lane, 0, 0xffffffffu, 0xffffffffu, best, code, acc);
-#pragma unroll
-      for (int t = 0; t < L; ++t) {
-        const int j = jc + lane + t * G;
-        if (j < s && best[t] < kInf)
-          atomicMin(hm + j, ((unsigned long long)(uint32_t)best[t] << 32) | (uint32_t)code[t]);
-      }
-    }
-    if (lane == 0) acc[kAccEnt] += cend - hc.y;
-    __threadfence();
-    int last = 0;
-    if (lane == 0) last = atomicAdd(g.hub_cnt + hc.x, 1) == (end - beg + G - 1) / G - 1;
-    last = __shfl_sync(0xffffffffu, last, 0);
-    if (!last) continue;
-    __threadfence();
-    const int64_t rowu = a.base + (int64_t)u * s;
-    bool imp = false;
-    for (int j = lane; j < s; j += G) {
-      const unsigned long long r = atomicExch(hm + j, ~0ull);  // read and clear
-      if (j >= a.m || r == ~0ull) continue;
-      const int32_t c2 = (int32_t)(r >> 32);
-      const int32_t own = a.cost[rowu + j];
-      if (c2 >= own) continue;
-      if (rs.ub > 0 && c2 > prune_cap(a, rs.ub, u, (uint32_t)__ldg(a.lmasks + j))) continue;
-      a.cost[rowu + j] = c2;
-      a.par[rowu + j] = (int32_t)(uint32_t)(r & 0xffffffffull);
-      imp = true;
-      ++acc[kAccImproved];
-    }
-    if (lane == 0) {
-      atomicExch(g.hub_cnt + hc.x, 0);
-      ++acc[kAccVert];
-    }
-    if (__ballot_sync(0xffffffffu, imp) && lane == 0) {
-      rs.next_flag[u] = 1;
-      ++acc[kAccChanged];
+  for (int64_t c0 = warp; c0 < g.nchunks; c0 += 32 * nwarps) {
+    const int64_t cl = c0 + lane * nwarps;
+    const bool want = cl < g.nchunks && (rs.all_cand || rs.cand_cur[g.chunk_vtx[cl]] != 0);
+    unsigned bal = __ballot_sync(0xffffffffu, want);
+    while (bal) {
+      const int64_t c = c0 + (int64_t)(__ffs(bal) - 1) * nwarps;
+      bal &= bal - 1u;
+      hub_chunk_relax<L>(g, a, rs, c, acc);
     }
   }
 }
@@ -623,18 +651,24 @@ __device__ __forceinline__ void hub_mark(const GraphDev& g, const LevelArgs& a, 
   const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   const int32_t s = a.stride;
-  for (int64_t c = warp; c < g.nchunks; c += nwarps) {
-    const int32_t u = g.chunk_vtx[c];
-    if (!rs.next_flag[u]) continue;
-    const int2 hc = g.hub_chunk[c];
-    const int32_t e = hc.y + lane;
-    if (e >= g.row_ptr[u + 1]) continue;
-    const int2 x = g.adj[e];
-    const int32_t* hv = a.cost + a.base + (int64_t)u * s;
-    const int32_t* yv = a.cost + a.base + (int64_t)x.x * s;
-    if (improves_row(a, rs.ub, x.x, x.y, [&](int j) { return light_or_inf(hv[j], rs.ub_light); },
-                     [&](int j) { return yv[j]; }, a.m))
-      mark_candidate(rs.cand_next, x.x, acc);
+  for (int64_t c0 = warp; c0 < g.nchunks; c0 += 32 * nwarps) {  // chunks taken as in hub_relax
+    const int64_t cl = c0 + lane * nwarps;
+    const bool want = cl < g.nchunks && rs.next_flag[g.chunk_vtx[cl]] != 0;
+    unsigned bal = __ballot_sync(0xffffffffu, want);
+    while (bal) {
+      const int64_t c = c0 + (int64_t)(__ffs(bal) - 1) * nwarps;
+      bal &= bal - 1u;
+      const int32_t u = g.chunk_vtx[c];
+      const int2 hc = g.hub_chunk[c];
+      const int32_t e = hc.y + lane;
+      if (e >= g.row_ptr[u + 1]) continue;
+      const int2 x = g.adj[e];
+      const int32_t* hv = a.cost + a.base + (int64_t)u * s;
+      const int32_t* yv = a.cost + a.base + (int64_t)x.x * s;
+      if (improves_row(a, rs.ub, x.x, x.y, [&](int j) { return light_or_inf(hv[j], rs.ub_light); },
+                       [&](int j) { return yv[j]; }, a.m))
+        mark_candidate(rs.cand_next, x.x, acc);
+    }
   }
 }
 
@@ -884,10 +918,7 @@ __global__ void __launch_bounds__(kGrowThreads, (MP <= 16 ? 3 : 2)) k_grow_threa
   uint32_t acc[kAccN] = {0, 0, 0, 0, 0, 0, 0};
   const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t i = t0; i < g.V; i += nthreads) {
-    rs.clear_flag[i] = 0;
-    rs.cand_clear[i] = 0;
-  }
+  clear_flags(a, rs, t0, nthreads);
   if (rs.dense)
     hub_relax<(MP + 31) / 32>(g, a, rs, acc);
   else
@@ -962,10 +993,7 @@ __global__ void __launch_bounds__(kGrowThreads, (L >= 3 ? 3 : 4)) k_grow_group(G
   {
     const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t i = t0; i < g.V; i += nthreads) {
-      rs.clear_flag[i] = 0;
-      rs.cand_clear[i] = 0;
-    }
+    clear_flags(a, rs, t0, nthreads);
   }
   if (rs.dense)
     hub_relax<((G * L + 31) / 32 < 4 ? (G * L + 31) / 32 : 4)>(g, a, rs, acc);
