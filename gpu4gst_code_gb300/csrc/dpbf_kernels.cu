@@ -522,15 +522,23 @@ __device__ __forceinline__ void group_relax(const GraphDev& g, const LevelArgs& 
       vv[i] = __shfl_sync(gmask_lanes, nv, sl, G);
       ww[i] = __shfl_sync(gmask_lanes, nw, sl, G);
     }
+    // every load is issued unconditionally at an address inside row vv[i]
+    // (entries past the row's end read its last entry; slots without a
+    // source read the row of the group's first lane), so all of them are in
+    // flight together whatever registers the compiler assigns; the unwanted
+    // values are masked afterwards
     int32_t c[kGatherUnroll][L];
 #pragma unroll
     for (int i = 0; i < kGatherUnroll; ++i) {
-      const int64_t rowv = a.base + (int64_t)vv[i] * s + jc;
+      const int32_t* rowv = a.cost + a.base + (int64_t)vv[i] * s;
 #pragma unroll
-      for (int t = 0; t < L; ++t) {
-        const int j = glane + t * G;
-        c[i][t] = (src[i] >= 0 && jc + j < s) ? light_or_inf(a.cost[rowv + j], rs.ub_light) : kInf;
-      }
+      for (int t = 0; t < L; ++t) c[i][t] = rowv[min(jc + glane + t * G, s - 1)];
+    }
+#pragma unroll
+    for (int i = 0; i < kGatherUnroll; ++i) {
+#pragma unroll
+      for (int t = 0; t < L; ++t)
+        c[i][t] = (src[i] >= 0 && jc + glane + t * G < s) ? light_or_inf(c[i][t], rs.ub_light) : kInf;
     }
 #pragma unroll
     for (int i = 0; i < kGatherUnroll; ++i) {
