@@ -315,6 +315,7 @@ namespace {
 
 constexpr int kGatherUnroll = 4;
 constexpr int kDenseGrab = 32;  // sweep positions a warp takes at a time in dense rounds (one per lane)
+constexpr int kWarpMarkMax = 16;  // changed rows of a warp up to which its lanes share each row's marking
 
 struct RoundState {
   int32_t r;
@@ -754,14 +755,16 @@ __global__ void __launch_bounds__(kGrowThreads) k_grow_hubs(GraphDev g, LevelArg
   round_flush(a, rs, acc, ba);
 }
 
-// Thread per vertex: the vertex's MP-entry row lives in registers.
+// Thread per vertex: the vertex's MP-entry row lives in registers. True
+// when the row changed (the caller's warp then marks its neighbours,
+// warp_mark).
 template <int MP>
-__device__ __forceinline__ void thread_vertex(const GraphDev& g, const LevelArgs& a, const RoundState& rs,
+__device__ __forceinline__ bool thread_vertex(const GraphDev& g, const LevelArgs& a, const RoundState& rs,
                                               int32_t u, uint32_t (&acc)[kAccN]) {
   constexpr int U = MP <= 8 ? 4 : 2;
   constexpr int Q = MP / 4;
   const int32_t beg = g.row_ptr[u], end = g.row_ptr[u + 1];
-  if (end - beg > g.deg_big) return;  // hub: handled in 32-entry chunks
+  if (end - beg > g.deg_big) return false;  // hub: handled in 32-entry chunks
   int4* rowc = reinterpret_cast<int4*>(a.cost + a.base + (int64_t)u * MP);
   int32_t best[MP];
   // parent of entry j as (CSR entry - beg), one byte each (rows are at most
@@ -781,7 +784,7 @@ __device__ __forceinline__ void thread_vertex(const GraphDev& g, const LevelArgs
   for (int j = 0; j < MP; ++j) live |= j < a.m && best[j] != 0;  // cost-0 states cannot improve
   ++acc[kAccVert];
   acc[kAccEnt] += end - beg;
-  if (!live) return;
+  if (!live) return false;
   // software pipeline: the next batch's CSR entries (and, in sparse rounds,
   // their change flags) are loaded while this batch's rows are gathered
   int32_t nv[U], nw[U];
@@ -872,7 +875,7 @@ __device__ __forceinline__ void thread_vertex(const GraphDev& g, const LevelArgs
     }
     any |= ((code[j >> 2] >> sh) & 0xffu) != 0xffu;
   }
-  if (!any) return;
+  if (!any) return false;
 #pragma unroll
   for (int q = 0; q < Q; ++q) rowc[q] = make_int4(best[4 * q], best[4 * q + 1], best[4 * q + 2], best[4 * q + 3]);
   int32_t* rowp = a.par + a.base + (int64_t)u * MP;
@@ -886,34 +889,65 @@ __device__ __forceinline__ void thread_vertex(const GraphDev& g, const LevelArgs
   }
   rs.next_flag[u] = 1;
   ++acc[kAccChanged];
-  if (rs.dense) return;  // the next round sweeps every vertex
-  // mark a neighbour only if the new row improves it for some mask (within
-  // its bound): its row can only decrease later, so an unmarked neighbour
-  // never needs this row
+  return true;
+}
+
+// Marks, for every vertex of the warp whose row changed this round (chg),
+// the neighbours that the new row improves (within their bound): the
+// warp's lanes take one neighbour each, so a changed vertex costs one
+// step rather than a serial walk by its own lane. A neighbour is marked
+// only if the new row improves it for some mask: its row can only
+// decrease later, so an unmarked neighbour never needs this row. Every
+// lane of the warp must call it; dense rounds mark nothing (the next
+// round sweeps every vertex).
+template <int MP>
+__device__ __forceinline__ void warp_mark(const GraphDev& g, const LevelArgs& a, const RoundState& rs, int32_t u,
+                                          bool chg, uint32_t (&acc)[kAccN]) {
+  constexpr int Q = MP / 4;
+  if (rs.dense) return;
+  unsigned pend = __ballot_sync(0xffffffffu, chg);
+  if (!pend) return;
+  __syncwarp();  // the changed rows' stores are visible to the whole warp
+  const int lane = threadIdx.x & 31;
+  // with many changed rows in the warp, each lane walks its own row's
+  // neighbours (those walks run side by side); with few, the warp's lanes
+  // share each changed row's neighbours
+  const bool own = __popc(pend) > kWarpMarkMax;
+  if (own) pend = chg ? 1u : 0u;
+  while (pend) {
+    const int src = __ffs(pend) - 1;
+    pend &= pend - 1u;
+    const int32_t w = own ? u : __shfl_sync(0xffffffffu, u, src);
+    const int32_t beg = g.row_ptr[w], end = g.row_ptr[w + 1];
+    // w's new row is read 16 bytes at a time (in the shared walk at the
+    // same address in every lane: broadcast loads, cached), light-filtered
+    const int4* wr = reinterpret_cast<const int4*>(a.cost + a.base + (int64_t)w * MP);
+    for (int32_t e = own ? beg : beg + lane; e < end; e += own ? 1 : 32) {
+      const int2 x = g.adj[e];
+      const int4* rv = reinterpret_cast<const int4*>(a.cost + a.base + (int64_t)x.x * MP);
+      uint32_t bits = 0;  // masks the new row improves at x
 #pragma unroll
-  for (int j = 0; j < MP; ++j) best[j] = light_or_inf(best[j], rs.ub_light);
-  for (int32_t e = beg; e < end; ++e) {
-    const int2 x = g.adj[e];
-    const int4* rv = reinterpret_cast<const int4*>(a.cost + a.base + (int64_t)x.x * MP);
-    uint32_t bits = 0;  // masks the new row improves at x
-#pragma unroll
-    for (int q = 0; q < Q; ++q) {
-      const int4 t = rv[q];
-      bits |= (best[4 * q] + x.y < t.x ? 1u : 0u) << (4 * q);
-      bits |= (best[4 * q + 1] + x.y < t.y ? 1u : 0u) << (4 * q + 1);
-      bits |= (best[4 * q + 2] + x.y < t.z ? 1u : 0u) << (4 * q + 2);
-      bits |= (best[4 * q + 3] + x.y < t.w ? 1u : 0u) << (4 * q + 3);
+      for (int q = 0; q < Q; ++q) {
+        const int4 t = rv[q], h = wr[q];
+        bits |= (light_or_inf(h.x, rs.ub_light) + x.y < t.x ? 1u : 0u) << (4 * q);
+        bits |= (light_or_inf(h.y, rs.ub_light) + x.y < t.y ? 1u : 0u) << (4 * q + 1);
+        bits |= (light_or_inf(h.z, rs.ub_light) + x.y < t.z ? 1u : 0u) << (4 * q + 2);
+        bits |= (light_or_inf(h.w, rs.ub_light) + x.y < t.w ? 1u : 0u) << (4 * q + 3);
+      }
+      bool better = bits != 0;
+      if (better && rs.ub > 0) {  // the same test under x's one-label caps
+        int32_t dd[16];
+        load_label_bound(a, rs.ub, x.x, dd);
+        better = false;
+        const int32_t* wj = a.cost + a.base + (int64_t)w * MP;
+        while (bits && !better) {
+          const int j = __ffs(bits) - 1;
+          bits &= bits - 1u;
+          better = light_or_inf(wj[j], rs.ub_light) + x.y + label_bound(dd, (uint32_t)__ldg(a.lmasks + j)) <= rs.ub;
+        }
+      }
+      if (better) mark_candidate(rs.cand_next, x.x, acc);
     }
-    bool better = bits != 0;
-    if (better && rs.ub > 0) {  // the same test under x's one-label caps
-      int32_t dd[16];
-      load_label_bound(a, rs.ub, x.x, dd);
-      better = false;
-#pragma unroll
-      for (int j = 0; j < MP; ++j)
-        better |= ((bits >> j) & 1u) && best[j] + x.y + label_bound(dd, (uint32_t)__ldg(a.lmasks + j)) <= rs.ub;
-    }
-    if (better) mark_candidate(rs.cand_next, x.x, acc);
   }
 }
 
@@ -947,7 +981,9 @@ __global__ void __launch_bounds__(kGrowThreads, (MP <= 16 ? 3 : 2)) k_grow_threa
       base = __shfl_sync(0xffffffffu, base, 0);
       if ((int64_t)base >= g.nsmall) break;
       const int64_t i = (int64_t)base + lane;
-      if (i < g.nsmall) thread_vertex<MP>(g, a, rs, g.order[(rs.r & 1) ? g.nsmall - 1 - i : i], acc);
+      const int32_t u = i < g.nsmall ? g.order[(rs.r & 1) ? g.nsmall - 1 - i : i] : -1;
+      const bool chg = u >= 0 && thread_vertex<MP>(g, a, rs, u, acc);
+      warp_mark<MP>(g, a, rs, u, chg, acc);
     }
   } else {
     // candidates only: a warp reads kCandTile candidate bytes at a time (8
@@ -981,7 +1017,11 @@ __global__ void __launch_bounds__(kGrowThreads, (MP <= 16 ? 3 : 2)) k_grow_threa
       for (int b = 0; b < 8; ++b)
         if (((w2[b >> 2] >> (8 * (b & 3))) & 0xffu) != 0) tile[wib][pos++] = (int32_t)(v0 + b);
       __syncwarp();
-      for (int i = lane; i < total; i += 32) thread_vertex<MP>(g, a, rs, tile[wib][i], acc);
+      for (int i0 = 0; i0 < total; i0 += 32) {
+        const int32_t u = i0 + lane < total ? tile[wib][i0 + lane] : -1;
+        const bool chg = u >= 0 && thread_vertex<MP>(g, a, rs, u, acc);
+        warp_mark<MP>(g, a, rs, u, chg, acc);
+      }
       __syncwarp();
     }
   }
