@@ -198,6 +198,130 @@ __global__ void __launch_bounds__(kGrowThreads) k_merge(GraphDev g, LevelArgs a)
 // by row. The level's split table sits in shared memory, so a split costs
 // its two row loads; the vertex's group mask and one-label bound are
 // loaded once; the row is written 16 bytes at a time.
+// Queries with at most kMergeStagedWords words of lower-level row per
+// vertex (k <= 7): a thread copies its vertex's rows of levels 1..l-1 into
+// shared memory once (light-filtered there when the merge uses light
+// parts), a column per thread, and every split then reads two shared words
+// at offsets precomputed into the block's copy of the split table, instead
+// of computing two global row addresses from the split's levels.
+constexpr int kMergeStagedThreads = 128;
+constexpr int kMergeStagedWords = 136;
+
+__global__ void __launch_bounds__(kMergeStagedThreads) k_merge_staged(GraphDev g, LevelArgs a, MergeLevels ml) {
+  constexpr int NT = kMergeStagedThreads;
+  extern __shared__ int32_t msm[];
+  __shared__ int32_t loff[kMergeTabK + 1];  // level l's first word in a vertex's staged rows
+  int32_t* sp = msm;                                            // m + 1
+  int2* ss = reinterpret_cast<int2*>(msm + ((a.m + 2) & ~1));  // nsplits: staged word offsets x NT
+  int32_t* rows = reinterpret_cast<int32_t*>(ss + a.nsplits);   // staged words x NT
+  if (threadIdx.x == 0) {
+    int32_t o = 0;
+    for (int l = 1; l < a.level; ++l) {
+      loff[l] = o;
+      o += ml.stride[l];
+    }
+  }
+  for (int i = threadIdx.x; i <= a.m; i += blockDim.x) sp[i] = a.msplit_ptr[i];
+  __syncthreads();
+  for (int i = threadIdx.x; i < a.nsplits; i += blockDim.x) {
+    const int2 x = a.msplits[i];
+    ss[i] = make_int2((loff[x.x >> 24] + (x.x & 0xffffff)) * NT, (loff[x.y >> 24] + (x.y & 0xffffff)) * NT);
+  }
+  __syncthreads();
+  const int32_t ub = (a.level >= 2) ? a.params->ub : 0;
+  const int32_t ub_light = a.params->ub;
+  const int32_t ovf_limit = a.params->ovf_limit;
+  const bool light_parts = a.level < a.k;
+  uint8_t* flag2 = a.flags + 2 * (int64_t)a.vpad;
+  long long acc[3] = {0, 0, 0};  // finite states, splits, overflow
+  const int64_t v = (int64_t)blockIdx.x * NT + threadIdx.x;
+  if (v < g.V) {
+    int32_t* col = rows + threadIdx.x;
+    for (int l = 1; l < a.level; ++l) {
+      const int4* src = reinterpret_cast<const int4*>(a.cost + ml.off[l] + v * ml.stride[l]);
+      int32_t* dst = col + loff[l] * NT;
+      for (int q = 0; q < (ml.stride[l] >> 2); ++q) {
+        int4 t = src[q];
+        if (light_parts) {
+          t.x = light_or_inf(t.x, ub_light);
+          t.y = light_or_inf(t.y, ub_light);
+          t.z = light_or_inf(t.z, ub_light);
+          t.w = light_or_inf(t.w, ub_light);
+        }
+        dst[(4 * q) * NT] = t.x;
+        dst[(4 * q + 1) * NT] = t.y;
+        dst[(4 * q + 2) * NT] = t.z;
+        dst[(4 * q + 3) * NT] = t.w;
+      }
+    }
+    const uint32_t gm = __ldg(a.gmask + v);
+    int32_t dd[16];
+    if (ub > 0) load_label_bound(a, ub, (int32_t)v, dd);
+    int4* rowc = reinterpret_cast<int4*>(a.cost + a.base + v * a.stride);
+    int4* rowp = reinterpret_cast<int4*>(a.par + a.base + v * a.stride);
+    bool any = false;
+    for (int j0 = 0; j0 < a.stride; j0 += 4) {
+      int32_t b4[4], c4[4];
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        const int j = j0 + t;
+        int32_t best = kInf, code = kLeaf;
+        if (j < a.m) {
+          const uint32_t S = (uint32_t)__ldg(a.lmasks + j);
+          if ((gm & S) == S) best = 0;
+          const int32_t cap = ub > 0 ? ub - label_bound(dd, S) : kInf;
+          if (cap < 0) {
+            best = kInf;
+          } else if (best != 0) {
+            int win = -1;
+            const int i1 = sp[j + 1];
+            for (int i = sp[j]; i < i1; ++i) {
+              const int2 x = ss[i];
+              const int32_t c1 = col[x.x], c2 = col[x.y];
+              if (c1 < kInf && c2 < kInf) {
+                const int32_t c = c1 + c2;  // both < 2^30: no wrap
+                if (c >= ovf_limit)
+                  acc[2] = 1;
+                else if (c < best) {
+                  best = c;
+                  win = i;
+                }
+              }
+            }
+            acc[1] += i1 - sp[j];
+            if (win >= 0) {
+              const int2 x = a.msplits[win];
+              code = -__ldg(ml.lmasks_all + ml.mbase[x.x >> 24] + (x.x & 0xffffff));
+            }
+          }
+          if (best < kInf && best > cap) {
+            best = kInf;
+            code = kLeaf;
+          }
+        }
+        b4[t] = best;
+        c4[t] = code;
+        if (best < kInf) {
+          any = true;
+          ++acc[0];
+        }
+      }
+      rowc[j0 >> 2] = make_int4(b4[0], b4[1], b4[2], b4[3]);
+      rowp[j0 >> 2] = make_int4(c4[0], c4[1], c4[2], c4[3]);
+    }
+    if (any) flag2[v] = 1;
+  }
+  block_sum(acc);
+  if (threadIdx.x == 0) {
+    if (acc[0]) {
+      atomicAdd(&a.ctl->changed[2], (int32_t)acc[0]);
+      atomicAdd(&a.ctr->states, (unsigned long long)acc[0]);
+    }
+    if (a.params->stats_on) add_stat(a.stats, kStatSplits, acc[1]);
+    if (acc[2]) atomicExch(&a.ctr->overflow, 1);
+  }
+}
+
 __global__ void __launch_bounds__(kGrowThreads) k_merge_vertex(GraphDev g, LevelArgs a, MergeLevels ml) {
   extern __shared__ int32_t msm[];
   int32_t* sp = msm;                                                // m + 1
@@ -1280,6 +1404,19 @@ cudaError_t launch_group_masks(const int32_t* group_ptr, const int32_t* members,
 
 cudaError_t launch_merge(const GraphDev& g, const LevelArgs& a, const MergeLevels& ml, cudaStream_t stream) {
   if (a.k <= kMergeTabK && a.msplit_ptr) {
+    int32_t words = 0;  // lower-level row words per vertex
+    for (int l = 1; l < a.level; ++l) words += ml.stride[l];
+    if (words <= kMergeStagedWords) {
+      const size_t smem = (size_t)((a.m + 2) & ~1) * sizeof(int32_t) + (size_t)a.nsplits * sizeof(int2) +
+                          (size_t)words * kMergeStagedThreads * sizeof(int32_t);
+      if (smem > 48 * 1024) {  // up to ~72 KB (set on the current device every time)
+        const cudaError_t e = cudaFuncSetAttribute(k_merge_staged, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+      }
+      const int64_t blocks = ((int64_t)g.V + kMergeStagedThreads - 1) / kMergeStagedThreads;  // a thread per vertex
+      k_merge_staged<<<(unsigned)blocks, kMergeStagedThreads, smem, stream>>>(g, a, ml);
+      return cudaGetLastError();
+    }
     const size_t smem = (size_t)((a.m + 2) & ~1) * sizeof(int32_t) + (size_t)a.nsplits * sizeof(int2);
     if (smem > 48 * 1024) {  // k = 9, 10: up to ~60 KB (set on the current device every time)
       const cudaError_t e = cudaFuncSetAttribute(k_merge_vertex, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
