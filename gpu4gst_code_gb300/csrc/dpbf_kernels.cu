@@ -909,45 +909,18 @@ __device__ __forceinline__ bool thread_vertex(const GraphDev& g, const LevelArgs
   ++acc[kAccVert];
   acc[kAccEnt] += end - beg;
   if (!live) return false;
-  // software pipeline: the next batch's CSR entries (and, in sparse rounds,
-  // their change flags) are loaded while this batch's rows are gathered
-  int32_t nv[U], nw[U];
-  bool act[U];
-#pragma unroll
-  for (int i = 0; i < U; ++i) {
-    act[i] = beg + i < end;
-    nv[i] = 0;
-    nw[i] = 0;
-    if (act[i]) {
-      const int2 x = g.adj[beg + i];
-      nv[i] = x.x;
-      nw[i] = x.y;
-    }
-  }
-  if (!rs.dense) {
-#pragma unroll
-    for (int i = 0; i < U; ++i) act[i] = act[i] && rs.cur_flag[nv[i]] != 0;
-  }
-  for (int32_t e0 = beg; e0 < end; e0 += U) {
-    int32_t nv2[U], nw2[U];
-    bool act2[U];
-#pragma unroll
-    for (int i = 0; i < U; ++i) {
-      act2[i] = e0 + U + i < end;
-      nv2[i] = 0;
-      nw2[i] = 0;
-      if (act2[i]) {
-        const int2 x = g.adj[e0 + U + i];
-        nv2[i] = x.x;
-        nw2[i] = x.y;
-      }
-    }
+  // gathers the rows of up to U neighbours (slot i: ok, vertex, weight, CSR
+  // entry - beg) and folds them into best / code. A kInf (or heavy) row
+  // entry gives c >= kInf and never wins; rows hold values below ovf_limit
+  // (checked when stored), so c cannot wrap or reach kInf from a finite entry
+  auto relax_batch = [&](const bool (&ok)[U], const int32_t (&nvx)[U], const int32_t (&nwx)[U],
+                         const uint32_t (&rel)[U]) {
     int32_t rows[U][MP];
 #pragma unroll
     for (int i = 0; i < U; ++i) {
-      if (act[i]) {
+      if (ok[i]) {
         ++acc[kAccRows];
-        const int4* rv = reinterpret_cast<const int4*>(a.cost + a.base + (int64_t)nv[i] * MP);
+        const int4* rv = reinterpret_cast<const int4*>(a.cost + a.base + (int64_t)nvx[i] * MP);
 #pragma unroll
         for (int q = 0; q < Q; ++q) {
           const int4 x = rv[q];
@@ -961,30 +934,94 @@ __device__ __forceinline__ bool thread_vertex(const GraphDev& g, const LevelArgs
         for (int j = 0; j < MP; ++j) rows[i][j] = kInf;
       }
     }
-    // a kInf (or heavy) row entry gives c >= kInf and never wins; rows hold
-    // values below ovf_limit (checked when stored), so c cannot wrap or
-    // reach kInf from a finite entry
 #pragma unroll
     for (int i = 0; i < U; ++i) {
-      const uint32_t rel = (uint32_t)(e0 + i - beg);
 #pragma unroll
       for (int j = 0; j < MP; ++j) {
-        const int32_t c = light_or_inf(rows[i][j], rs.ub_light) + nw[i];
+        const int32_t c = light_or_inf(rows[i][j], rs.ub_light) + nwx[i];
         const bool lt = c < best[j];
         best[j] = lt ? c : best[j];
         const int sh = 8 * (j & 3);
-        code[j >> 2] = lt ? ((code[j >> 2] & ~(0xffu << sh)) | (rel << sh)) : code[j >> 2];
+        code[j >> 2] = lt ? ((code[j >> 2] & ~(0xffu << sh)) | (rel[i] << sh)) : code[j >> 2];
       }
     }
-    if (!rs.dense) {
-#pragma unroll
-      for (int i = 0; i < U; ++i) act2[i] = act2[i] && rs.cur_flag[nv2[i]] != 0;
-    }
+  };
+  if (rs.dense) {
+    // every neighbour; software pipeline: the next batch's CSR entries are
+    // loaded while this batch's rows are gathered
+    int32_t nv[U], nw[U];
+    bool act[U];
 #pragma unroll
     for (int i = 0; i < U; ++i) {
-      nv[i] = nv2[i];
-      nw[i] = nw2[i];
-      act[i] = act2[i];
+      act[i] = beg + i < end;
+      nv[i] = 0;
+      nw[i] = 0;
+      if (act[i]) {
+        const int2 x = g.adj[beg + i];
+        nv[i] = x.x;
+        nw[i] = x.y;
+      }
+    }
+    for (int32_t e0 = beg; e0 < end; e0 += U) {
+      int32_t nv2[U], nw2[U];
+      bool act2[U];
+#pragma unroll
+      for (int i = 0; i < U; ++i) {
+        act2[i] = e0 + U + i < end;
+        nv2[i] = 0;
+        nw2[i] = 0;
+        if (act2[i]) {
+          const int2 x = g.adj[e0 + U + i];
+          nv2[i] = x.x;
+          nw2[i] = x.y;
+        }
+      }
+      uint32_t rel[U];
+#pragma unroll
+      for (int i = 0; i < U; ++i) rel[i] = (uint32_t)(e0 + i - beg);
+      relax_batch(act, nv, nw, rel);
+#pragma unroll
+      for (int i = 0; i < U; ++i) {
+        nv[i] = nv2[i];
+        nw[i] = nw2[i];
+        act[i] = act2[i];
+      }
+    }
+  } else {
+    // sparse rounds: first the change flags of every CSR entry (8
+    // independent loads at a time) into a bit mask, then only the changed
+    // neighbours' rows, U at a time: the loop no longer waits on a flag
+    // load per pair of entries
+    uint64_t actm = 0;  // rows are at most kDegBigMax = 64 entries long
+    for (int32_t e0 = beg; e0 < end; e0 += 8) {
+      int32_t nb[8];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) nb[i] = e0 + i < end ? g.adj[e0 + i].x : -1;
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+        if (nb[i] >= 0 && rs.cur_flag[nb[i]] != 0) actm |= 1ull << (e0 + i - beg);  // e0 + i < end: shift < 64
+    }
+    while (actm) {
+      bool ok[U];
+      uint32_t rel[U];
+      int32_t nvx[U], nwx[U];
+#pragma unroll
+      for (int i = 0; i < U; ++i) {
+        ok[i] = actm != 0ull;
+        rel[i] = ok[i] ? (uint32_t)(__ffsll((long long)actm) - 1) : 0u;
+        if (ok[i]) actm &= actm - 1ull;
+        nvx[i] = 0;
+        nwx[i] = 0;
+      }
+#pragma unroll
+      for (int i = 0; i < U; ++i) {
+        if (ok[i]) {
+          const int2 x = g.adj[beg + (int32_t)rel[i]];
+          nvx[i] = x.x;
+          nwx[i] = x.y;
+        }
+      }
+      relax_batch(ok, nvx, nwx, rel);
     }
   }
   bool any = false;
