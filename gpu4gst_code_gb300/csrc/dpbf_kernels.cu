@@ -199,16 +199,18 @@ __global__ void __launch_bounds__(kGrowThreads) k_merge(GraphDev g, LevelArgs a)
 // its two row loads; the vertex's group mask and one-label bound are
 // loaded once; the row is written 16 bytes at a time.
 // Queries with at most kMergeStagedWords words of lower-level row per
-// vertex (k <= 7): a thread copies its vertex's rows of levels 1..l-1 into
+// vertex (k <= 8): a thread copies its vertex's rows of levels 1..l-1 into
 // shared memory once (light-filtered there when the merge uses light
 // parts), a column per thread, and every split then reads two shared words
 // at offsets precomputed into the block's copy of the split table, instead
-// of computing two global row addresses from the split's levels.
-constexpr int kMergeStagedThreads = 128;
-constexpr int kMergeStagedWords = 136;
+// of computing two global row addresses from the split's levels. Blocks of
+// NT threads: 128 up to kMergeStagedWords128 words, 64 beyond (at most
+// 64 KB of columns either way).
+constexpr int kMergeStagedWords128 = 136;  // k <= 7
+constexpr int kMergeStagedWords = 256;     // k = 8
 
-__global__ void __launch_bounds__(kMergeStagedThreads) k_merge_staged(GraphDev g, LevelArgs a, MergeLevels ml) {
-  constexpr int NT = kMergeStagedThreads;
+template <int NT>
+__global__ void __launch_bounds__(NT) k_merge_staged(GraphDev g, LevelArgs a, MergeLevels ml) {
   extern __shared__ int32_t msm[];
   __shared__ int32_t loff[kMergeTabK + 1];  // level l's first word in a vertex's staged rows
   int32_t* sp = msm;                                            // m + 1
@@ -1439,23 +1441,32 @@ cudaError_t launch_group_masks(const int32_t* group_ptr, const int32_t* members,
   return cudaGetLastError();
 }
 
+// Dynamic shared memory a launch may take without opting in: 48 KB less
+// the kernel's static shared memory (under 1 KB for the merge kernels).
+constexpr size_t kSmemNoOptIn = 47 * 1024;
+
 cudaError_t launch_merge(const GraphDev& g, const LevelArgs& a, const MergeLevels& ml, cudaStream_t stream) {
   if (a.k <= kMergeTabK && a.msplit_ptr) {
     int32_t words = 0;  // lower-level row words per vertex
     for (int l = 1; l < a.level; ++l) words += ml.stride[l];
     if (words <= kMergeStagedWords) {
+      const int nt = words <= kMergeStagedWords128 ? 128 : 64;
       const size_t smem = (size_t)((a.m + 2) & ~1) * sizeof(int32_t) + (size_t)a.nsplits * sizeof(int2) +
-                          (size_t)words * kMergeStagedThreads * sizeof(int32_t);
-      if (smem > 48 * 1024) {  // up to ~72 KB (set on the current device every time)
-        const cudaError_t e = cudaFuncSetAttribute(k_merge_staged, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                          (size_t)words * nt * sizeof(int32_t);
+      const void* fn = nt == 128 ? (const void*)k_merge_staged<128> : (const void*)k_merge_staged<64>;
+      if (smem > kSmemNoOptIn) {  // up to ~80 KB (set on the current device every time)
+        const cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
       }
-      const int64_t blocks = ((int64_t)g.V + kMergeStagedThreads - 1) / kMergeStagedThreads;  // a thread per vertex
-      k_merge_staged<<<(unsigned)blocks, kMergeStagedThreads, smem, stream>>>(g, a, ml);
+      const int64_t blocks = ((int64_t)g.V + nt - 1) / nt;  // a thread per vertex
+      if (nt == 128)
+        k_merge_staged<128><<<(unsigned)blocks, 128, smem, stream>>>(g, a, ml);
+      else
+        k_merge_staged<64><<<(unsigned)blocks, 64, smem, stream>>>(g, a, ml);
       return cudaGetLastError();
     }
     const size_t smem = (size_t)((a.m + 2) & ~1) * sizeof(int32_t) + (size_t)a.nsplits * sizeof(int2);
-    if (smem > 48 * 1024) {  // k = 9, 10: up to ~60 KB (set on the current device every time)
+    if (smem > kSmemNoOptIn) {  // k = 9, 10: up to ~60 KB (set on the current device every time)
       const cudaError_t e = cudaFuncSetAttribute(k_merge_vertex, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return e;
     }
