@@ -236,24 +236,27 @@ __global__ void __launch_bounds__(NT) k_merge_staged(GraphDev g, LevelArgs a, Me
   const bool light_parts = a.level < a.k;
   uint8_t* flag2 = a.flags + 2 * (int64_t)a.vpad;
   long long acc[3] = {0, 0, 0};  // finite states, splits, overflow
+  // staged costs are unsigned with "none" (kInf, or heavy when the merge
+  // uses light parts) as kStagedInf = 3 * 2^30: a sum of two finite costs
+  // (each below 2^30) stays below 2^31, any sum with a "none" is at least
+  // 2^31, and no sum wraps, so a split is two loads, an add and a min
+  constexpr uint32_t kStagedInf = 0xC0000000u;
+  auto staged = [&](int32_t c) -> int32_t {
+    return (int32_t)((light_parts ? light_or_inf(c, ub_light) : c) >= kInf ? kStagedInf : (uint32_t)c);
+  };
   const int64_t v = (int64_t)blockIdx.x * NT + threadIdx.x;
   if (v < g.V) {
     int32_t* col = rows + threadIdx.x;
+    const uint32_t* colu = reinterpret_cast<const uint32_t*>(col);
     for (int l = 1; l < a.level; ++l) {
       const int4* src = reinterpret_cast<const int4*>(a.cost + ml.off[l] + v * ml.stride[l]);
       int32_t* dst = col + loff[l] * NT;
       for (int q = 0; q < (ml.stride[l] >> 2); ++q) {
-        int4 t = src[q];
-        if (light_parts) {
-          t.x = light_or_inf(t.x, ub_light);
-          t.y = light_or_inf(t.y, ub_light);
-          t.z = light_or_inf(t.z, ub_light);
-          t.w = light_or_inf(t.w, ub_light);
-        }
-        dst[(4 * q) * NT] = t.x;
-        dst[(4 * q + 1) * NT] = t.y;
-        dst[(4 * q + 2) * NT] = t.z;
-        dst[(4 * q + 3) * NT] = t.w;
+        const int4 t = src[q];
+        dst[(4 * q) * NT] = staged(t.x);
+        dst[(4 * q + 1) * NT] = staged(t.y);
+        dst[(4 * q + 2) * NT] = staged(t.z);
+        dst[(4 * q + 3) * NT] = staged(t.w);
       }
     }
     const uint32_t gm = __ldg(a.gmask + v);
@@ -275,25 +278,26 @@ __global__ void __launch_bounds__(NT) k_merge_staged(GraphDev g, LevelArgs a, Me
           if (cap < 0) {
             best = kInf;
           } else if (best != 0) {
+            uint32_t bu = 0xffffffffu;
             int win = -1;
             const int i1 = sp[j + 1];
             for (int i = sp[j]; i < i1; ++i) {
               const int2 x = ss[i];
-              const int32_t c1 = col[x.x], c2 = col[x.y];
-              if (c1 < kInf && c2 < kInf) {
-                const int32_t c = c1 + c2;  // both < 2^30: no wrap
-                if (c >= ovf_limit)
-                  acc[2] = 1;
-                else if (c < best) {
-                  best = c;
-                  win = i;
-                }
+              const uint32_t c = colu[x.x] + colu[x.y];
+              if (c < bu) {
+                bu = c;
+                win = i;
               }
             }
             acc[1] += i1 - sp[j];
-            if (win >= 0) {
-              const int2 x = a.msplits[win];
-              code = -__ldg(ml.lmasks_all + ml.mbase[x.x >> 24] + (x.x & 0xffffff));
+            if (bu < 0x80000000u) {  // both parts finite
+              if (bu >= (uint32_t)ovf_limit) {
+                acc[2] = 1;  // the cheapest tree reaches the cost limit
+              } else {
+                best = (int32_t)bu;
+                const int2 x = a.msplits[win];
+                code = -__ldg(ml.lmasks_all + ml.mbase[x.x >> 24] + (x.x & 0xffffff));
+              }
             }
           }
           if (best < kInf && best > cap) {
