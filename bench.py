@@ -182,7 +182,7 @@ class ClockSampler:
 # DRAM bytes (read + write) of all growth-kernel launches of one plain
 # query, summed from one ncu capture per workload (profiles/); None where
 # no capture exists.
-TRAFFIC_PER_STEP = {"ba1m_k6": 9.21e9}  # profiles/grow_dram_ba1m_k6.md
+TRAFFIC_PER_STEP = {"ba1m_k6": 9.18e9}  # profiles/grow_dram_ba1m_k6.md
 
 
 def table_bytes(V, k):
