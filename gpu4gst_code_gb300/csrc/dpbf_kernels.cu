@@ -842,9 +842,13 @@ __global__ void __launch_bounds__(kGrowThreads) k_seed(GraphDev g, LevelArgs a) 
                      [&](int j) { return yu[j]; }, a.m))
       mark_candidate(cand0, x.x, acc);
   };
+  // the merge flagged every vertex with a finite state (flag array 2): only
+  // those rows are read
+  const uint8_t* merged = a.flags + 2 * (int64_t)a.vpad;
   for (int64_t c = warp; c < g.nchunks; c += nwarps) {
+    const int32_t u = g.chunk_vtx[c];
+    if (!merged[u]) continue;
     const int2 hc = g.hub_chunk[c];
-    const int32_t u = g.big[hc.x];
     const int32_t* hv = a.cost + a.base + (int64_t)u * s;
     bool light = false;
     for (int j = lane; j < a.m; j += 32) light |= light_or_inf(hv[j], ub_light) < kInf;
@@ -855,7 +859,7 @@ __global__ void __launch_bounds__(kGrowThreads) k_seed(GraphDev g, LevelArgs a) 
   for (int64_t vbase = warp * 32; vbase < g.V; vbase += nwarps * 32) {
     const int64_t vl = vbase + lane;
     bool light = false;
-    if (vl < g.V && g.row_ptr[vl + 1] - g.row_ptr[vl] <= g.deg_big) {
+    if (vl < g.V && merged[vl] && g.row_ptr[vl + 1] - g.row_ptr[vl] <= g.deg_big) {
       const int32_t* hv = a.cost + a.base + vl * s;
       for (int j = 0; j < a.m; ++j) light |= light_or_inf(hv[j], ub_light) < kInf;
     }

@@ -630,7 +630,9 @@ gst_status build_query_graph(gst_graph* g, int32_t k) {
     if (st == GST_OK && cudaEventRecord(ws.ev[3 * l + 1], s) != cudaSuccess)
       st = fail(GST_CUDA_ERROR, "event record");
     if (st == GST_OK && l < k) st = capture_growth_loop(g, a, s);
-    if (st == GST_OK && l < k && launch_ub_refine(graph_dev(g), a, g->num_sms, s) != cudaSuccess)
+    // refinement after the last grown wave would only tighten the final
+    // merge's cap, and the final merge evaluates every split either way
+    if (st == GST_OK && l < k - 1 && launch_ub_refine(graph_dev(g), a, g->num_sms, s) != cudaSuccess)
       st = fail(GST_CUDA_ERROR, "bound refinement launch");
     if (st == GST_OK && cudaEventRecord(ws.ev[3 * l + 2], s) != cudaSuccess)
       st = fail(GST_CUDA_ERROR, "event record");
@@ -782,8 +784,10 @@ gst_status run_host_loop(gst_graph* g, int32_t k, int64_t* launches, bool* timeo
         }
         if (ws.h_ctl->last_changed == 0) break;
       }
-      GST_CUDA(launch_ub_refine(gd, a, g->num_sms, s));
-      ++*launches;
+      if (l < k - 1) {  // not after the last grown wave (see build_query_graph)
+        GST_CUDA(launch_ub_refine(gd, a, g->num_sms, s));
+        ++*launches;
+      }
     }
     GST_CUDA(cudaEventRecord(ws.ev[3 * l + 2], s));
   }
@@ -842,7 +846,10 @@ gst_status solve_one(gst_graph* g, const int32_t* group_ptr, const int32_t* memb
   GST_CUDA(cudaEventRecord(ws.ev[2], s));
   GST_CUDA(cudaStreamSynchronize(s));
   const Counters& c = *ws.h_ctr;
-  if (use_graph) launches = 1 + k + 2 * (k - 1) + (int64_t)c.rounds_total * (g->nchunks > 0 ? 2 : 1) + 2;
+  // masks, k merges, a seed per grown wave, a refinement per grown wave but
+  // the last, the rounds, argmin and backtrack
+  if (use_graph)
+    launches = 1 + k + (k - 1) + std::max(k - 2, 0) + (int64_t)c.rounds_total * (g->nchunks > 0 ? 2 : 1) + 2;
   r->ub = ws.h_params->ub;  // the bound as the last wave saw it (refined on the device)
   r->launches = launches;
   r->states = (int64_t)c.states;
@@ -1213,7 +1220,7 @@ gst_status propose_tree(gst_graph* g, const gst_scorer* sc, const int32_t* group
     st = GST_OK;
     g_last_error.clear();
     // a capped solve stops before its epilogue: the round loop's launches
-    tmp.launches = 1 + 2 + 2 * 1 + (int64_t)kProposeRounds * (g->nchunks > 0 ? 2 : 1);
+    tmp.launches = 1 + 2 + 1 + (int64_t)kProposeRounds * (g->nchunks > 0 ? 2 : 1);
   }
   if (st != GST_OK) return st;
   launches += tmp.launches + 1;  // + the path walk
