@@ -712,6 +712,7 @@ __device__ __forceinline__ void hub_chunk_relax(const GraphDev& g, const LevelAr
   const int32_t beg = g.row_ptr[u], end = g.row_ptr[u + 1];
   const int32_t cend = min(end, hc.y + G);
   unsigned long long* hm = g.hub_min + (int64_t)hc.x * g.hub_stride;
+  bool folded = false;  // this lane folded a minimum into the scratch row
   for (int jc = 0; jc < s; jc += CH) {
     int32_t best[L], code[L];
 #pragma unroll
@@ -723,12 +724,16 @@ __device__ __forceinline__ void hub_chunk_relax(const GraphDev& g, const LevelAr
 #pragma unroll
     for (int t = 0; t < L; ++t) {
       const int j = jc + lane + t * G;
-      if (j < s && best[t] < kInf)
+      if (j < s && best[t] < kInf) {
         atomicMin(hm + j, ((unsigned long long)(uint32_t)best[t] << 32) | (uint32_t)code[t]);
+        folded = true;
+      }
     }
   }
   if (lane == 0) acc[kAccEnt] += cend - hc.y;
-  __threadfence();
+  // the folded minima must be visible before the chunk counts as done; a
+  // chunk that folded nothing has nothing to order
+  if (__any_sync(0xffffffffu, folded)) __threadfence();
   int last = 0;
   if (lane == 0) last = atomicAdd(g.hub_cnt + hc.x, 1) == (end - beg + G - 1) / G - 1;
   last = __shfl_sync(0xffffffffu, last, 0);
@@ -1306,20 +1311,26 @@ __global__ void __launch_bounds__(kGrowThreads) k_ub_refine(GraphDev g, LevelArg
     int32_t dd[16];
 #pragma unroll
     for (int gg = 0; gg < 16; ++gg) dd[gg] = gg < a.k ? d[gg] : 0;
-    const int32_t* row = a.cost + a.base + v * a.stride;
-    for (int j = 0; j < a.m; ++j) {
-      const int32_t c = row[j];
-      if (c >= kInf) continue;
-      const uint32_t S = (uint32_t)__ldg(a.lmasks + j);
-      long long sum = c;
-      bool ok = true;
+    const int4* row = reinterpret_cast<const int4*>(a.cost + a.base + v * a.stride);  // rows are 16-byte aligned
+    for (int j0 = 0; j0 < a.m; j0 += 4) {
+      const int4 q = row[j0 >> 2];
+      const int32_t c4[4] = {q.x, q.y, q.z, q.w};
 #pragma unroll
-      for (int gg = 0; gg < 16; ++gg)
-        if (gg < a.k && !((S >> gg) & 1u)) {
-          ok &= dd[gg] < kInf;
-          sum += dd[gg];
-        }
-      if (ok && sum < best) best = sum;
+      for (int t = 0; t < 4; ++t) {
+        const int j = j0 + t;
+        const int32_t c = c4[t];
+        if (j >= a.m || c >= kInf) continue;
+        const uint32_t S = (uint32_t)__ldg(a.lmasks + j);
+        long long sum = c;
+        bool ok = true;
+#pragma unroll
+        for (int gg = 0; gg < 16; ++gg)
+          if (gg < a.k && !((S >> gg) & 1u)) {
+            ok &= dd[gg] < kInf;
+            sum += dd[gg];
+          }
+        if (ok && sum < best) best = sum;
+      }
     }
   }
 #pragma unroll
