@@ -38,6 +38,7 @@ constexpr int kCandTile = 256;
 // Dense rounds when the previous round changed more than V >> this
 // (sparse rounds with marking stay cheaper up to about half the graph).
 constexpr int kDefaultDenseShift = 1;
+constexpr int kDefaultDenseShiftPruned = 2;  // solves with a bound or bound refinement
 
 __host__ __device__ constexpr int32_t row_stride(int32_t m) { return (m + 3) & ~3; }
 

@@ -821,8 +821,12 @@ gst_status solve_one(gst_graph* g, const int32_t* group_ptr, const int32_t* memb
   ws.h_params->ovf_limit = kInf - std::max<int32_t>(g->max_w, 1);
   const gst_graph* tg = g->parent ? g->parent : g;
   const int32_t tuned = tg->tuned_shift[k];
+  // default threshold: V/2 unpruned; V/4 when the solve prunes (fewer rows
+  // change per round, so sparse rounds stay cheaper for longer)
+  const bool pruned = o.refine_bound != 0 || o.upper_bound > 0;
   ws.h_params->dense_shift = o.dense_shift > 0 && o.dense_shift < 31 ? o.dense_shift
                              : tuned > 0                              ? tuned
+                             : pruned                                 ? kDefaultDenseShiftPruned
                                                                       : kDefaultDenseShift;
   ws.h_params->refine = o.refine_bound ? 1 : 0;
 

@@ -70,8 +70,9 @@ typedef struct gst_opts {
   int32_t collect_stats;
   /* A growth round runs dense (every vertex, every neighbour row, no
    * candidate marks) when the previous round changed more than
-   * V >> dense_shift vertices; 0 = the default (1). A tuning knob only:
-   * results do not depend on it. */
+   * V >> dense_shift vertices; 0 = the default (1; 2 when the solve prunes
+   * with upper_bound or refine_bound, or the value gst_autotune chose for
+   * this k). A tuning knob only: results do not depend on it. */
   int32_t dense_shift;
   /* 1 = after every DP wave, lower the pruning bound to the cheapest
    * feasible subgraph seen so far: a state T(v,S) plus v's shortest paths
