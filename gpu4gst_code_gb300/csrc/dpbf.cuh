@@ -147,7 +147,19 @@ struct LevelArgs {
   int32_t nsplits;
   cudaGraphConditionalHandle cond;  // while-loop handle when captured
   int32_t use_cond;
+  // pruning caps of this level's states, written by the merge when a bound
+  // exists (level >= 2): cap(v,S) = ub - LB(v, groups outside S), rows of
+  // stride `stride`; growth keeps a state only if its cost is <= its cap
+  int32_t* capt;
+  // tour table of the PrunedDP++ tour bound (k <= kTourMaxK, 2 <= level < k;
+  // null otherwise): path[(i << k | X) * k + j] = the cheapest order of
+  // visiting the groups of X from group i to group j, over lower bounds of
+  // the group-to-group distances, clamped at the bound
+  const int32_t* tour;
 };
+
+// Groups up to which the merge adds the tour bound to the one-label bound.
+constexpr int kTourMaxK = 7;
 
 // Queries with at most kMergeTabK groups merge a vertex per thread from
 // per-level split tables (k_merge_vertex); larger k use k_merge.
@@ -171,6 +183,10 @@ cudaError_t launch_merge(const GraphDev& g, const LevelArgs& a, const MergeLevel
 cudaError_t launch_grow_round(const GraphDev& g, const LevelArgs& a, int num_sms, cudaStream_t stream,
                               int64_t* launches);
 cudaError_t launch_seed(const GraphDev& g, const LevelArgs& a, int num_sms, cudaStream_t stream);
+// Before wave a.level's merge (a.tour non-null): the tour table for the
+// current bound, from wave 1's distances of the query's members.
+cudaError_t launch_tour_table(const LevelArgs& a, const int32_t* group_ptr, const int32_t* members,
+                              const int32_t* perm, int32_t* tour, cudaStream_t stream);
 // After wave a.level's growth: with params->refine set, lowers params->ub to
 // the cheapest T(v,S) + sum of T(v,{g}) over the groups g outside S.
 cudaError_t launch_ub_refine(const GraphDev& g, const LevelArgs& a, int num_sms, cudaStream_t stream);

@@ -120,6 +120,12 @@ __device__ __forceinline__ int32_t label_bound(const int32_t (&dd)[16], uint32_t
   return lb;
 }
 
+// Growth under a bound (waves >= 2): the cap of state (v, mask rank j) that
+// the wave's merge wrote (read-only during the wave).
+__device__ __forceinline__ int32_t cap_at(const LevelArgs& a, int32_t v, int j) {
+  return __ldg(a.capt + (int64_t)v * a.stride + j);
+}
+
 // ------------------------------------------------------------------ merge --
 // One thread per (v, slot) of the level's rows: T(v,S) = 0 when S is inside
 // groups(v), else the best split T(v,S1) + T(v,S^S1) over S1 holding the
@@ -140,12 +146,13 @@ __global__ void __launch_bounds__(kGrowThreads) k_merge(GraphDev g, LevelArgs a)
     const int32_t j = (int32_t)(idx - (int64_t)v * a.stride);
     int32_t best = kInf;
     int32_t code = kLeaf;
+    int32_t cap = -1;  // padding slots: nothing fits
     if (j < a.m) {
       const uint32_t S = (uint32_t)__ldg(a.lmasks + j);
       if ((__ldg(a.gmask + v) & S) == S) best = 0;
       // under a bound, a state whose lower bound alone exceeds it is dead:
       // no split needs enumerating
-      const int32_t cap = (ub > 0 && a.level >= 2) ? prune_cap(a, ub, v, S) : kInf;
+      cap = (ub > 0 && a.level >= 2) ? prune_cap(a, ub, v, S) : kInf;
       if (cap < 0) best = kInf;
       if (a.level >= 2 && best != 0 && cap >= 0) {
         const uint32_t low = S & (0u - S), rest = S ^ low;
@@ -178,6 +185,7 @@ __global__ void __launch_bounds__(kGrowThreads) k_merge(GraphDev g, LevelArgs a)
     }
     a.cost[a.base + idx] = best;
     a.par[a.base + idx] = code;
+    if (ub > 0) a.capt[idx] = cap;  // the growth of this wave prunes by it
     if (best < kInf) {
       flag2[v] = 1;
       ++acc[0];
@@ -262,19 +270,45 @@ __global__ void __launch_bounds__(NT) k_merge_staged(GraphDev g, LevelArgs a, Me
     const uint32_t gm = __ldg(a.gmask + v);
     int32_t dd[16];
     if (ub > 0) load_label_bound(a, ub, (int32_t)v, dd);
+    // the tour bound reads wave 1's distances from the staged level-1 row
+    // (words 0..k-1): light ones are exact, the others exceed ub / 2, so
+    // min(staged, ub / 2 + 1) is dd with a runtime index
+    const uint32_t beyond = (uint32_t)(ub / 2 + 1);
+    const uint32_t full = (1u << a.k) - 1u;
     int4* rowc = reinterpret_cast<int4*>(a.cost + a.base + v * a.stride);
     int4* rowp = reinterpret_cast<int4*>(a.par + a.base + v * a.stride);
+    int4* rowk = reinterpret_cast<int4*>(a.capt + v * a.stride);
     bool any = false;
     for (int j0 = 0; j0 < a.stride; j0 += 4) {
-      int32_t b4[4], c4[4];
+      int32_t b4[4], c4[4], k4[4];
 #pragma unroll
       for (int t = 0; t < 4; ++t) {
         const int j = j0 + t;
         int32_t best = kInf, code = kLeaf;
+        k4[t] = -1;  // padding slots: nothing fits
         if (j < a.m) {
           const uint32_t S = (uint32_t)__ldg(a.lmasks + j);
           if ((gm & S) == S) best = 0;
-          const int32_t cap = ub > 0 ? ub - label_bound(dd, S) : kInf;
+          int32_t lb = ub > 0 ? label_bound(dd, S) : 0;
+          const uint32_t X = full ^ S;
+          if (ub > 0 && a.tour && __popc(X) >= 2) {
+            // PrunedDP++'s tour bound (graph_v_of_v_idealID_PrunedDPPlusPlus.h:268-386):
+            // a tree joining v to the groups of X is at least half a walk
+            // from v through all of them, over lower bounds of every leg
+            int32_t lb1 = INT_MAX;
+            for (uint32_t xi = X; xi; xi &= xi - 1u) {
+              const int i = __ffs(xi) - 1;
+              const int32_t di = (int32_t)min(colu[i * NT], beyond);
+              const int32_t* fi = a.tour + (((int64_t)i << a.k) | X) * a.k;
+              for (uint32_t xj = X; xj; xj &= xj - 1u) {
+                const int i2 = __ffs(xj) - 1;
+                lb1 = min(lb1, (di + __ldg(fi + i2) + (int32_t)min(colu[i2 * NT], beyond)) >> 1);
+              }
+            }
+            lb = max(lb, lb1);
+          }
+          const int32_t cap = ub > 0 ? ub - lb : kInf;
+          k4[t] = cap < 0 ? -1 : cap;
           if (cap < 0) {
             best = kInf;
           } else if (best != 0) {
@@ -314,6 +348,7 @@ __global__ void __launch_bounds__(NT) k_merge_staged(GraphDev g, LevelArgs a, Me
       }
       rowc[j0 >> 2] = make_int4(b4[0], b4[1], b4[2], b4[3]);
       rowp[j0 >> 2] = make_int4(c4[0], c4[1], c4[2], c4[3]);
+      if (ub > 0) rowk[j0 >> 2] = make_int4(k4[0], k4[1], k4[2], k4[3]);  // the growth of this wave prunes by it
     }
     if (any) flag2[v] = 1;
   }
@@ -347,17 +382,20 @@ __global__ void __launch_bounds__(kGrowThreads) k_merge_vertex(GraphDev g, Level
     if (ub > 0) load_label_bound(a, ub, (int32_t)v, dd);
     int4* rowc = reinterpret_cast<int4*>(a.cost + a.base + v * a.stride);
     int4* rowp = reinterpret_cast<int4*>(a.par + a.base + v * a.stride);
+    int4* rowk = reinterpret_cast<int4*>(a.capt + v * a.stride);
     bool any = false;
     for (int j0 = 0; j0 < a.stride; j0 += 4) {
-      int32_t b4[4], c4[4];
+      int32_t b4[4], c4[4], k4[4];
 #pragma unroll
       for (int t = 0; t < 4; ++t) {
         const int j = j0 + t;
         int32_t best = kInf, code = kLeaf;
+        k4[t] = -1;  // padding slots: nothing fits
         if (j < a.m) {
           const uint32_t S = (uint32_t)__ldg(a.lmasks + j);
           if ((gm & S) == S) best = 0;
           const int32_t cap = ub > 0 ? ub - label_bound(dd, S) : kInf;
+          k4[t] = cap < 0 ? -1 : cap;
           if (cap < 0) {
             best = kInf;
           } else if (best != 0) {
@@ -401,6 +439,7 @@ __global__ void __launch_bounds__(kGrowThreads) k_merge_vertex(GraphDev g, Level
       }
       rowc[j0 >> 2] = make_int4(b4[0], b4[1], b4[2], b4[3]);
       rowp[j0 >> 2] = make_int4(c4[0], c4[1], c4[2], c4[3]);
+      if (ub > 0) rowk[j0 >> 2] = make_int4(k4[0], k4[1], k4[2], k4[3]);  // the growth of this wave prunes by it
     }
     if (any) flag2[v] = 1;
   }
@@ -523,12 +562,10 @@ __device__ __forceinline__ bool improves_row(const LevelArgs& a, int32_t ub, int
     for (int jj = 0; jj < n; ++jj) bits |= (vals(j0 + jj) + w < y(j0 + jj) ? 1u : 0u) << jj;
     if (!bits) continue;
     if (ub <= 0) return true;
-    int32_t dd[16];
-    load_label_bound(a, ub, v, dd);
     while (bits) {
       const int j = j0 + __ffs(bits) - 1;
       bits &= bits - 1u;
-      if (vals(j) + w + label_bound(dd, (uint32_t)__ldg(a.lmasks + j)) <= ub) return true;
+      if (vals(j) + w <= cap_at(a, v, j)) return true;
     }
   }
   return false;
@@ -747,7 +784,7 @@ __device__ __forceinline__ void hub_chunk_relax(const GraphDev& g, const LevelAr
     const int32_t c2 = (int32_t)(r >> 32);
     const int32_t own = a.cost[rowu + j];
     if (c2 >= own) continue;
-    if (rs.ub > 0 && c2 > prune_cap(a, rs.ub, u, (uint32_t)__ldg(a.lmasks + j))) continue;
+    if (rs.ub > 0 && c2 > cap_at(a, u, j)) continue;
     a.cost[rowu + j] = c2;
     a.par[rowu + j] = (int32_t)(uint32_t)(r & 0xffffffffull);
     imp = true;
@@ -1045,7 +1082,7 @@ __device__ __forceinline__ bool thread_vertex(const GraphDev& g, const LevelArgs
     const int sh = 8 * (j & 3);
     const bool imp = ((code[j >> 2] >> sh) & 0xffu) != 0xffu;
     if (imp && best[j] >= rs.ovf_limit) acc[kAccOverflow] = 1;
-    if (imp && rs.ub > 0 && best[j] > prune_cap(a, rs.ub, u, (uint32_t)__ldg(a.lmasks + j))) {
+    if (imp && rs.ub > 0 && best[j] > cap_at(a, u, j)) {
       best[j] = a.cost[a.base + (int64_t)u * MP + j];  // keep the stored value
       code[j >> 2] |= 0xffu << sh;
     }
@@ -1111,15 +1148,13 @@ __device__ __forceinline__ void warp_mark(const GraphDev& g, const LevelArgs& a,
         bits |= (light_or_inf(h.w, rs.ub_light) + x.y < t.w ? 1u : 0u) << (4 * q + 3);
       }
       bool better = bits != 0;
-      if (better && rs.ub > 0) {  // the same test under x's one-label caps
-        int32_t dd[16];
-        load_label_bound(a, rs.ub, x.x, dd);
+      if (better && rs.ub > 0) {  // the same test under x's caps
         better = false;
         const int32_t* wj = a.cost + a.base + (int64_t)w * MP;
         while (bits && !better) {
           const int j = __ffs(bits) - 1;
           bits &= bits - 1u;
-          better = light_or_inf(wj[j], rs.ub_light) + x.y + label_bound(dd, (uint32_t)__ldg(a.lmasks + j)) <= rs.ub;
+          better = light_or_inf(wj[j], rs.ub_light) + x.y <= cap_at(a, x.x, j);
         }
       }
       if (better) mark_candidate(rs.cand_next, x.x, acc);
@@ -1269,7 +1304,7 @@ __global__ void __launch_bounds__(kGrowThreads, (L >= 3 ? 3 : 4)) k_grow_group(G
           for (int t = 0; t < L; ++t) {
             const int j = jc + glane + t * G;
             if (j < a.m && best[t] < own[t]) {
-              if (rs.ub > 0 && best[t] > prune_cap(a, rs.ub, u, (uint32_t)__ldg(a.lmasks + j))) continue;
+              if (rs.ub > 0 && best[t] > cap_at(a, u, j)) continue;
               a.cost[rowu + j] = best[t];
               a.par[rowu + j] = code[t];
               imp = true;
@@ -1354,6 +1389,58 @@ __global__ void __launch_bounds__(kGrowThreads) k_ub_refine(GraphDev g, LevelArg
 }
 
 // ----------------------------------------------------------------- argmin --
+// ------------------------------------------------------------ tour table --
+// Lower bounds of the group-to-group distances: D[a][b] = the smallest
+// min(T(m,{a}), ub/2 + 1) over the members m of group b (wave 1's
+// distances; light ones are exact and heavy ones exceed ub/2, so the min
+// bounds the distance from below either way), made symmetric with the
+// larger of D[a][b] and D[b][a] (both bound the same distance). Then
+// path[i][X][j] = the cheapest order of visiting every group of X from
+// group i to group j over legs D, by subsets of growing size, clamped at
+// ub (a clamp only lowers the bound); orders that do not exist keep the
+// clamp. The tables of PrunedDP++'s tour bound
+// (graph_v_of_v_idealID_PrunedDPPlusPlus.h:268-386) for this query's
+// groups, rebuilt before every merge because the bound may have dropped.
+__global__ void __launch_bounds__(256) k_tour_table(LevelArgs a, const int32_t* __restrict__ group_ptr,
+                                                    const int32_t* __restrict__ members,
+                                                    const int32_t* __restrict__ perm, int32_t* __restrict__ tour) {
+  constexpr int KM = kTourMaxK;
+  __shared__ int32_t D[KM][KM];
+  __shared__ int32_t F[KM * (1 << KM) * KM];
+  const int32_t ub = a.params->ub;
+  if (ub <= 0) return;  // no bound: the merge does not read the table
+  const int k = a.k, W = 1 << k, kk = k * k;
+  const int32_t beyond = ub / 2 + 1;
+  for (int t = threadIdx.x; t < KM * KM; t += blockDim.x) D[t / KM][t % KM] = beyond;
+  for (int t = threadIdx.x; t < k * W * k; t += blockDim.x) F[t] = ub;
+  __syncthreads();
+  for (int b = 0; b < k; ++b)
+    for (int32_t i = group_ptr[b] + threadIdx.x; i < group_ptr[b + 1]; i += blockDim.x) {
+      const int32_t* d = a.cost + (int64_t)perm[members[i]] * a.stride1;  // wave 1: rank of {g} is g
+      for (int g2 = 0; g2 < k; ++g2) atomicMin(&D[g2][b], min(d[g2], beyond));
+    }
+  __syncthreads();
+  int32_t sym = 0;
+  if (threadIdx.x < kk) sym = max(D[threadIdx.x / k][threadIdx.x % k], D[threadIdx.x % k][threadIdx.x / k]);
+  __syncthreads();
+  if (threadIdx.x < kk) D[threadIdx.x / k][threadIdx.x % k] = sym;
+  if (threadIdx.x < k) F[((threadIdx.x << k) | (1 << threadIdx.x)) * k + threadIdx.x] = 0;
+  __syncthreads();
+  for (int p = 2; p <= k; ++p) {  // subsets of p groups from those of p - 1
+    for (int t = threadIdx.x; t < W * kk; t += blockDim.x) {
+      const int X = t / kk, i = (t / k) % k, j = t % k;
+      if (__popc(X) != p || !((X >> i) & 1) || !((X >> j) & 1) || i == j) continue;
+      const int prev = X ^ (1 << j);
+      int32_t best = ub;
+      for (int l = 0; l < k; ++l)
+        if ((prev >> l) & 1) best = min(best, F[((i << k) | prev) * k + l] + D[l][j]);  // both <= ub < 2^30
+      F[((i << k) | X) * k + j] = best;
+    }
+    __syncthreads();
+  }
+  for (int t = threadIdx.x; t < k * W * k; t += blockDim.x) tour[t] = F[t];
+}
+
 __global__ void k_argmin(int32_t V, const int32_t* __restrict__ full_slice, int32_t stride, Counters* ctr) {
   unsigned long long best = ~0ull;
   for (int32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
@@ -1568,6 +1655,13 @@ cudaError_t launch_grow_round(const GraphDev& g, const LevelArgs& a, int num_sms
   if (a.stride <= 64) return group_round<32, 2>(g, a, num_sms, stream);
   if (a.stride <= 96) return group_round<32, 3>(g, a, num_sms, stream);
   return group_round<32, 4>(g, a, num_sms, stream);
+}
+
+cudaError_t launch_tour_table(const LevelArgs& a, const int32_t* group_ptr, const int32_t* members,
+                              const int32_t* perm, int32_t* tour, cudaStream_t stream) {
+  if (a.k > kTourMaxK) return cudaErrorInvalidValue;
+  k_tour_table<<<1, 256, 0, stream>>>(a, group_ptr, members, perm, tour);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_seed(const GraphDev& g, const LevelArgs& a, int num_sms, cudaStream_t stream) {

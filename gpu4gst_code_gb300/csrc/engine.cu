@@ -125,6 +125,8 @@ struct Workspace {
   unsigned long long* hub_min = nullptr;  // nbig x hub_stride scratch minima
   int32_t* hub_cnt = nullptr;             // nbig chunk counters
   int32_t hub_stride = 0;
+  int32_t* capt = nullptr;  // V x the widest row stride: the current wave's pruning caps
+  int32_t* tour = nullptr;  // kTourMaxK x 2^kTourMaxK x kTourMaxK tour-bound table
   // pinned host mirrors
   Counters* h_ctr = nullptr;
   GrowCtl* h_ctl = nullptr;
@@ -318,6 +320,8 @@ void free_workspace(Workspace& ws) {
   dfree(ws.out_e);
   dfree(ws.hub_min);
   dfree(ws.hub_cnt);
+  dfree(ws.capt);
+  dfree(ws.tour);
   for (void* p : {(void*)ws.h_ctr, (void*)ws.h_ctl, (void*)ws.h_params, (void*)ws.h_stats, (void*)ws.h_out_v,
                   (void*)ws.h_out_e})
     if (p) cudaFreeHost(p);
@@ -377,6 +381,7 @@ gst_status ensure_workspace(gst_graph* g, int32_t k, int64_t nmembers) {
     GST_CUDA(cudaMalloc(&ws.qb, (size_t)ws.bt_cap * sizeof(int2)));
     GST_CUDA(cudaMalloc(&ws.out_v, (size_t)ws.bt_cap * sizeof(int32_t)));
     GST_CUDA(cudaMalloc(&ws.out_e, (size_t)ws.bt_cap * sizeof(int3)));
+    GST_CUDA(cudaMalloc(&ws.tour, (size_t)kTourMaxK * (1 << kTourMaxK) * kTourMaxK * sizeof(int32_t)));
   }
   if (k > ws.k_cap) {
     dfree(ws.cost);
@@ -388,8 +393,10 @@ gst_status ensure_workspace(gst_graph* g, int32_t k, int64_t nmembers) {
     GST_CUDA(cudaMalloc(&ws.par, entries * sizeof(int32_t)));
     dfree(ws.hub_min);
     dfree(ws.hub_cnt);
+    dfree(ws.capt);
     int32_t smax = 4;
     for (int l = 1; l <= k; ++l) smax = std::max(smax, row_stride(binom(k, l)));
+    GST_CUDA(cudaMalloc(&ws.capt, (size_t)V * smax * sizeof(int32_t)));
     ws.hub_stride = smax;
     const size_t nh = std::max<size_t>(1, (size_t)g->nbig);
     GST_CUDA(cudaMalloc(&ws.hub_min, nh * (size_t)smax * sizeof(unsigned long long)));
@@ -516,6 +523,8 @@ LevelArgs level_args(gst_graph* g, int32_t k, int32_t l) {
   a.msplits = k <= kMergeTabK ? ws.msplits + ws.h_ms_off[l] : nullptr;
   a.nsplits = k <= kMergeTabK ? ws.h_ms_n[l] : 0;
   a.use_cond = 0;
+  a.capt = ws.capt;
+  a.tour = (k <= kTourMaxK && l >= 2 && l < k) ? ws.tour : nullptr;  // the last merge has no groups left
   return a;
 }
 
@@ -552,6 +561,10 @@ gst_status enqueue_merge(gst_graph* g, const LevelArgs& a, cudaStream_t s, int64
   Workspace& ws = g->ws;
   GST_CUDA(cudaMemsetAsync(ws.flags, 0, 6 * (size_t)vpad_of(g->V), s));
   GST_CUDA(cudaMemsetAsync(ws.ctl, 0, sizeof(GrowCtl), s));
+  if (a.tour) {  // the tour bound's tables for the bound as it stands now (no-op without one)
+    GST_CUDA(launch_tour_table(a, ws.d_group_ptr, ws.d_members, g->d_perm, ws.tour, s));
+    ++*launches;
+  }
   GST_CUDA(launch_merge(graph_dev(g), a, merge_levels(g, a.k), s));
   ++*launches;
   if (a.level < a.k) {  // how round 0 of the wave starts
@@ -851,9 +864,11 @@ gst_status solve_one(gst_graph* g, const int32_t* group_ptr, const int32_t* memb
   GST_CUDA(cudaStreamSynchronize(s));
   const Counters& c = *ws.h_ctr;
   // masks, k merges, a seed per grown wave, a refinement per grown wave but
-  // the last, the rounds, argmin and backtrack
+  // the last, the tour tables (k <= kTourMaxK, waves 2..k-1), the rounds,
+  // argmin and backtrack
   if (use_graph)
-    launches = 1 + k + (k - 1) + std::max(k - 2, 0) + (int64_t)c.rounds_total * (g->nchunks > 0 ? 2 : 1) + 2;
+    launches = 1 + k + (k - 1) + std::max(k - 2, 0) + (k <= kTourMaxK ? std::max(k - 2, 0) : 0) +
+               (int64_t)c.rounds_total * (g->nchunks > 0 ? 2 : 1) + 2;
   r->ub = ws.h_params->ub;  // the bound as the last wave saw it (refined on the device)
   r->launches = launches;
   r->states = (int64_t)c.states;
