@@ -158,8 +158,9 @@ struct LevelArgs {
   const int32_t* tour;
 };
 
-// Groups up to which the merge adds the tour bound to the one-label bound.
-constexpr int kTourMaxK = 7;
+// Groups up to which the merge adds the tour bound to the one-label bound
+// (the staged merge's limit).
+constexpr int kTourMaxK = 8;
 
 // Queries with at most kMergeTabK groups merge a vertex per thread from
 // per-level split tables (k_merge_vertex); larger k use k_merge.

@@ -1406,7 +1406,7 @@ __global__ void __launch_bounds__(256) k_tour_table(LevelArgs a, const int32_t* 
                                                     const int32_t* __restrict__ perm, int32_t* __restrict__ tour) {
   constexpr int KM = kTourMaxK;
   __shared__ int32_t D[KM][KM];
-  __shared__ int32_t F[KM * (1 << KM) * KM];
+  extern __shared__ int32_t F[];  // k x 2^k x k (64 KB at k = 8)
   const int32_t ub = a.params->ub;
   if (ub <= 0) return;  // no bound: the merge does not read the table
   const int k = a.k, W = 1 << k, kk = k * k;
@@ -1660,7 +1660,12 @@ cudaError_t launch_grow_round(const GraphDev& g, const LevelArgs& a, int num_sms
 cudaError_t launch_tour_table(const LevelArgs& a, const int32_t* group_ptr, const int32_t* members,
                               const int32_t* perm, int32_t* tour, cudaStream_t stream) {
   if (a.k > kTourMaxK) return cudaErrorInvalidValue;
-  k_tour_table<<<1, 256, 0, stream>>>(a, group_ptr, members, perm, tour);
+  const size_t smem = (size_t)a.k * ((size_t)1 << a.k) * a.k * sizeof(int32_t);
+  if (smem > kSmemNoOptIn) {  // k = 8 (set on the current device every time)
+    const cudaError_t e = cudaFuncSetAttribute(k_tour_table, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  k_tour_table<<<1, 256, smem, stream>>>(a, group_ptr, members, perm, tour);
   return cudaGetLastError();
 }
 
