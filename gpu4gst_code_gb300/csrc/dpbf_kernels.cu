@@ -58,7 +58,9 @@ __device__ __forceinline__ void add_stat(long long* stats, int slot, long long x
 // 1 grows only light states (2 * cost <= ub, see below), so T(v,{g}) is the
 // exact distance when it is light and otherwise only known to exceed ub/2:
 // min(T(v,{g}), ub/2 + 1) is a valid lower bound in both cases.
-// -1 = state dead.
+// -1 = state dead. The merges for k <= 8 add the tour bound (k_merge_staged);
+// every merge writes the caps of its wave to the cap table, which growth
+// reads (cap_at).
 __device__ __forceinline__ int32_t prune_cap(const LevelArgs& a, int32_t ub, int32_t v, uint32_t S) {
   const int32_t* d = a.cost + (int64_t)v * a.stride1;  // wave 1 slice starts at 0; rank({g}) = g
   const int32_t beyond = ub / 2 + 1;
@@ -489,7 +491,7 @@ constexpr int kWarpMarkMax = 16;  // changed rows of a warp up to which its lane
 struct RoundState {
   int32_t r;
   bool dense, all_cand, stats;
-  int32_t ub;        // one-label pruning bound (waves >= 2)
+  int32_t ub;        // pruning bound (waves >= 2; states are capped by the wave's cap table)
   int32_t ub_light;  // only states with 2 * cost <= ub_light grow (all waves)
   int32_t ovf_limit;  // stored costs must stay below this (kInf - largest weight)
   const uint8_t* cur_flag;
@@ -548,10 +550,10 @@ __device__ __forceinline__ void mark_candidate(uint8_t* cand, int32_t v, uint32_
 
 // Does some entry j of vals (light-filtered costs of the marking vertex,
 // edge weight w still to add) improve vertex v's entry y(j)? With a bound
-// the improved value must also pass v's one-label cap for mask j. Masks go
-// in passes of 32: the comparisons of a pass are independent (their loads
-// overlap) and leave a bit set per improved mask; v's bound is loaded only
-// when some bit is set.
+// the improved value must also pass v's cap for mask j (the wave's cap
+// table). Masks go in passes of 32: the comparisons of a pass are
+// independent (their loads overlap) and leave a bit set per improved mask;
+// v's caps are loaded only for set bits.
 template <class Vals, class Row>
 __device__ __forceinline__ bool improves_row(const LevelArgs& a, int32_t ub, int32_t v, int32_t w, const Vals& vals,
                                              const Row& y, int m) {
