@@ -83,17 +83,24 @@ def log(*a):
     print(*a, file=sys.stderr, flush=True)
 
 
-def make_graph(wl):
-    from gpu4gst_code_gb300 import native as N
+def _generators(gen):
+    """The seeded instance generators: the product library's (ours) or the
+    oracle's own build of the same source (the reference arm, which must not
+    load the product library)."""
+    if gen is None:
+        from gpu4gst_code_gb300 import native as gen
+    return gen
 
+
+def make_graph(wl, gen=None):
+    N = _generators(gen)
     if "E" in wl:
         return N.gen_random_connected(wl["V"], wl["E"], wl["wmin"], wl["wmax"], wl["graph_seed"])
     return N.gen_barabasi_albert(wl["V"], wl["m"], wl["wmin"], wl["wmax"], wl["graph_seed"])
 
 
-def make_query(wl, g, i):
-    from gpu4gst_code_gb300 import native as N
-
+def make_query(wl, g, i, gen=None):
+    N = _generators(gen)
     seed = 1000 + i
     k = wl["k"]
     if isinstance(k, tuple):  # k uniform in [lo, hi], seeded per query
@@ -106,8 +113,55 @@ def make_query(wl, g, i):
 
 # ------------------------------------------------------------- replicas --
 def rank_query_ids(rank: int, n: int) -> range:
-    """Query seeds of one replica: every rank solves its own n queries."""
+    """Query indices of one replica's timed steps: every rank solves its own
+    n queries (rank 0: 0 .. n-1, the indices tests/golden/large.json holds
+    oracle costs for)."""
     return range(rank * n, (rank + 1) * n)
+
+
+def warmup_query_ids(rank: int, n: int) -> range:
+    """Query indices of the untimed warm-up steps, apart from every timed one."""
+    return range(100_000 + rank * n, 100_000 + (rank + 1) * n)
+
+
+def golden_costs(workload: str) -> dict:
+    """{query index: oracle cost} of tests/golden/large.json for a workload."""
+    p = ROOT / "tests" / "golden" / "large.json"
+    try:
+        cases = json.loads(p.read_text())["cases"]
+    except (OSError, ValueError, KeyError):
+        return {}
+    return {c["index"]: (c["cost"], c["groups_digest"]) for c in cases if c["workload"] == workload}
+
+
+def groups_digest(gp, mem) -> str:
+    import hashlib
+
+    h = hashlib.sha256()
+    for a in (gp, mem):
+        h.update(np.ascontiguousarray(a, dtype=np.int32).tobytes())
+    return h.hexdigest()[:16]
+
+
+def parity_vs_golden(workload: str, indices, queries, costs) -> dict:
+    """Compares the costs of timed queries with the oracle costs committed
+    for the same query indices; raises on a mismatch."""
+    gold = golden_costs(workload)
+    checked, mism = 0, []
+    for i, (gp, mem), c in zip(indices, queries, costs):
+        if i not in gold:
+            continue
+        want, dig = gold[i]
+        if dig != groups_digest(gp, mem):
+            raise AssertionError(f"{workload} query {i}: regenerated groups differ from the golden instance")
+        checked += 1
+        if c != want:
+            mism.append((i, c, want))
+    if mism:
+        raise AssertionError(f"{workload}: costs differ from the oracle: {mism}")
+    return {"checked": checked, "mismatches": 0,
+            "source": "tests/golden/large.json: oracle.dpbf (C restatement of the reference CPU DPBF) on the same "
+                      "seeded queries"}
 
 
 def max_over_ranks(values, dist=None):
@@ -192,6 +246,19 @@ def table_bytes(V, k):
     return 8 * V * sum((comb(k, l) + 3) // 4 * 4 for l in range(1, k + 1))
 
 
+def sweep_bytes(V, nnz, k):
+    """Bytes of one sweep per grown wave (waves 1 .. k-1): every vertex reads
+    its row_ptr pair and its own row, every CSR entry its (col, w) and the
+    neighbour's row once, and every row (cost + parent) is written once."""
+    from math import comb
+
+    tot = 0
+    for l in range(1, k):
+        s = (comb(k, l) + 3) // 4 * 4
+        tot += V * (8 + 4 * s) + nnz * (8 + 4 * s) + V * 8 * s
+    return tot
+
+
 def traffic_per_step(wl):
     return TRAFFIC_PER_STEP.get(wl.get("name"))
 
@@ -215,19 +282,19 @@ def run_reference(args, wl):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    g = make_graph(wl)
+    g = make_graph(wl, oracle)
     threads = max(1, min(os.cpu_count() or 1, max(args.steps, args.warmup)))
 
     def one(i):
-        gp, mem = make_query(wl, g, i)
+        gp, mem = make_query(wl, g, i, oracle)
         r = oracle.dpbf(g.row_ptr, g.col, g.w, gp, mem)
         return r.cost
 
     with cf.ThreadPoolExecutor(max_workers=threads) as ex:
         if args.warmup:
-            list(ex.map(one, range(args.warmup)))
+            list(ex.map(one, warmup_query_ids(0, args.warmup)))
         t0 = time.perf_counter()
-        costs = list(ex.map(one, range(args.warmup, args.warmup + args.steps)))
+        costs = list(ex.map(one, rank_query_ids(0, args.steps)))
         wall = time.perf_counter() - t0
     value = args.steps / wall
     line = {
@@ -259,10 +326,15 @@ def run_serving(args, wl, world, rank, local_rank, dist):
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
     g = make_graph(wl)
     B = wl["batch"]
-    n_total = args.warmup + args.steps
-    ids = rank_query_ids(rank, n_total * B + 32)
-    queries = [make_query(wl, g, i) for i in ids]
-    sample, queries = queries[:32], queries[32:]
+    # timed batch j holds query indices rank_query_ids(rank, K * B)[j*B : (j+1)*B]
+    # (rank 0's first batch starts at index 0, the indices the golden costs
+    # cover); warm-up batches and the autotune sample use indices of their own
+    timed_ids = list(rank_query_ids(rank, args.steps * B))
+    warm_ids = list(warmup_query_ids(rank, args.warmup * B))
+    sample = [make_query(wl, g, 200_000 + 32 * rank + i) for i in range(32)]
+    timed_q = [make_query(wl, g, i) for i in timed_ids]
+    warm_q = [make_query(wl, g, i) for i in warm_ids]
+    queries = timed_q
     dg = N.Graph(g.row_ptr, g.col, g.w)
     t = time.perf_counter()
     lanes = dg.autotune(sample, refine_bound=True)
@@ -271,14 +343,14 @@ def run_serving(args, wl, world, rank, local_rank, dist):
     clocks = None
     for method in ("plain", "bounded"):
         refine = method == "bounded"
-        batches = [queries[i * B:(i + 1) * B] for i in range(n_total)]
-        for b in batches[:args.warmup]:
-            dg.solve_batch(b, use_graph=True, refine_bound=refine)
+        batches = [timed_q[i * B:(i + 1) * B] for i in range(args.steps)]
+        for i in range(args.warmup):
+            dg.solve_batch(warm_q[i * B:(i + 1) * B], use_graph=True, refine_bound=refine)
         if dist:
             dist.barrier()
         walls, lat_own, lat_done, costs, launches = [], [], [], [], 0
         with ClockSampler(local_rank) as clk:
-            for b in batches[args.warmup:]:
+            for b in batches:
                 flush.fill_(len(walls) & 0xFF)
                 torch.cuda.synchronize()
                 t0 = time.perf_counter()
@@ -298,6 +370,7 @@ def run_serving(args, wl, world, rank, local_rank, dist):
                             p50=float(np.percentile(lat_own, 50)), p99=float(np.percentile(lat_own, 99)),
                             c50=float(np.percentile(lat_done, 50)), c99=float(np.percentile(lat_done, 99)))
     assert arms["plain"]["costs"] == arms["bounded"]["costs"]
+    parity = parity_vs_golden(args.workload, timed_ids, timed_q, arms["bounded"]["costs"]) if rank == 0 else None
     head = arms["bounded"]
     h2d = int(np.mean([(len(q[0]) + len(q[1])) * 4 for q in queries]))
     line = {
@@ -316,6 +389,7 @@ def run_serving(args, wl, world, rank, local_rank, dist):
         "e2e": {"value": head["qps"], "unit": UNIT, "h2d_bytes_per_step": h2d * B, "d2h_bytes_per_step": 400 * B},
         "gpu_launches": head["launches"],
         "clocks": clocks,
+        "parity": parity,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -375,8 +449,11 @@ def main():
     t = time.perf_counter()
     g = make_graph(wl)
     log(f"graph: V={g.V} nnz={g.nnz} ({time.perf_counter() - t:.1f}s)")
+    # steps 0 .. W-1 are warm-up queries, steps W .. W+K-1 the timed ones
+    # (rank 0's timed query indices are 0 .. K-1: golden oracle costs exist)
     n_total = args.warmup + args.steps
-    queries = [make_query(wl, g, i) for i in rank_query_ids(rank, n_total)]
+    timed_ids = list(rank_query_ids(rank, args.steps))
+    queries = [make_query(wl, g, i) for i in list(warmup_query_ids(rank, args.warmup)) + timed_ids]
     t = time.perf_counter()
     dg = N.Graph(g.row_ptr, g.col, g.w)
     upload_ms = 1e3 * (time.perf_counter() - t)
@@ -392,7 +469,7 @@ def main():
         gp, mem = queries[i]
         t0 = time.perf_counter()
         if method == "plain":
-            r = dg.solve(gp, mem, collect_stats=True, use_graph=use_graph)
+            r = dg.solve(gp, mem, use_graph=use_graph)
         elif method == "bounded":
             r = dg.solve(gp, mem, refine_bound=True, use_graph=use_graph)
         else:
@@ -438,6 +515,10 @@ def main():
     launches = sum(r.launches for r, _ in head["results"])
     peak, peak_kind = measured_hbm_peak()
     achieved = grow_bytes / (grow_ms / 1e3) / 1e9 if grow_ms > 0 else 0.0
+    sweep = sweep_bytes(g.V, g.nnz, wl["k"])
+    traffic = traffic_per_step(wl)
+    parity = parity_vs_golden(args.workload, timed_ids, queries[args.warmup:], costs[methods[-1]]) \
+        if rank == 0 else None
     h2d = int(np.mean([(len(q[0]) + len(q[1])) * 4 for q in queries[args.warmup:]]))
     d2h = int(np.mean([64 + 4 * len(r.vertices) + 12 * len(r.edges) for r, _ in head["results"]]))
     line = {
@@ -464,7 +545,15 @@ def main():
                      "peak_kind": peak_kind, "traffic": traffic_per_step(wl),
                      "traffic_note": "DRAM bytes of the growth kernels per query, one ncu capture (profiles/)",
                      "algorithmic_bytes_per_step": grow_bytes / args.steps,
-                     "grow_ms_per_step": grow_ms / args.steps},
+                     "grow_ms_per_step": grow_ms / args.steps,
+                     "rounds_per_grown_wave": sum(r.stats["rounds"] for r in roof) / len(roof) / max(1, wl["k"] - 1),
+                     "dram_frac": (traffic / (grow_ms / args.steps / 1e3) / 1e9 / peak) if traffic else None,
+                     "one_sweep_bytes_per_step": sweep,
+                     "one_sweep_frac": sweep / (grow_ms / args.steps / 1e3) / 1e9 / peak,
+                     "note": "achieved = the growth kernels' own count of the bytes each round moves (every round "
+                             "counted); one_sweep = the bytes of a single sweep per grown wave, which no number of "
+                             "rounds changes"},
+        "parity": parity,
         "e2e": {"value": head["e2e"], "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "clocks": clocks,

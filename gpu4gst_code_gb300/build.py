@@ -2,13 +2,18 @@
 
 Compiles the CUDA/C++ sources under csrc/ with nvcc (one -gencode, sm_103a)
 and g++, in parallel, and links them into gpu4gst_code_gb300/_lib/libgst.so
-with the CUDA runtime linked statically. Rebuilds only when a source or
-header is newer than the library. No cmake, no torch extension machinery.
+with the CUDA runtime linked statically. Rebuilds whenever the content of a
+source, a header, the flags, the host architecture or the toolkit differs
+from what the library was built from (a SHA-256 stamp written beside it),
+so a library copied from another machine or built from other sources is
+never reused. No cmake, no torch extension machinery.
 """
 from __future__ import annotations
 
 import concurrent.futures as cf
+import hashlib
 import os
+import platform
 import shutil
 import subprocess
 from pathlib import Path
@@ -47,11 +52,30 @@ def _inputs() -> list[Path]:
     return files
 
 
+STAMP = LIB.with_suffix(".so.sha256")
+
+
+def _digest(inputs: list[Path]) -> str:
+    """SHA-256 over every input's name and bytes, the flags, the host
+    architecture and the nvcc binary's path and size."""
+    h = hashlib.sha256()
+    h.update(" ".join(ARCH + NVCC_FLAGS + CXX_FLAGS + CU_SOURCES + CXX_SOURCES).encode())
+    h.update(platform.machine().encode())
+    try:
+        nv = Path(nvcc())
+        h.update(f"{nv}:{nv.stat().st_size}".encode())
+    except (RuntimeError, OSError):
+        pass
+    for p in inputs:
+        h.update(p.name.encode())
+        h.update(p.read_bytes() if p.exists() else b"<missing>")
+    return h.hexdigest()
+
+
 def _stale(out: Path, inputs: list[Path]) -> bool:
-    if not out.exists():
+    if not out.exists() or not STAMP.exists():
         return True
-    t = out.stat().st_mtime
-    return any(p.stat().st_mtime > t for p in inputs if p.exists())
+    return STAMP.read_text().strip() != _digest(inputs)
 
 
 def _run(cmd: list[str]) -> None:
@@ -85,6 +109,7 @@ def build_library(force: bool = False, verbose: bool = False) -> Path:
     tmp = LIB.with_suffix(".so.tmp")
     _run([nv, *ARCH, "-shared", "-cudart", "static", *map(str, objs), "-o", str(tmp)])
     os.replace(tmp, LIB)
+    STAMP.write_text(_digest(inputs) + "\n")
     if verbose:
         print(f"built {LIB}")
     return LIB

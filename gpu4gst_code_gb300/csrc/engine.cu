@@ -1543,22 +1543,30 @@ gst_status gst_solve_batch(gst_graph* g, int32_t nq, const int32_t* ks, const in
   g_last_error.clear();
   if (!out || !g || nq < 0 || (nq > 0 && (!ks || !group_ptr))) return fail(GST_BAD_INPUT, "bad batch arguments");
   const gst_opts o = resolve_opts(opts);
+  // Query q's groups start at ks[0] + ... + ks[q-1], counting queries whose
+  // k is out of range too: such a query fails alone (GST_BAD_INPUT in its
+  // result) and the later queries keep their own groups. A negative k
+  // leaves the layout undefined, so it rejects the whole batch.
+  for (int32_t q = 0; q < nq; ++q) {
+    out[q] = nullptr;
+    if (ks[q] < 0) return fail(GST_BAD_INPUT, "negative k in batch");
+  }
   // per-query group arrays, rebased
   std::vector<std::vector<int32_t>> gps((size_t)nq);
   std::vector<const int32_t*> mems((size_t)nq, nullptr);
   std::vector<gst_status> pre((size_t)nq, GST_OK);
   int64_t gbase = 0;
   for (int32_t q = 0; q < nq; ++q) {
-    out[q] = nullptr;
+    const int64_t b = gbase;
+    gbase += ks[q];
     if (ks[q] < 1 || ks[q] > GST_MAX_K) {
       pre[(size_t)q] = GST_BAD_INPUT;
       continue;
     }
     auto& gp = gps[(size_t)q];
     gp.resize((size_t)ks[q] + 1);
-    for (int32_t i = 0; i <= ks[q]; ++i) gp[(size_t)i] = group_ptr[gbase + i] - group_ptr[gbase];
-    mems[(size_t)q] = members ? members + group_ptr[gbase] : nullptr;
-    gbase += ks[q];
+    for (int32_t i = 0; i <= ks[q]; ++i) gp[(size_t)i] = group_ptr[b + i] - group_ptr[b];
+    mems[(size_t)q] = members ? members + group_ptr[b] : nullptr;
   }
   const int32_t want = o.concurrency > 0 ? o.concurrency : (g->tuned_lanes > 0 ? g->tuned_lanes : kDefaultLanes);
   const int32_t nl = std::max(1, std::min({want, nq, kMaxLanes}));
@@ -1573,16 +1581,17 @@ gst_status gst_solve_batch(gst_graph* g, int32_t nq, const int32_t* ks, const in
     cudaSetDevice(c->device);
     std::lock_guard<std::mutex> lock(c->mu);
     for (int32_t q; (q = next.fetch_add(1)) < nq;) {
-      if (pre[(size_t)q] != GST_OK) {
-        errs[(size_t)q] = "k out of range in batch";
-        continue;
-      }
       auto* r = new (std::nothrow) gst_result;
       if (!r) {
         errs[(size_t)q] = "host allocation failed";
         continue;
       }
       out[q] = r;
+      if (pre[(size_t)q] != GST_OK) {  // this query alone fails; its result says so
+        r->status = pre[(size_t)q];
+        errs[(size_t)q] = "k out of range in batch";
+        continue;
+      }
       const auto ts = std::chrono::steady_clock::now();
       g_last_error.clear();
       bool empty = false;
@@ -1735,10 +1744,12 @@ gst_status gst_pool_solve_batch(gst_pool* p, int32_t nq, const int32_t* ks, cons
   g_last_error.clear();
   if (!p || p->replicas.empty() || !out || nq < 0 || (nq > 0 && (!ks || !group_ptr)))
     return fail(GST_BAD_INPUT, "bad pool batch arguments");
-  // where each query's groups start
+  // where each query's groups start (as gst_solve_batch: a query whose k is
+  // out of range fails alone, a negative k rejects the batch)
   std::vector<int64_t> gofs((size_t)nq + 1, 0);
   for (int32_t q = 0; q < nq; ++q) {
-    if (ks[q] < 1 || ks[q] > GST_MAX_K) return fail(GST_BAD_INPUT, "k out of range in batch");
+    out[q] = nullptr;
+    if (ks[q] < 0) return fail(GST_BAD_INPUT, "negative k in batch");
     gofs[(size_t)q + 1] = gofs[(size_t)q] + ks[q];
   }
   const int32_t chunk = std::max(1, std::min(16, nq / (4 * (int32_t)p->replicas.size()) + 1));

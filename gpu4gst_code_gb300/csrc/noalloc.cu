@@ -172,6 +172,9 @@ extern "C" gst_status gst_group_distances_noalloc(const int32_t* row_ptr, const 
   if (V < 1 || nnz < 0 || nnz >= INT32_MAX || num_sources < 0 || !row_ptr || !dist || !pred ||
       (nnz > 0 && (!col || !w)) || (num_sources > 0 && !sources))
     return GST_BAD_INPUT;
+  // an error still pending from the caller's earlier work is theirs: leave
+  // it pending and run nothing, rather than report it as this call's own
+  if (cudaPeekAtLastError() != cudaSuccess) return GST_CUDA_ERROR;
   unsigned char* scratch = nullptr;
   gst_status st = scratch_of_current_device(&scratch);
   if (st != GST_OK) return st;
@@ -189,6 +192,7 @@ extern "C" gst_status gst_group_distances_noalloc(const int32_t* row_ptr, const 
   for (;;) {
     for (int i = 0; i < kNaPollEvery; ++i, ++r)
       k_na_round<<<blocks, kNaThreads, 0, s>>>(row_ptr, col, w, V, nnz, dist, pred, scratch, (int32_t)(r % 3));
+    if (cudaGetLastError() != cudaSuccess) return GST_CUDA_ERROR;  // a round failed to launch
     if (cudaMemcpyAsync(&host_ctl, scratch, sizeof(NaCtl), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
         cudaStreamSynchronize(s) != cudaSuccess)
       return GST_CUDA_ERROR;

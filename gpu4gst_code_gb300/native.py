@@ -388,8 +388,11 @@ class Graph:
         return int(lanes.value)
 
     def solve_batch(self, queries, *, upper_bound=0, use_graph=False, collect_stats=False, refine_bound=False,
-                    concurrency=0) -> list[Result]:
-        """queries: list of (group_ptr, members) or list of member-list lists."""
+                    concurrency=0, raise_on_error=True) -> list[Result]:
+        """queries: list of (group_ptr, members) or list of member-list lists.
+        A query that fails alone (k out of range) has its status in its own
+        result; raise_on_error=False returns the results instead of raising
+        the batch's first error."""
         ks_a, gp_a, mem_a = self._pack_batch(queries)
         n = len(ks_a)
         outs = (C.c_void_p * n)()
@@ -403,7 +406,7 @@ class Graph:
                 lib().gst_result_free(outs[i])
             else:
                 res.append(None)
-        if st not in (Status.OK, Status.INFEASIBLE):
+        if raise_on_error and st not in (Status.OK, Status.INFEASIBLE):
             raise GSTError(st, msg)
         return res
 

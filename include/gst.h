@@ -123,8 +123,11 @@ gst_status gst_solve(gst_graph *g, const int32_t *group_ptr, const int32_t *memb
  * [b_q, b_q + ks[q]) with b_q = ks[0] + ... + ks[q-1], and group j is
  * members[group_ptr[j] .. group_ptr[j+1]). out[q] receives each query's
  * result (also for infeasible queries); the return value is the first
- * non-OK, non-INFEASIBLE status, else GST_OK. No counterpart in the
- * reference (it runs one query per DPBF_GPU call). */
+ * non-OK, non-INFEASIBLE status, else GST_OK. A query whose k is 0 or above
+ * GST_MAX_K fails alone: its result has status GST_BAD_INPUT and the other
+ * queries are solved on their own groups (b_q still counts its ks[q]); a
+ * negative k rejects the whole batch (GST_BAD_INPUT, every out[q] NULL).
+ * No counterpart in the reference (it runs one query per DPBF_GPU call). */
 gst_status gst_solve_batch(gst_graph *g, int32_t nq, const int32_t *ks, const int32_t *group_ptr,
                            const int32_t *members, const gst_opts *opts, gst_result **out);
 
@@ -207,7 +210,10 @@ void gst_result_stats(const gst_result *r, int64_t *stats8);
  * where unreachable) and pred[V] (the CSR entry e of u's row with col[e] the
  * next vertex towards the sources and dist[u] = dist[col[e]] + w[e]; -1 for
  * sources and unreachable vertices). `stream` is a cudaStream_t (NULL: the
- * default stream); the call returns after its work on that stream is done.
+ * default stream). The call is synchronous: between batches of rounds it
+ * copies a few control words to the host and waits on `stream`
+ * (cudaStreamSynchronize), and it returns after all its work on that
+ * stream is done.
  *
  * Limit: V <= GST_NOALLOC_MAX_VERTICES, else GST_TOO_LARGE and nothing runs.
  * The frontier scratch (3 MiB + 256 B) is a fixed array in the library's
@@ -219,7 +225,11 @@ void gst_result_stats(const gst_result *r, int64_t *stats8);
  * GPU (other streams, other host threads) race and corrupt each other.
  * Errors are returned as the status only (gst_last_error() is not set):
  * GST_BAD_INPUT for NULL pointers, V < 1 or a source / CSR entry out of
- * range, GST_OVERFLOW, GST_TIMEOUT, GST_CUDA_ERROR.
+ * range, GST_OVERFLOW, GST_TIMEOUT, GST_CUDA_ERROR. A CUDA error still
+ * pending from the caller's own earlier work makes the call return
+ * GST_CUDA_ERROR before it launches anything, and the error is left
+ * pending for the caller to read. With num_sources = 0 every vertex is
+ * unreachable (dist GST_COST_LIMIT, pred -1).
  * No counterpart in the reference. */
 gst_status gst_group_distances_noalloc(const int32_t *row_ptr, const int32_t *col, const int32_t *w, int32_t V,
                                        int64_t nnz, const int32_t *sources, int32_t num_sources, int32_t *dist,

@@ -18,7 +18,14 @@
  *   - groups: for each g in cumpulsory_group_vertices, in iteration order,
  *     the members are the first elements of group_graph[g] (DPQ.cu:22-34);
  *   - the CSR arrays of toCSR (managed memory, host-readable) are the graph;
- *     they are uploaded once per CSR_graph (keyed by all_edge) and kept;
+ *     they are uploaded once and kept resident, keyed by the three array
+ *     addresses, V, E_all and a checksum of the arrays' contents, so a CSR
+ *     freed by the caller (rucgraph/test_gpu.h:281-283) whose addresses a
+ *     later toCSR reuses for another graph is uploaded afresh, never
+ *     mistaken for the old one; gst_dropin::release_all() frees every
+ *     resident copy;
+ *   - the solve runs through the captured CUDA-graph driver (one graph
+ *     launch per query, gst_opts.use_graph = 1);
  *   - returns the tree (vertices with weight 0, edges with the CSR's int
  *     weights, as the backtrack adds them at DPQ.cu:744-750), sets
  *     *real_cost, adds the states written to *pointer1 and stores the
@@ -46,20 +53,73 @@
 
 namespace gst_dropin {
 
+// What identifies an uploaded CSR: its arrays' addresses and sizes and a
+// 64-bit mix of their contents (FNV-1a over the words).
+struct CsrKey {
+  const int *pointer, *edge, *weight;
+  int V, E;
+  uint64_t sum;
+  bool operator==(const CsrKey &o) const {
+    return pointer == o.pointer && edge == o.edge && weight == o.weight && V == o.V && E == o.E && sum == o.sum;
+  }
+};
+
+inline uint64_t csr_checksum(const CSR_graph &graph) {
+  uint64_t h = 1469598103934665603ull;
+  auto mix = [&h](const int *a, int64_t n) {
+    for (int64_t i = 0; i < n; ++i) {
+      h ^= (uint32_t)a[i];
+      h *= 1099511628211ull;
+    }
+  };
+  mix(graph.all_pointer, (int64_t)graph.V + 1);
+  mix(graph.all_edge, graph.E_all);
+  mix(graph.all_edge_weight, graph.E_all);
+  return h;
+}
+
+struct Resident {
+  std::mutex mu;
+  std::vector<std::pair<CsrKey, gst_graph *>> graphs;
+};
+
+inline Resident &resident() {
+  static Resident r;
+  return r;
+}
+
+// The resident copy of `graph`, uploaded on first use. A cached copy whose
+// addresses match but whose sizes or contents differ (the caller freed the
+// CSR and a later toCSR reused the addresses) is freed and replaced.
 inline gst_graph *resident_graph(CSR_graph &graph) {
-  static std::mutex mu;
-  static std::unordered_map<const int *, gst_graph *> cache;
-  std::lock_guard<std::mutex> lock(mu);
-  auto it = cache.find(graph.all_edge);
-  if (it != cache.end()) return it->second;
+  Resident &res = resident();
+  std::lock_guard<std::mutex> lock(res.mu);
+  const CsrKey key{graph.all_pointer, graph.all_edge, graph.all_edge_weight, graph.V, graph.E_all,
+                   csr_checksum(graph)};
+  for (auto it = res.graphs.begin(); it != res.graphs.end(); ++it) {
+    if (it->first == key) return it->second;
+    if (it->first.pointer == key.pointer || it->first.edge == key.edge || it->first.weight == key.weight) {
+      gst_graph_free(it->second);  // stale: its arrays were freed and reused
+      res.graphs.erase(it);
+      break;
+    }
+  }
   gst_graph *g = nullptr;
   if (gst_graph_upload(graph.all_pointer, graph.all_edge, graph.all_edge_weight, graph.V, graph.E_all, &g) !=
       GST_OK) {
     std::cout << "DPBF_GPU: graph upload failed: " << gst_last_error() << std::endl;
     return nullptr;
   }
-  cache[graph.all_edge] = g;
+  res.graphs.push_back({key, g});
   return g;
+}
+
+// Frees every resident graph copy (e.g. after the caller frees its CSRs).
+inline void release_all() {
+  Resident &res = resident();
+  std::lock_guard<std::mutex> lock(res.mu);
+  for (auto &e : res.graphs) gst_graph_free(e.second);
+  res.graphs.clear();
 }
 
 }  // namespace gst_dropin
@@ -83,9 +143,12 @@ graph_hash_of_mixed_weighted DPBF_GPU(node **host_tree, node *host_tree_one_d, C
     for (auto &e : group_graph[gid]) members.push_back(e.first);
     group_ptr.push_back((int32_t)members.size());
   }
+  gst_opts opts{};
+  opts.struct_size = (int32_t)sizeof(gst_opts);
+  opts.use_graph = 1;  // one captured CUDA graph per query
   gst_result *r = nullptr;
   const gst_status st = gst_solve(g, group_ptr.data(), members.data(), (int32_t)cumpulsory_group_vertices.size(),
-                                  nullptr, &r);
+                                  &opts, &r);
   if (st == GST_OK) {
     std::vector<int32_t> vs((size_t)gst_result_num_vertices(r)), es(3 * (size_t)gst_result_num_edges(r));
     gst_result_vertices(r, vs.data());

@@ -15,7 +15,9 @@ this package. The product library never calls into it.
 from __future__ import annotations
 
 import ctypes as C
+import hashlib
 import os
+import platform
 import shutil
 import subprocess
 from pathlib import Path
@@ -26,7 +28,14 @@ HERE = Path(__file__).resolve().parent
 BUILD_DIR = HERE.parent / "_build" / "oracle"
 ORACLE_LIB = BUILD_DIR / "liboracle.so"
 REF_LIB = HERE / "_ref" / "libref_dpbf.so"
-REFERENCE_ROOT = Path(os.environ.get("GST_REFERENCE_ROOT", "/root/reference"))
+# The reference checkout: $GST_REFERENCE_ROOT, else a directory named
+# "reference" beside this repository's checkout. Absent on hosts that only
+# run the built library; everything that needs it is skipped there.
+REFERENCE_ROOT = Path(os.environ["GST_REFERENCE_ROOT"]) if os.environ.get("GST_REFERENCE_ROOT") \
+    else HERE.parent.parent / "reference"
+GEN_LIB = BUILD_DIR / "liboracle_gen.so"
+GEN_SRC = HERE.parent / "gpu4gst_code_gb300" / "csrc" / "gen.cpp"
+GEN_INCLUDE = HERE.parent / "include"
 
 INF = 2**31 - 1
 I32P = C.POINTER(C.c_int32)
@@ -36,16 +45,43 @@ F64P = C.POINTER(C.c_double)
 OK, INFEASIBLE, STOPPED = 0, 1, 2
 
 
+def _stamp_ok(out: Path, inputs: list[Path], flags: list[str]) -> tuple[bool, str]:
+    """(out is current, digest): a SHA-256 of the inputs, the flags and the
+    host architecture, kept in <out>.sha256."""
+    h = hashlib.sha256(" ".join(flags + [platform.machine()]).encode())
+    for p in inputs:
+        h.update(p.read_bytes())
+    d = h.hexdigest()
+    stamp = out.with_suffix(out.suffix + ".sha256")
+    return out.exists() and stamp.exists() and stamp.read_text().strip() == d, d
+
+
+def _build_so(out: Path, cmd: list[str], inputs: list[Path], force: bool) -> Path:
+    ok, d = _stamp_ok(out, inputs, cmd)
+    if ok and not force:
+        return out
+    BUILD_DIR.mkdir(parents=True, exist_ok=True)
+    tmp = out.with_suffix(f".so.{os.getpid()}.tmp")  # concurrent builders never share a temporary
+    subprocess.run(cmd + ["-o", str(tmp)], check=True)
+    os.replace(tmp, out)
+    out.with_suffix(out.suffix + ".sha256").write_text(d + "\n")
+    return out
+
+
 def build_oracle(force: bool = False) -> Path:
     src = HERE / "dpbf_oracle.c"
-    if not force and ORACLE_LIB.exists() and ORACLE_LIB.stat().st_mtime >= src.stat().st_mtime:
-        return ORACLE_LIB
-    BUILD_DIR.mkdir(parents=True, exist_ok=True)
     cc = shutil.which("gcc") or "cc"
-    tmp = ORACLE_LIB.with_suffix(".so.tmp")
-    subprocess.run([cc, "-O2", "-std=c11", "-shared", "-fPIC", str(src), "-o", str(tmp)], check=True)
-    os.replace(tmp, ORACLE_LIB)
-    return ORACLE_LIB
+    return _build_so(ORACLE_LIB, [cc, "-O2", "-std=c11", "-shared", "-fPIC", str(src)], [src], force)
+
+
+def build_gen(force: bool = False) -> Path:
+    """The seeded instance generators (the same source the product library
+    compiles, include/gst_gen.h) as a library of their own, so that the
+    reference arm of the benchmark builds its instances without loading the
+    product library."""
+    cxx = shutil.which("g++") or "c++"
+    return _build_so(GEN_LIB, [cxx, "-O2", "-std=c++17", "-shared", "-fPIC", "-I", str(GEN_INCLUDE), str(GEN_SRC)],
+                     [GEN_SRC, GEN_INCLUDE / "gst_gen.h"], force)
 
 
 def build_ref(force: bool = False) -> Path | None:
@@ -227,3 +263,90 @@ def check_tree(row_ptr, col, w, group_ptr, members, vertices, edges, cost) -> st
         if not any(int(m) in vs for m in mem[gp[g]:gp[g + 1]]):
             return f"group {g} not covered"
     return None
+
+
+# ------------------------------------------------------------- generators --
+_GEN = None
+
+
+def gen_lib() -> C.CDLL:
+    global _GEN
+    if _GEN is None:
+        dll = C.CDLL(str(build_gen()))
+        sig = {
+            "gst_gen_random_connected": (C.c_void_p, [C.c_int32, C.c_int64, C.c_int32, C.c_int32, C.c_uint64]),
+            "gst_gen_barabasi_albert": (C.c_void_p, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_uint64]),
+            "gst_host_graph_num_vertices": (C.c_int32, [C.c_void_p]),
+            "gst_host_graph_num_entries": (C.c_int64, [C.c_void_p]),
+            "gst_host_graph_copy": (None, [C.c_void_p, I32P, I32P, I32P]),
+            "gst_host_graph_free": (None, [C.c_void_p]),
+            "gst_gen_groups_uniform": (C.c_void_p, [C.c_int32, C.c_int32, C.c_int32, C.c_uint64]),
+            "gst_gen_groups_zipf_degree": (C.c_void_p, [I32P, I32P, C.c_int32, C.c_int64, C.c_int32, C.c_double,
+                                                        C.c_int32, C.c_int32, C.c_uint64]),
+            "gst_host_groups_k": (C.c_int32, [C.c_void_p]),
+            "gst_host_groups_num_members": (C.c_int64, [C.c_void_p]),
+            "gst_host_groups_copy": (None, [C.c_void_p, I32P, I32P]),
+            "gst_host_groups_free": (None, [C.c_void_p]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(dll, name)
+            fn.restype, fn.argtypes = res, args
+        _GEN = dll
+    return _GEN
+
+
+class HostCSR:
+    def __init__(self, row_ptr, col, w):
+        self.row_ptr, self.col, self.w = row_ptr, col, w
+
+    @property
+    def V(self) -> int:
+        return len(self.row_ptr) - 1
+
+    @property
+    def nnz(self) -> int:
+        return len(self.col)
+
+
+def _take_graph(h) -> HostCSR:
+    L = gen_lib()
+    if not h:
+        raise ValueError("generator rejected its parameters")
+    try:
+        V, n = L.gst_host_graph_num_vertices(h), L.gst_host_graph_num_entries(h)
+        rp, col, w = np.zeros(V + 1, np.int32), np.zeros(n, np.int32), np.zeros(n, np.int32)
+        L.gst_host_graph_copy(h, _p(rp), _p(col), _p(w))
+    finally:
+        L.gst_host_graph_free(h)
+    return HostCSR(rp, col, w)
+
+
+def _take_groups(h):
+    L = gen_lib()
+    if not h:
+        raise ValueError("group generator rejected its parameters")
+    try:
+        k, n = L.gst_host_groups_k(h), L.gst_host_groups_num_members(h)
+        gp, mem = np.zeros(k + 1, np.int32), np.zeros(n, np.int32)
+        L.gst_host_groups_copy(h, _p(gp), _p(mem))
+    finally:
+        L.gst_host_groups_free(h)
+    return gp, mem
+
+
+def gen_random_connected(V, E, wmin, wmax, seed) -> HostCSR:
+    return _take_graph(gen_lib().gst_gen_random_connected(V, E, wmin, wmax, seed))
+
+
+def gen_barabasi_albert(V, m, wmin, wmax, seed) -> HostCSR:
+    return _take_graph(gen_lib().gst_gen_barabasi_albert(V, m, wmin, wmax, seed))
+
+
+def gen_groups_uniform(V, k, size, seed):
+    return _take_groups(gen_lib().gst_gen_groups_uniform(V, k, size, seed))
+
+
+def gen_groups_zipf_degree(g, k, s, size_min, size_max, seed):
+    rp, col = _i32(g.row_ptr), _i32(g.col)
+    return _take_groups(gen_lib().gst_gen_groups_zipf_degree(_p(rp), _p(col), g.V, g.nnz, k, s, size_min, size_max,
+                                                             seed))

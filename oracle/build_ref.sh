@@ -3,10 +3,12 @@
 # from the reference checkout) into oracle/_ref/libref_dpbf.so, together with
 # the Boost.Heap stand-in under oracle/ref/shim. Test infrastructure only.
 #
-# Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+# Usage: oracle/build_ref.sh [REFERENCE_ROOT]
+#   (default: $GST_REFERENCE_ROOT, else the "reference" directory beside
+#   this repository's checkout)
 set -eu
-REF=${1:-/root/reference}
 HERE=$(cd "$(dirname "$0")" && pwd)
+REF=${1:-${GST_REFERENCE_ROOT:-$HERE/../../reference}}
 if [ ! -f "$REF/rucgraph/graph_v_of_v_idealID_DPBF_only_ec.h" ]; then
   echo "reference sources not found under $REF" >&2
   exit 3

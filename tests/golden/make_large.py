@@ -1,0 +1,107 @@
+"""Generates tests/golden/large.json: oracle costs of the benchmark's own
+queries at the sizes the workloads name.
+
+For every workload of bench.py listed below, the graph and the first N
+queries (query i is seeded 1000 + i, exactly as bench.py makes them) are
+built with the oracle's own build of the seeded generators (oracle.gen_*,
+the same source as include/gst_gen.h) and solved by the CPU oracle's C
+restatement of the reference DPBF (oracle.dpbf, pinned against the
+reference's own graph_v_of_v_idealID_DPBF_only_ec by tests/test_oracle.py).
+Each case records digests of the regenerated graph and groups, so a reader
+can check that it rebuilt the same instance, the optimal cost, the states
+the oracle popped and its single-core time.
+
+The GPU machine never runs this script (it takes tens of minutes and ~10 GB of
+host memory per 2M- or 4M-vertex query); bench.py and the -m gpu tests only
+read the committed file.
+
+  python tests/golden/make_large.py [--workloads ba1m_k6,ba2m_k8,...] [--jobs N]
+"""
+from __future__ import annotations
+
+import argparse
+import concurrent.futures as cf
+import hashlib
+import json
+import multiprocessing as mp
+import os
+import platform
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parents[1]
+sys.path.insert(0, str(ROOT))
+
+OUT = HERE / "large.json"
+
+# workload -> (query indices, parallel jobs; the 2M and 4M instances need ~10 GB each)
+PLAN = {
+    "rc1k_k3": (range(0, 40), 8),
+    "ba1m_k6": (range(0, 30), 6),
+    "serve256": (range(0, 48), 6),
+    "ba2m_k8": (range(0, 3), 3),
+    "ba4m_k7": (range(0, 3), 3),
+}
+
+
+def digest(*arrays) -> str:
+    h = hashlib.sha256()
+    for a in arrays:
+        h.update(np.ascontiguousarray(a, dtype=np.int32).tobytes())
+    return h.hexdigest()[:16]
+
+
+def _solve(args):
+    name, i = args
+    import bench
+    import oracle
+
+    wl = dict(bench.WORKLOADS[name], name=name)
+    g = bench.make_graph(wl, oracle)
+    gp, mem = bench.make_query(wl, g, i, oracle)
+    t = time.perf_counter()
+    r = oracle.dpbf(g.row_ptr, g.col, g.w, gp, mem)
+    sec = time.perf_counter() - t
+    if r.cost >= 0:
+        err = oracle.check_tree(g.row_ptr, g.col, g.w, gp, mem, r.vertices, r.edges, r.cost)
+        if err is not None:
+            raise RuntimeError(f"{name} query {i}: oracle tree invalid: {err}")
+    return {"workload": name, "index": i, "seed": 1000 + i, "k": int(len(gp) - 1),
+            "graph_digest": digest(g.row_ptr, g.col, g.w), "groups_digest": digest(gp, mem),
+            "cost": int(r.cost), "pops": int(r.pops), "oracle_s": round(sec, 3)}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--workloads", default=",".join(PLAN))
+    ap.add_argument("--jobs", type=int, default=0, help="parallel oracle processes (0: the plan's)")
+    args = ap.parse_args()
+    import oracle
+
+    oracle.build_oracle()  # once, before the workers start
+    oracle.build_gen()
+    done = json.loads(OUT.read_text()) if OUT.exists() else {"cases": []}
+    have = {(c["workload"], c["index"]) for c in done["cases"]}
+    for name in args.workloads.split(","):
+        idx, jobs = PLAN[name]
+        todo = [(name, i) for i in idx if (name, i) not in have]
+        if not todo:
+            continue
+        ctx = mp.get_context("spawn")
+        with cf.ProcessPoolExecutor(max_workers=args.jobs or jobs, mp_context=ctx) as ex:
+            for case in ex.map(_solve, todo):
+                done["cases"].append(case)
+                print(json.dumps(case), flush=True)
+                done["cases"].sort(key=lambda c: (c["workload"], c["index"]))
+                done["generator"] = ("tests/golden/make_large.py: bench.py's workloads and query seeds, oracle.gen_* "
+                                     "instances, oracle.dpbf costs")
+                done["host"] = f"{platform.machine()}, {os.cpu_count()} threads"
+                OUT.write_text(json.dumps(done, indent=1) + "\n")
+
+
+if __name__ == "__main__":
+    main()

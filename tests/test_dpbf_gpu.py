@@ -155,6 +155,37 @@ def test_many_group_counts(k):
         _check(g.row_ptr, g.col, g.w, gp, mem, res, want.cost)
 
 
+@pytest.mark.parametrize("k", [11, 12])
+def test_wide_masks_merge_per_state(k):
+    """k > 10 merges a state per thread (k_merge, mask-table lookups): exact
+    against the oracle unpruned, with a starting bound and with refinement."""
+    g = native.gen_random_connected(300, 900, 1, 40, 60 + k)
+    gp, mem = native.gen_groups_uniform(300, k, 2, 70 + k)
+    want = oracle.dpbf(g.row_ptr, g.col, g.w, gp, mem)
+    assert want.status == oracle.OK
+    with native.Graph(g.row_ptr, g.col, g.w) as dg:
+        for kw in ({}, {"upper_bound": 2 * want.cost + 1}, {"upper_bound": want.cost}, {"refine_bound": True}):
+            for use_graph in (False, True):
+                res = dg.solve(gp, mem, use_graph=use_graph, **kw)
+                _check(g.row_ptr, g.col, g.w, gp, mem, res, want.cost)
+        if want.cost > 1:
+            assert dg.solve(gp, mem, upper_bound=want.cost - 1).status == Status.INFEASIBLE
+
+
+def test_batch_query_with_bad_k_fails_alone():
+    """A query whose k is out of range fails by itself; the queries after it
+    keep their own groups (their offsets count the bad query's k)."""
+    g = native.gen_random_connected(600, 2000, 1, 50, 71)
+    q1 = native.gen_groups_uniform(600, 3, 4, 72)
+    bad = native.gen_groups_uniform(600, 17, 2, 73)
+    q3 = native.gen_groups_uniform(600, 3, 4, 74)
+    with native.Graph(g.row_ptr, g.col, g.w) as dg:
+        res = dg.solve_batch([q1, bad, q3], raise_on_error=False)
+    assert res[1].status == Status.BAD_INPUT
+    for (gp, mem), r in ((q1, res[0]), (q3, res[2])):
+        _check(g.row_ptr, g.col, g.w, gp, mem, r, oracle.dpbf(g.row_ptr, g.col, g.w, gp, mem).cost)
+
+
 @pytest.mark.parametrize("use_graph", MODES)
 def test_workspace_reuse_across_k_and_repeat(use_graph):
     g = native.gen_barabasi_albert(4000, 4, 1, 100, 3)
@@ -228,6 +259,10 @@ def test_stats_and_launch_count(use_graph):
         assert res.launches >= 1 + 5 + st["rounds"] + 2
 
 
+def _oracle_costs(g, qs):
+    return [oracle.dpbf(g.row_ptr, g.col, g.w, gp, mem).cost for gp, mem in qs]
+
+
 def _ba_queries(V, n, seed):
     g = native.gen_barabasi_albert(V, 4, 1, 100, seed)
     rng = np.random.default_rng(seed)
@@ -240,8 +275,9 @@ def test_concurrent_batch_matches_single(concurrency):
     """gst_solve_batch runs queries on concurrent solve contexts (lanes)
     over one resident graph: every result equals the single solve."""
     g, qs = _ba_queries(20_000, 12, 31)
+    want = _oracle_costs(g, qs)
     with native.Graph(g.row_ptr, g.col, g.w) as dg:
-        want = [dg.solve(gp, mem, use_graph=True).cost for gp, mem in qs]
+        assert [dg.solve(gp, mem, use_graph=True).cost for gp, mem in qs] == want
         for refine in (False, True):
             got = dg.solve_batch(qs, use_graph=True, refine_bound=refine, concurrency=concurrency)
             assert [r.cost for r in got] == want
@@ -252,8 +288,8 @@ def test_concurrent_batch_matches_single(concurrency):
 
 def test_autotune_keeps_results_exact():
     g, qs = _ba_queries(20_000, 16, 37)
+    want = _oracle_costs(g, qs)
     with native.Graph(g.row_ptr, g.col, g.w) as dg:
-        want = [dg.solve(gp, mem).cost for gp, mem in qs]
         lanes = dg.autotune(qs[:8], refine_bound=True)
         assert lanes in (1, 2, 4, 8)
         got = dg.solve_batch(qs, use_graph=True, refine_bound=True)
@@ -287,8 +323,7 @@ def test_replica_pool_matches_single():
     node one per device) share a batch by work stealing; results equal the
     single solves and both replicas take queries."""
     g, qs = _ba_queries(20_000, 24, 41)
-    with native.Graph(g.row_ptr, g.col, g.w) as dg:
-        want = [dg.solve(gp, mem).cost for gp, mem in qs]
+    want = _oracle_costs(g, qs)
     with native.Pool(g.row_ptr, g.col, g.w, [0, 0]) as pool:
         assert pool.replicas == 2
         got = pool.solve_batch(qs, refine_bound=True, concurrency=2)

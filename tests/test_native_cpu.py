@@ -131,7 +131,9 @@ def test_dropin_adapter_compiles_against_reference_headers(tmp_path):
     import shutil
     import subprocess
 
-    ref = Path("/root/reference/rucgraph")
+    import oracle
+
+    ref = oracle.REFERENCE_ROOT / "rucgraph"
     if not (ref / "DPQ.cuh").exists() or not shutil.which("g++"):
         pytest.skip("reference headers not present")
     native.lib()

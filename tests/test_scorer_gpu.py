@@ -99,6 +99,7 @@ def test_proposal_is_feasible_and_learned_solve_exact(use_scorer):
         with N.Graph(g.row_ptr, g.col, g.w) as dg, N.Scorer(learn.init_params(seed)) as sc:
             s = sc if use_scorer else None
             plain = dg.solve(gp, mem, use_graph=True)
+            assert plain.cost == oracle.dpbf(g.row_ptr, g.col, g.w, gp, mem).cost
             prop = dg.propose(s, gp, mem)
             assert prop.status == N.Status.OK
             err = oracle.check_tree(g.row_ptr, g.col, g.w, gp, mem, prop.vertices, prop.edges, prop.cost)
