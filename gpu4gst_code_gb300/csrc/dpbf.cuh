@@ -30,7 +30,10 @@ constexpr int32_t kLeaf = INT32_MIN;
 constexpr int kDegBigMin = 32;
 constexpr int kDegBigMax = 64;
 constexpr int kGrowThreads = 256;  // block size of growth / merge kernels
-constexpr int kMaxThreadMasks = 24;  // waves with stride <= this: a thread per vertex
+constexpr int kMaxThreadMasks = 24;  // waves with stride <= this: a thread per vertex (sparse rounds)
+// Dense rounds of waves with stride <= this run a team of stride/4 lanes per
+// vertex, each lane holding four masks (k_grow_team).
+constexpr int kMaxTeamStride = 32;
 // Sparse rounds scan candidate flags in tiles of this many consecutive
 // vertex IDs (one warp each). The graph is relabelled at upload so that
 // every tile holds a mix of degrees (see gst_graph_upload).
@@ -100,7 +103,7 @@ struct Counters {
   int32_t bt_nv, bt_ne, bt_states;
   int32_t rounds_total; // growth rounds that did work, all waves
   int32_t timeout;
-  int32_t pad;
+  int32_t grow_launches;      // growth-round kernels launched (each counts itself)
   unsigned long long best;    // (cost << 32) | root, argmin of the full mask
   unsigned long long states;  // states written by merges + growth
 };

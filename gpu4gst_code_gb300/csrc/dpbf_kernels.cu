@@ -823,6 +823,145 @@ __device__ __forceinline__ void hub_relax(const GraphDev& g, const LevelArgs& a,
   }
 }
 
+// Hub chunks of waves with stride 4G <= kMaxTeamStride, all 32 entries in
+// flight at once: the warp compacts the chunk's active entries (dense
+// rounds: all; sparse rounds: those whose neighbour changed) into shared
+// memory, then splits into 32/GP teams of GP lanes (GP = G rounded up to a
+// power of two; lanes G .. GP-1 of a team idle). Team t takes active
+// entries t, t + T, ... four at a time, lane q loading the 16-byte quarter
+// q of each neighbour's row, so the warp has up to 32 rows in flight where
+// a mask-per-lane walk has four. The teams' minima are combined by
+// shuffles; team 0 folds them into the hub's scratch row and the chunk
+// completes as in hub_chunk_relax (the last chunk of a hub applies the
+// row).
+template <int GP>
+__device__ __forceinline__ void hub_chunk_team(const GraphDev& g, const LevelArgs& a, const RoundState& rs,
+                                               int64_t c, int4* wbuf, uint32_t (&acc)[kAccN]) {
+  constexpr int T = 32 / GP;
+  const int lane = threadIdx.x & 31;
+  const int team = lane / GP, glane = lane - team * GP;
+  const int G = a.stride >> 2;
+  const int32_t s = a.stride;
+  const int32_t u = g.chunk_vtx[c];
+  const int2 hc = g.hub_chunk[c];  // (hub index, first CSR entry of the chunk)
+  const int32_t beg = g.row_ptr[u], end = g.row_ptr[u + 1];
+  const int32_t cend = min(end, hc.y + 32);
+  const int32_t e = hc.y + lane;
+  int2 x = make_int2(0, 0);
+  bool act = false;
+  if (e < cend) {
+    x = g.adj[e];
+    act = rs.dense || rs.cur_flag[x.x] != 0;
+  }
+  const unsigned bal = __ballot_sync(0xffffffffu, act);
+  const int n = __popc(bal);
+  if (act) wbuf[__popc(bal & ((1u << lane) - 1u))] = make_int4(x.x, x.y, e, 0);
+  __syncwarp();
+  int32_t best[4] = {kInf, kInf, kInf, kInf};
+  int32_t code[4] = {-1, -1, -1, -1};
+  const bool on = glane < G;
+  const int4* tab = reinterpret_cast<const int4*>(a.cost + a.base);
+  for (int i0 = team; i0 < n; i0 += 4 * T) {
+    int4 it[4], r[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) it[q] = wbuf[min(i0 + q * T, n - 1)];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) r[q] = on ? tab[(int64_t)it[q].x * G + glane] : make_int4(kInf, kInf, kInf, kInf);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      if (i0 + q * T >= n) continue;
+      const int32_t rv[4] = {r[q].x, r[q].y, r[q].z, r[q].w};
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        const int32_t cc = light_or_inf(rv[t], rs.ub_light) + it[q].y;  // both < 2^30: no wrap
+        if (cc < best[t]) {
+          best[t] = cc;
+          code[t] = it[q].z;
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int off = GP; off < 32; off <<= 1) {
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      const int32_t ob = __shfl_xor_sync(0xffffffffu, best[t], off);
+      const int32_t oc = __shfl_xor_sync(0xffffffffu, code[t], off);
+      if (ob < best[t] || (ob == best[t] && (uint32_t)oc < (uint32_t)code[t])) {
+        best[t] = ob;
+        code[t] = oc;
+      }
+    }
+  }
+  if (lane == 0) {
+    acc[kAccEnt] += cend - hc.y;
+    acc[kAccRows] += n;
+  }
+  unsigned long long* hm = g.hub_min + (int64_t)hc.x * g.hub_stride;
+  bool folded = false;
+  if (team == 0 && on) {
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      if (best[t] >= kInf) continue;
+      if (best[t] >= rs.ovf_limit) acc[kAccOverflow] = 1;
+      atomicMin(hm + 4 * glane + t, ((unsigned long long)(uint32_t)best[t] << 32) | (uint32_t)code[t]);
+      folded = true;
+    }
+  }
+  __syncwarp();  // wbuf is reused by the warp's next chunk
+  // the folded minima must be visible before the chunk counts as done; a
+  // chunk that folded nothing has nothing to order
+  if (__any_sync(0xffffffffu, folded)) __threadfence();
+  int last = 0;
+  if (lane == 0) last = atomicAdd(g.hub_cnt + hc.x, 1) == (end - beg + 31) / 32 - 1;
+  last = __shfl_sync(0xffffffffu, last, 0);
+  if (!last) return;
+  __threadfence();
+  const int64_t rowu = a.base + (int64_t)u * s;
+  bool imp = false;
+  for (int j = lane; j < s; j += 32) {
+    const unsigned long long r = atomicExch(hm + j, ~0ull);  // read and clear
+    if (j >= a.m || r == ~0ull) continue;
+    const int32_t c2 = (int32_t)(r >> 32);
+    const int32_t own = a.cost[rowu + j];
+    if (c2 >= own) continue;
+    if (rs.ub > 0 && c2 > cap_at(a, u, j)) continue;
+    a.cost[rowu + j] = c2;
+    a.par[rowu + j] = (int32_t)(uint32_t)(r & 0xffffffffull);
+    imp = true;
+    ++acc[kAccImproved];
+  }
+  if (lane == 0) {
+    atomicExch(g.hub_cnt + hc.x, 0);
+    ++acc[kAccVert];
+  }
+  if (__ballot_sync(0xffffffffu, imp) && lane == 0) {
+    rs.next_flag[u] = 1;
+    ++acc[kAccChanged];
+  }
+}
+
+// hub_relax for waves with stride <= kMaxTeamStride (hub_chunk_team).
+template <int GP>
+__device__ __forceinline__ void hub_relax_team(const GraphDev& g, const LevelArgs& a, const RoundState& rs,
+                                               uint32_t (&acc)[kAccN]) {
+  __shared__ int4 hbuf[kGrowThreads / 32][32];
+  int4* wbuf = hbuf[threadIdx.x >> 5];
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t c0 = warp; c0 < g.nchunks; c0 += 32 * nwarps) {
+    const int64_t cl = c0 + lane * nwarps;
+    const bool want = cl < g.nchunks && (rs.all_cand || rs.cand_cur[g.chunk_vtx[cl]] != 0);
+    unsigned bal = __ballot_sync(0xffffffffu, want);
+    while (bal) {
+      const int64_t c = c0 + (int64_t)(__ffs(bal) - 1) * nwarps;
+      bal &= bal - 1u;
+      hub_chunk_team<GP>(g, a, rs, c, wbuf, acc);
+    }
+  }
+}
+
 // Sparse rounds: for every hub that changed in this round's hub kernel, the
 // warp that takes one of its 32-entry chunks marks the chunk's neighbours
 // that the hub's new row improves (within their bound). Lanes read the
@@ -924,12 +1063,26 @@ __global__ void __launch_bounds__(kGrowThreads) k_seed(GraphDev g, LevelArgs a) 
 // and relax the hubs inside the round kernel, beside the other vertices.
 template <int L>
 __global__ void __launch_bounds__(kGrowThreads) k_grow_hubs(GraphDev g, LevelArgs a) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&a.ctr->grow_launches, 1);
   RoundState rs;
   if (!round_begin(g, a, rs) || rs.dense) return;
   __shared__ BlockAcc ba;
   block_acc_init(ba);
   uint32_t acc[kAccN] = {0, 0, 0, 0, 0, 0, 0};
   hub_relax<L>(g, a, rs, acc);
+  round_flush(a, rs, acc, ba);
+}
+
+// The hub kernel of sparse rounds for waves with stride <= kMaxTeamStride.
+template <int GP>
+__global__ void __launch_bounds__(kGrowThreads) k_grow_hubs_team(GraphDev g, LevelArgs a) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&a.ctr->grow_launches, 1);
+  RoundState rs;
+  if (!round_begin(g, a, rs) || rs.dense) return;
+  __shared__ BlockAcc ba;
+  block_acc_init(ba);
+  uint32_t acc[kAccN] = {0, 0, 0, 0, 0, 0, 0};
+  hub_relax_team<GP>(g, a, rs, acc);
   round_flush(a, rs, acc, ba);
 }
 
@@ -1166,8 +1319,10 @@ __device__ __forceinline__ void warp_mark(const GraphDev& g, const LevelArgs& a,
 
 template <int MP>
 __global__ void __launch_bounds__(kGrowThreads, (MP <= 16 ? 3 : 2)) k_grow_thread(GraphDev g, LevelArgs a) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&a.ctr->grow_launches, 1);
   RoundState rs;
   if (!round_begin(g, a, rs)) return;
+  if (rs.dense) return;  // dense rounds run in k_grow_team
   __shared__ BlockAcc ba;
   block_acc_init(ba);
   uint32_t acc[kAccN] = {0, 0, 0, 0, 0, 0, 0};
@@ -1241,11 +1396,141 @@ __global__ void __launch_bounds__(kGrowThreads, (MP <= 16 ? 3 : 2)) k_grow_threa
   round_end(a, rs, acc, ba);
 }
 
+// Dense rounds of waves with row stride 4G <= kMaxTeamStride: a team of G
+// lanes relaxes one vertex, lane q holding masks 4q .. 4q+3 of its row.
+// Per neighbour a lane issues one 16-byte load (its quarter, half, ... of
+// the neighbour's row; the team's loads together read the row's
+// contiguous 16G bytes) after loading the CSR entry, which every lane of
+// the team reads at the same address. UNR neighbours are in flight at a
+// time: their CSR entries are loaded unconditionally at clamped addresses,
+// then their rows, then folded. A team holds 8 best / parent registers,
+// not the whole row, so more warps stay resident than with a thread per
+// vertex, and a neighbour costs a team one load and three integer
+// operations per mask instead of a thread's serial chain. LIGHT: the solve
+// prunes, only light neighbour states grow (light_or_inf).
+template <int G, int UNR, bool LIGHT>
+__device__ __forceinline__ void team_vertex(const GraphDev& g, const LevelArgs& a, const RoundState& rs, int32_t u,
+                                            int glane, unsigned tmask, uint32_t (&acc)[kAccN]) {
+  constexpr int S = 4 * G;
+  const int32_t beg = g.row_ptr[u], end = g.row_ptr[u + 1];
+  if (end - beg > g.deg_big) return;  // hub: relaxed in 32-entry chunks (hub_relax)
+  const int64_t rowu = a.base + (int64_t)u * S;
+  const int4 own4 = reinterpret_cast<const int4*>(a.cost + rowu)[glane];
+  const int32_t own[4] = {own4.x, own4.y, own4.z, own4.w};
+  int32_t best[4] = {own4.x, own4.y, own4.z, own4.w};
+  int32_t code[4] = {-1, -1, -1, -1};
+  bool live = false;
+#pragma unroll
+  for (int t = 0; t < 4; ++t) live |= 4 * glane + t < a.m && own[t] != 0;  // cost-0 states cannot improve
+  if (glane == 0) {
+    ++acc[kAccVert];
+    acc[kAccEnt] += end - beg;
+  }
+  if (!(__ballot_sync(tmask, live) & tmask)) return;
+  const int4* tab = reinterpret_cast<const int4*>(a.cost + a.base);
+  for (int32_t e0 = beg; e0 < end; e0 += UNR) {
+    int2 x[UNR];
+#pragma unroll
+    for (int i = 0; i < UNR; ++i) x[i] = g.adj[min(e0 + i, end - 1)];
+    int4 r[UNR];
+#pragma unroll
+    for (int i = 0; i < UNR; ++i) r[i] = tab[(int64_t)x[i].x * G + glane];
+#pragma unroll
+    for (int i = 0; i < UNR; ++i) {
+      if (e0 + i < end) {
+        const int32_t rv[4] = {r[i].x, r[i].y, r[i].z, r[i].w};
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+          // a kInf (or, pruning, heavy) entry gives c >= kInf and never wins;
+          // stored costs stay below ovf_limit, so c cannot wrap
+          const int32_t c = (LIGHT ? light_or_inf(rv[t], rs.ub_light) : rv[t]) + x[i].y;
+          if (c < best[t]) {
+            best[t] = c;
+            code[t] = e0 + i;
+          }
+        }
+      }
+    }
+  }
+  if (glane == 0) acc[kAccRows] += end - beg;
+  bool imp = false;
+#pragma unroll
+  for (int t = 0; t < 4; ++t) {
+    if (code[t] < 0) continue;
+    if (best[t] >= rs.ovf_limit) acc[kAccOverflow] = 1;
+    if (rs.ub > 0 && best[t] > cap_at(a, u, 4 * glane + t)) {  // over the state's cap: keep the stored value
+      best[t] = own[t];
+      code[t] = -1;
+      continue;
+    }
+    imp = true;
+  }
+  if (imp) {
+    reinterpret_cast<int4*>(a.cost + rowu)[glane] = make_int4(best[0], best[1], best[2], best[3]);
+#pragma unroll
+    for (int t = 0; t < 4; ++t)
+      if (code[t] >= 0) {
+        a.par[rowu + 4 * glane + t] = code[t];
+        ++acc[kAccImproved];
+      }
+  }
+  if ((__ballot_sync(tmask, imp) & tmask) && glane == 0) {
+    rs.next_flag[u] = 1;
+    ++acc[kAccChanged];
+  }
+}
+
+// The dense rounds of waves whose stride is 4G (sparse rounds return at
+// once: k_grow_thread runs them). Hubs first (32-entry chunks), then the
+// other vertices in growth order: a warp takes 32 sweep positions at a time
+// from the round's counter, its 32/G teams take them in turn. Odd rounds
+// sweep backwards, as the thread kernel does.
+template <int G, int UNR>
+__global__ void __launch_bounds__(kGrowThreads, (G <= 4 ? 4 : 3)) k_grow_team(GraphDev g, LevelArgs a) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&a.ctr->grow_launches, 1);
+  RoundState rs;
+  if (!round_begin(g, a, rs)) return;
+  if (!rs.dense) return;
+  __shared__ BlockAcc ba;
+  block_acc_init(ba);
+  uint32_t acc[kAccN] = {0, 0, 0, 0, 0, 0, 0};
+  const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
+  clear_flags(a, rs, t0, nthreads);
+  hub_relax_team<(G <= 1 ? 1 : G <= 2 ? 2 : G <= 4 ? 4 : 8)>(g, a, rs, acc);
+  constexpr int T = 32 / G;  // teams per warp; lanes T*G .. 31 idle
+  const int lane = threadIdx.x & 31;
+  const int team = lane / G, glane = lane - team * G;
+  const unsigned tmask = team < T ? (G == 32 ? 0xffffffffu : ((1u << G) - 1u) << (team * G)) : 0u;
+  uint32_t* work = &a.ctl->work[rs.r % 3];
+  const bool light = rs.ub_light > 0;
+  for (;;) {
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(work, (uint32_t)kDenseGrab);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if ((int64_t)base >= g.nsmall) break;
+    if (team < T) {
+      for (int p = team; p < kDenseGrab; p += T) {
+        const int64_t i = (int64_t)base + p;
+        if (i >= g.nsmall) break;
+        const int32_t u = g.order[(rs.r & 1) ? g.nsmall - 1 - i : i];
+        if (light)
+          team_vertex<G, UNR, true>(g, a, rs, u, glane, tmask, acc);
+        else
+          team_vertex<G, UNR, false>(g, a, rs, u, glane, tmask, acc);
+      }
+    }
+    __syncwarp();
+  }
+  round_end(a, rs, acc, ba);
+}
+
 // G lanes per vertex for waves wider than kMaxThreadMasks. Each warp takes
 // 32 consecutive vertices at a time, finds the candidates among them with
 // one ballot, and its 32/G groups take the candidates in turn.
 template <int G, int L>
 __global__ void __launch_bounds__(kGrowThreads, (L >= 3 ? 3 : 4)) k_grow_group(GraphDev g, LevelArgs a) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&a.ctr->grow_launches, 1);
   RoundState rs;
   if (!round_begin(g, a, rs)) return;
   __shared__ BlockAcc ba;
@@ -1622,6 +1907,19 @@ cudaError_t hub_round(const GraphDev& g, const LevelArgs& a, int num_sms, cudaSt
   return cudaGetLastError();
 }
 
+template <int GP>
+cudaError_t hub_team_round(const GraphDev& g, const LevelArgs& a, int num_sms, cudaStream_t stream,
+                           int64_t* launches) {
+  if (g.nchunks == 0) return cudaSuccess;
+  static const int occ = resident_blocks(k_grow_hubs_team<GP>);
+  const int64_t warps_per_block = kGrowThreads / 32;
+  int64_t blocks = (g.nchunks + warps_per_block - 1) / warps_per_block;
+  if (blocks > (int64_t)num_sms * occ) blocks = (int64_t)num_sms * occ;
+  k_grow_hubs_team<GP><<<(unsigned)blocks, kGrowThreads, 0, stream>>>(g, a);
+  ++*launches;
+  return cudaGetLastError();
+}
+
 template <int MP>
 cudaError_t thread_round(const GraphDev& g, const LevelArgs& a, int num_sms, cudaStream_t stream) {
   static const int occ = resident_blocks(k_grow_thread<MP>);
@@ -1635,23 +1933,52 @@ cudaError_t group_round(const GraphDev& g, const LevelArgs& a, int num_sms, cuda
 }
 }  // namespace
 
+template <int G>
+cudaError_t team_round(const GraphDev& g, const LevelArgs& a, int num_sms, cudaStream_t stream) {
+  constexpr int UNR = 4;
+  static const int occ = resident_blocks(k_grow_team<G, UNR>);
+  return launch_round(k_grow_team<G, UNR>, occ, g, a, num_sms, kGrowThreads / G, stream);
+}
+
 cudaError_t launch_grow_round(const GraphDev& g, const LevelArgs& a, int num_sms, cudaStream_t stream,
                               int64_t* launches) {
   const int lanes = (a.stride + 31) / 32;  // masks per lane in the hub kernel, in passes of at most 4
-  const cudaError_t he = lanes <= 1   ? hub_round<1>(g, a, num_sms, stream, launches)
+  const int G = a.stride >> 2;
+  const cudaError_t he = a.stride <= kMaxThreadMasks
+                             ? (G <= 1   ? hub_team_round<1>(g, a, num_sms, stream, launches)
+                                : G <= 2 ? hub_team_round<2>(g, a, num_sms, stream, launches)
+                                : G <= 4 ? hub_team_round<4>(g, a, num_sms, stream, launches)
+                                         : hub_team_round<8>(g, a, num_sms, stream, launches))
+                         : lanes <= 1 ? hub_round<1>(g, a, num_sms, stream, launches)
                          : lanes == 2 ? hub_round<2>(g, a, num_sms, stream, launches)
                          : lanes == 3 ? hub_round<3>(g, a, num_sms, stream, launches)
                                       : hub_round<4>(g, a, num_sms, stream, launches);
   if (he != cudaSuccess) return he;
   ++*launches;
+  // waves with a thread kernel: sparse rounds there, then dense rounds in the
+  // team kernel (each of the two returns at once in the other's rounds; a
+  // dense round that follows a sparse one in the same pass runs right away)
+  cudaError_t te = cudaSuccess;
   switch (a.stride) {
-    case 4: return thread_round<4>(g, a, num_sms, stream);
-    case 8: return thread_round<8>(g, a, num_sms, stream);
-    case 12: return thread_round<12>(g, a, num_sms, stream);
-    case 16: return thread_round<16>(g, a, num_sms, stream);
-    case 20: return thread_round<20>(g, a, num_sms, stream);
-    case 24: return thread_round<24>(g, a, num_sms, stream);
-    default: break;
+    case 4: te = thread_round<4>(g, a, num_sms, stream); break;
+    case 8: te = thread_round<8>(g, a, num_sms, stream); break;
+    case 12: te = thread_round<12>(g, a, num_sms, stream); break;
+    case 16: te = thread_round<16>(g, a, num_sms, stream); break;
+    case 20: te = thread_round<20>(g, a, num_sms, stream); break;
+    case 24: te = thread_round<24>(g, a, num_sms, stream); break;
+    default: te = cudaErrorNotSupported; break;
+  }
+  if (te != cudaErrorNotSupported) {
+    if (te != cudaSuccess) return te;
+    ++*launches;
+    switch (a.stride) {
+      case 4: return team_round<1>(g, a, num_sms, stream);
+      case 8: return team_round<2>(g, a, num_sms, stream);
+      case 12: return team_round<3>(g, a, num_sms, stream);
+      case 16: return team_round<4>(g, a, num_sms, stream);
+      case 20: return team_round<5>(g, a, num_sms, stream);
+      default: return team_round<6>(g, a, num_sms, stream);
+    }
   }
   if (a.stride <= 32) return group_round<16, 2>(g, a, num_sms, stream);
   if (a.stride <= 64) return group_round<32, 2>(g, a, num_sms, stream);

@@ -857,6 +857,7 @@ gst_status solve_one(gst_graph* g, const int32_t* group_ptr, const int32_t* memb
     if (st != GST_OK) return st;
     if (timeout) {
       GST_CUDA(cudaStreamSynchronize(s));
+      r->launches = launches;
       return fail(GST_TIMEOUT, "growth did not converge within max_rounds");
     }
   }
@@ -864,11 +865,11 @@ gst_status solve_one(gst_graph* g, const int32_t* group_ptr, const int32_t* memb
   GST_CUDA(cudaStreamSynchronize(s));
   const Counters& c = *ws.h_ctr;
   // masks, k merges, a seed per grown wave, a refinement per grown wave but
-  // the last, the tour tables (k <= kTourMaxK, waves 2..k-1), the rounds,
-  // argmin and backtrack
+  // the last, the tour tables (k <= kTourMaxK, waves 2..k-1), the growth
+  // kernels (each launch counts itself on the device), argmin and backtrack
   if (use_graph)
     launches = 1 + k + (k - 1) + std::max(k - 2, 0) + (k <= kTourMaxK ? std::max(k - 2, 0) : 0) +
-               (int64_t)c.rounds_total * (g->nchunks > 0 ? 2 : 1) + 2;
+               (int64_t)c.grow_launches + 2;
   r->ub = ws.h_params->ub;  // the bound as the last wave saw it (refined on the device)
   r->launches = launches;
   r->states = (int64_t)c.states;
@@ -1235,11 +1236,9 @@ gst_status propose_tree(gst_graph* g, const gst_scorer* sc, const int32_t* group
   o1.max_rounds = kProposeRounds;
   gst_result tmp;
   st = solve_one(g, gp1, mem1, 2, o1, &tmp);
-  if (st == GST_TIMEOUT) {
+  if (st == GST_TIMEOUT) {  // the capped rounds ran out: the distances so far are actual paths
     st = GST_OK;
     g_last_error.clear();
-    // a capped solve stops before its epilogue: the round loop's launches
-    tmp.launches = 1 + 2 + 1 + (int64_t)kProposeRounds * (g->nchunks > 0 ? 2 : 1);
   }
   if (st != GST_OK) return st;
   launches += tmp.launches + 1;  // + the path walk
