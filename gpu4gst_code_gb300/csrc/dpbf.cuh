@@ -104,6 +104,7 @@ struct Counters {
   int32_t rounds_total; // growth rounds that did work, all waves
   int32_t timeout;
   int32_t grow_launches;      // growth-round kernels launched (each counts itself)
+  int32_t pad;
   unsigned long long best;    // (cost << 32) | root, argmin of the full mask
   unsigned long long states;  // states written by merges + growth
 };
@@ -161,9 +162,10 @@ struct LevelArgs {
   const int32_t* tour;
 };
 
-// Groups up to which the merge adds the tour bound to the one-label bound
-// (the staged merge's limit).
-constexpr int kTourMaxK = 8;
+// Groups up to which the merge adds PrunedDP++'s tour bounds to the one-label
+// bound (k_tour_table keeps the k x 2^k x k path table in shared memory:
+// 162 KB at k = 9).
+constexpr int kTourMaxK = 9;
 
 // Queries with at most kMergeTabK groups merge a vertex per thread from
 // per-level split tables (k_merge_vertex); larger k use k_merge.

@@ -12,6 +12,7 @@
 //                   (:259-282): one label-correcting round, pull form
 //   k_argmin        host min scan over T(v,full) (:712-721)
 //   k_backtrack     host BFS over parent records (:729-758)
+#include <algorithm>
 #include <climits>
 #include <cstdint>
 
@@ -126,6 +127,29 @@ __device__ __forceinline__ int32_t label_bound(const int32_t (&dd)[16], uint32_t
 // the wave's merge wrote (read-only during the wave).
 __device__ __forceinline__ int32_t cap_at(const LevelArgs& a, int32_t v, int j) {
   return __ldg(a.capt + (int64_t)v * a.stride + j);
+}
+
+// PrunedDP++'s tour bounds of (v, X) for the merges that do not stage rows
+// (k_merge_vertex): wave-1 distances read from global memory (d1 = v's wave-1
+// row), capped at beyond = ub/2 + 1; lb1 over unordered end pairs i < j of
+// the path table, lb2 over W2 (k_tour_table). Sums stay below 2^31
+// (unsigned): each is at most ub / 2 + 1 + ub + ub / 2 + 1.
+__device__ __forceinline__ int32_t tour_bound(const LevelArgs& a, const int32_t* d1, uint32_t beyond, uint32_t X) {
+  const int32_t* w2 = a.tour + ((int64_t)a.k << a.k) * a.k;
+  uint32_t dmin = 0xffffffffu;
+  for (uint32_t xi = X; xi; xi &= xi - 1u) dmin = min(dmin, min((uint32_t)__ldg(d1 + __ffs(xi) - 1), beyond));
+  int32_t lb1 = INT_MAX, lb2 = 0;
+  for (uint32_t xi = X; xi; xi &= xi - 1u) {
+    const int i = __ffs(xi) - 1;
+    const uint32_t di = min((uint32_t)__ldg(d1 + i), beyond);
+    const int32_t* fi = a.tour + (((int64_t)i << a.k) | X) * a.k;
+    lb2 = max(lb2, (int32_t)((di + (uint32_t)__ldg(w2 + ((int64_t)i << a.k) + X) + dmin) >> 1));
+    for (uint32_t xj = xi & (xi - 1u); xj; xj &= xj - 1u) {
+      const int i2 = __ffs(xj) - 1;
+      lb1 = min(lb1, (int32_t)((di + (uint32_t)__ldg(fi + i2) + min((uint32_t)__ldg(d1 + i2), beyond)) >> 1));
+    }
+  }
+  return max(lb1, lb2);
 }
 
 // ------------------------------------------------------------------ merge --
@@ -296,18 +320,29 @@ __global__ void __launch_bounds__(NT) k_merge_staged(GraphDev g, LevelArgs a, Me
           if (ub > 0 && a.tour && __popc(X) >= 2) {
             // PrunedDP++'s tour bound (graph_v_of_v_idealID_PrunedDPPlusPlus.h:268-386):
             // a tree joining v to the groups of X is at least half a walk
-            // from v through all of them, over lower bounds of every leg
-            int32_t lb1 = INT_MAX;
+            // from v through all of them, over lower bounds of every leg.
+            // The walk's first and last groups i != j are taken as
+            // unordered pairs i < j: the path table is symmetric (a path
+            // reversed), and its i = j entries are no walks
+            // PrunedDP++'s second bound lb2 (PrunedDPPlusPlus.h:454-466):
+            // the walk passes through every group i of X, so it costs at
+            // least d(v,i) + W2[i][X] (the cheapest order from i over X)
+            // + the distance back from the nearest group of X, halved
+            int32_t lb1 = INT_MAX, lb2 = 0, dmin = INT_MAX;
+            for (uint32_t xi = X; xi; xi &= xi - 1u) dmin = min(dmin, (int32_t)min(colu[(__ffs(xi) - 1) * NT], beyond));
+            const int32_t* w2 = a.tour + ((int64_t)a.k << a.k) * a.k;
             for (uint32_t xi = X; xi; xi &= xi - 1u) {
               const int i = __ffs(xi) - 1;
               const int32_t di = (int32_t)min(colu[i * NT], beyond);
               const int32_t* fi = a.tour + (((int64_t)i << a.k) | X) * a.k;
-              for (uint32_t xj = X; xj; xj &= xj - 1u) {
+              // each sum is at most ub / 2 + 1 + ub + ub / 2 + 1: unsigned, no wrap
+              lb2 = max(lb2, (int32_t)(((uint32_t)di + (uint32_t)__ldg(w2 + ((int64_t)i << a.k) + X) + (uint32_t)dmin) >> 1));
+              for (uint32_t xj = xi & (xi - 1u); xj; xj &= xj - 1u) {
                 const int i2 = __ffs(xj) - 1;
-                lb1 = min(lb1, (di + __ldg(fi + i2) + (int32_t)min(colu[i2 * NT], beyond)) >> 1);
+                lb1 = min(lb1, (int32_t)(((uint32_t)di + (uint32_t)__ldg(fi + i2) + min(colu[i2 * NT], beyond)) >> 1));
               }
             }
-            lb = max(lb, lb1);
+            lb = max(lb, max(lb1, lb2));
           }
           const int32_t cap = ub > 0 ? ub - lb : kInf;
           k4[t] = cap < 0 ? -1 : cap;
@@ -382,6 +417,9 @@ __global__ void __launch_bounds__(kGrowThreads) k_merge_vertex(GraphDev g, Level
     const uint32_t gm = __ldg(a.gmask + v);
     int32_t dd[16];
     if (ub > 0) load_label_bound(a, ub, (int32_t)v, dd);
+    const int32_t* d1 = a.cost + v * a.stride1;  // wave 1 (rank of {g} is g), for the tour bound
+    const uint32_t beyond = (uint32_t)(ub / 2 + 1);
+    const uint32_t full = (1u << a.k) - 1u;
     int4* rowc = reinterpret_cast<int4*>(a.cost + a.base + v * a.stride);
     int4* rowp = reinterpret_cast<int4*>(a.par + a.base + v * a.stride);
     int4* rowk = reinterpret_cast<int4*>(a.capt + v * a.stride);
@@ -396,7 +434,10 @@ __global__ void __launch_bounds__(kGrowThreads) k_merge_vertex(GraphDev g, Level
         if (j < a.m) {
           const uint32_t S = (uint32_t)__ldg(a.lmasks + j);
           if ((gm & S) == S) best = 0;
-          const int32_t cap = ub > 0 ? ub - label_bound(dd, S) : kInf;
+          int32_t lb = ub > 0 ? label_bound(dd, S) : 0;
+          const uint32_t X = full ^ S;
+          if (ub > 0 && a.tour && __popc(X) >= 2) lb = max(lb, tour_bound(a, d1, beyond, X));
+          const int32_t cap = ub > 0 ? ub - lb : kInf;
           k4[t] = cap < 0 ? -1 : cap;
           if (cap < 0) {
             best = kInf;
@@ -490,6 +531,7 @@ constexpr int kWarpMarkMax = 16;  // changed rows of a warp up to which its lane
 
 struct RoundState {
   int32_t r;
+  int32_t prev;  // vertices the previous round changed
   bool dense, all_cand, stats;
   int32_t ub;        // pruning bound (waves >= 2; states are capped by the wave's cap table)
   int32_t ub_light;  // only states with 2 * cost <= ub_light grow (all waves)
@@ -510,7 +552,10 @@ __device__ __forceinline__ bool round_begin(const GraphDev& g, const LevelArgs& 
   const GrowCtl* ctl = a.ctl;
   rs.r = ctl->round;
   const int32_t prev = ctl->changed[(rs.r + 2) % 3];
-  if (prev == 0) {  // nothing changed in the previous round: converged
+  rs.prev = prev;
+  // converged (nothing changed in the previous round), or out of rounds: a
+  // later kernel of the same pass must not run another round
+  if (prev == 0 || ctl->timeout) {  // nothing changed in the previous round (converged), or out of rounds
     if (a.use_cond && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(a.cond, 0);
     return false;
   }
@@ -1153,83 +1198,41 @@ __device__ __forceinline__ bool thread_vertex(const GraphDev& g, const LevelArgs
       }
     }
   };
-  if (rs.dense) {
-    // every neighbour; software pipeline: the next batch's CSR entries are
-    // loaded while this batch's rows are gathered
-    int32_t nv[U], nw[U];
-    bool act[U];
+  // sparse rounds only (dense rounds run in k_grow_team): first the change
+  // flags of every CSR entry (8
+  // independent loads at a time) into a bit mask, then only the changed
+  // neighbours' rows, U at a time: the loop no longer waits on a flag
+  // load per pair of entries
+  uint64_t actm = 0;  // rows are at most kDegBigMax = 64 entries long
+  for (int32_t e0 = beg; e0 < end; e0 += 8) {
+    int32_t nb[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) nb[i] = e0 + i < end ? g.adj[e0 + i].x : -1;
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+      if (nb[i] >= 0 && rs.cur_flag[nb[i]] != 0) actm |= 1ull << (e0 + i - beg);  // e0 + i < end: shift < 64
+  }
+  while (actm) {
+    bool ok[U];
+    uint32_t rel[U];
+    int32_t nvx[U], nwx[U];
 #pragma unroll
     for (int i = 0; i < U; ++i) {
-      act[i] = beg + i < end;
-      nv[i] = 0;
-      nw[i] = 0;
-      if (act[i]) {
-        const int2 x = g.adj[beg + i];
-        nv[i] = x.x;
-        nw[i] = x.y;
+      ok[i] = actm != 0ull;
+      rel[i] = ok[i] ? (uint32_t)(__ffsll((long long)actm) - 1) : 0u;
+      if (ok[i]) actm &= actm - 1ull;
+      nvx[i] = 0;
+      nwx[i] = 0;
+    }
+#pragma unroll
+    for (int i = 0; i < U; ++i) {
+      if (ok[i]) {
+        const int2 x = g.adj[beg + (int32_t)rel[i]];
+        nvx[i] = x.x;
+        nwx[i] = x.y;
       }
     }
-    for (int32_t e0 = beg; e0 < end; e0 += U) {
-      int32_t nv2[U], nw2[U];
-      bool act2[U];
-#pragma unroll
-      for (int i = 0; i < U; ++i) {
-        act2[i] = e0 + U + i < end;
-        nv2[i] = 0;
-        nw2[i] = 0;
-        if (act2[i]) {
-          const int2 x = g.adj[e0 + U + i];
-          nv2[i] = x.x;
-          nw2[i] = x.y;
-        }
-      }
-      uint32_t rel[U];
-#pragma unroll
-      for (int i = 0; i < U; ++i) rel[i] = (uint32_t)(e0 + i - beg);
-      relax_batch(act, nv, nw, rel);
-#pragma unroll
-      for (int i = 0; i < U; ++i) {
-        nv[i] = nv2[i];
-        nw[i] = nw2[i];
-        act[i] = act2[i];
-      }
-    }
-  } else {
-    // sparse rounds: first the change flags of every CSR entry (8
-    // independent loads at a time) into a bit mask, then only the changed
-    // neighbours' rows, U at a time: the loop no longer waits on a flag
-    // load per pair of entries
-    uint64_t actm = 0;  // rows are at most kDegBigMax = 64 entries long
-    for (int32_t e0 = beg; e0 < end; e0 += 8) {
-      int32_t nb[8];
-#pragma unroll
-      for (int i = 0; i < 8; ++i) nb[i] = e0 + i < end ? g.adj[e0 + i].x : -1;
-#pragma unroll
-      for (int i = 0; i < 8; ++i)
-        if (nb[i] >= 0 && rs.cur_flag[nb[i]] != 0) actm |= 1ull << (e0 + i - beg);  // e0 + i < end: shift < 64
-    }
-    while (actm) {
-      bool ok[U];
-      uint32_t rel[U];
-      int32_t nvx[U], nwx[U];
-#pragma unroll
-      for (int i = 0; i < U; ++i) {
-        ok[i] = actm != 0ull;
-        rel[i] = ok[i] ? (uint32_t)(__ffsll((long long)actm) - 1) : 0u;
-        if (ok[i]) actm &= actm - 1ull;
-        nvx[i] = 0;
-        nwx[i] = 0;
-      }
-#pragma unroll
-      for (int i = 0; i < U; ++i) {
-        if (ok[i]) {
-          const int2 x = g.adj[beg + (int32_t)rel[i]];
-          nvx[i] = x.x;
-          nwx[i] = x.y;
-        }
-      }
-      relax_batch(ok, nvx, nwx, rel);
-    }
+    relax_batch(ok, nvx, nwx, rel);
   }
   bool any = false;
 #pragma unroll
@@ -1317,22 +1320,18 @@ __device__ __forceinline__ void warp_mark(const GraphDev& g, const LevelArgs& a,
   }
 }
 
+// A sparse round of a wave with row stride MP <= kMaxThreadMasks, after its
+// hub chunks ran (k_grow_hubs_team): flags of two rounds back cleared, the
+// changed hubs' neighbours marked, then every candidate (or, in the round
+// after a dense one, every vertex) relaxed by a thread and the neighbours
+// its new row improves marked (warp_mark).
 template <int MP>
-__global__ void __launch_bounds__(kGrowThreads, (MP <= 16 ? 3 : 2)) k_grow_thread(GraphDev g, LevelArgs a) {
-  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&a.ctr->grow_launches, 1);
-  RoundState rs;
-  if (!round_begin(g, a, rs)) return;
-  if (rs.dense) return;  // dense rounds run in k_grow_team
-  __shared__ BlockAcc ba;
-  block_acc_init(ba);
-  uint32_t acc[kAccN] = {0, 0, 0, 0, 0, 0, 0};
+__device__ __forceinline__ void thread_round_body(const GraphDev& g, const LevelArgs& a, const RoundState& rs,
+                                                  uint32_t (&acc)[kAccN]) {
   const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
   clear_flags(a, rs, t0, nthreads);
-  if (rs.dense)
-    hub_relax<(MP + 31) / 32>(g, a, rs, acc);
-  else
-    hub_mark(g, a, rs, acc);
+  hub_mark(g, a, rs, acc);
   // warps take their work from the round's counter, so blocks that draw
   // cheap vertices (or tiles without candidates) take more of them and no
   // SM idles while another finishes a fixed share
@@ -1393,6 +1392,18 @@ __global__ void __launch_bounds__(kGrowThreads, (MP <= 16 ? 3 : 2)) k_grow_threa
       __syncwarp();
     }
   }
+}
+
+template <int MP>
+__global__ void __launch_bounds__(kGrowThreads, (MP <= 16 ? 3 : 2)) k_grow_thread(GraphDev g, LevelArgs a) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&a.ctr->grow_launches, 1);
+  RoundState rs;
+  if (!round_begin(g, a, rs)) return;
+  if (rs.dense) return;  // dense rounds run in k_grow_team
+  __shared__ BlockAcc ba;
+  block_acc_init(ba);
+  uint32_t acc[kAccN] = {0, 0, 0, 0, 0, 0, 0};
+  thread_round_body<MP>(g, a, rs, acc);
   round_end(a, rs, acc, ba);
 }
 
@@ -1726,6 +1737,19 @@ __global__ void __launch_bounds__(256) k_tour_table(LevelArgs a, const int32_t* 
     __syncthreads();
   }
   for (int t = threadIdx.x; t < k * W * k; t += blockDim.x) tour[t] = F[t];
+  // W2[i][X] = the cheapest order visiting X from i, ending at any group
+  // j != i (0 for X = {i}): PrunedDP++'s W2 (PrunedDPPlusPlus.h:565-585)
+  for (int t = threadIdx.x; t < k * W; t += blockDim.x) {
+    const int i = t / W, X = t % W;
+    int32_t best = ub;
+    if (X == (1 << i)) {
+      best = 0;
+    } else if ((X >> i) & 1) {
+      for (int j = 0; j < k; ++j)
+        if (j != i && ((X >> j) & 1)) best = min(best, F[((i << k) | X) * k + j]);
+    }
+    tour[k * W * k + t] = best;
+  }
 }
 
 __global__ void k_argmin(int32_t V, const int32_t* __restrict__ full_slice, int32_t stride, Counters* ctr) {
@@ -1972,13 +1996,14 @@ cudaError_t launch_grow_round(const GraphDev& g, const LevelArgs& a, int num_sms
     if (te != cudaSuccess) return te;
     ++*launches;
     switch (a.stride) {
-      case 4: return team_round<1>(g, a, num_sms, stream);
-      case 8: return team_round<2>(g, a, num_sms, stream);
-      case 12: return team_round<3>(g, a, num_sms, stream);
-      case 16: return team_round<4>(g, a, num_sms, stream);
-      case 20: return team_round<5>(g, a, num_sms, stream);
-      default: return team_round<6>(g, a, num_sms, stream);
+      case 4: te = team_round<1>(g, a, num_sms, stream); break;
+      case 8: te = team_round<2>(g, a, num_sms, stream); break;
+      case 12: te = team_round<3>(g, a, num_sms, stream); break;
+      case 16: te = team_round<4>(g, a, num_sms, stream); break;
+      case 20: te = team_round<5>(g, a, num_sms, stream); break;
+      default: te = team_round<6>(g, a, num_sms, stream); break;
     }
+    return te;
   }
   if (a.stride <= 32) return group_round<16, 2>(g, a, num_sms, stream);
   if (a.stride <= 64) return group_round<32, 2>(g, a, num_sms, stream);

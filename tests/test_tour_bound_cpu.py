@@ -49,14 +49,41 @@ def tour_tables(d, group_ptr, members, ub):
     return dc, F
 
 
-def lower_bound(dc, F, X):
-    """LB(v, X) for every v: max(one-label, tour) as the merge takes it."""
+def path_from(F, X):
+    """W2[i] = the cheapest order visiting every group of X from group i,
+    ending anywhere: min over j != i of path[i][X][j] (0 when X = {i})."""
+    k = F.shape[0]
+    gs = [g for g in range(k) if (X >> g) & 1]
+    out = {}
+    for i in gs:
+        out[i] = 0 if len(gs) == 1 else min(int(F[i, X, j]) for j in gs if j != i)
+    return out
+
+
+def second_bound(dc, F, X):
+    """PrunedDP++'s lb2 (graph_v_of_v_idealID_PrunedDPPlusPlus.h:454-466):
+    max over i in X of (d(v,i) + W2[i][X] + min_j d(v,j)) / 2."""
+    gs = [g for g in range(dc.shape[1]) if (X >> g) & 1]
+    w2 = path_from(F, X)
+    dmin = dc[:, gs].min(axis=1)
+    lb = np.zeros(dc.shape[0], np.int64)
+    for i in gs:
+        lb = np.maximum(lb, (dc[:, i] + w2[i] + dmin) // 2)
+    return lb
+
+
+def lower_bound(dc, F, X, pairs_only=False):
+    """LB(v, X) for every v: max(one-label, tour) as the merge takes it.
+    pairs_only: the end groups as unordered pairs i < j, which is what the
+    merge evaluates: the path table is symmetric, and its i = j entries are
+    not walks (they hold the clamp), so leaving them out keeps the bound
+    valid and can only raise it."""
     gs = [g for g in range(dc.shape[1]) if (X >> g) & 1]
     lb = dc[:, gs].max(axis=1)
     if len(gs) >= 2:
         tour = np.full(dc.shape[0], np.iinfo(np.int64).max)
-        for i in gs:
-            for j in gs:
+        for a, i in enumerate(gs):
+            for j in (gs[a + 1:] if pairs_only else gs):
                 tour = np.minimum(tour, (dc[:, i] + F[i, X, j] + dc[:, j]) // 2)
         lb = np.maximum(lb, tour)
     return lb
@@ -85,8 +112,13 @@ def test_tour_bound_never_exceeds_the_cheapest_completion(kind, V, k, seed):
     stronger = 0
     for ub in (opt, 2 * opt, 1 << 29):  # any bound caps the distances validly
         dc, F = tour_tables(d, gp, mem, ub)
+        # the path table is symmetric: the cheapest order from i to j reversed
+        assert np.array_equal(F, F.transpose(2, 1, 0))
         for X in range(1, full + 1):
-            lb = lower_bound(dc, F, X)
+            lb_all = lower_bound(dc, F, X)
+            lb = lower_bound(dc, F, X, pairs_only=True)
+            assert np.all(lb >= lb_all)
+            lb = np.maximum(lb, second_bound(dc, F, X))
             t = T[:, X]
             fin = t < oracle.INF
             assert np.all(lb[fin] <= t[fin]), (ub, X, int(np.argmax(lb - np.where(fin, t, 0))))
