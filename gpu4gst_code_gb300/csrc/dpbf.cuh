@@ -30,6 +30,9 @@ constexpr int32_t kLeaf = INT32_MIN;
 constexpr int kDegBigMin = 32;
 constexpr int kDegBigMax = 64;
 constexpr int kGrowThreads = 256;  // block size of growth / merge kernels
+// Longest hub segment a warp relaxes in registers (hubs up to this degree
+// are relaxed whole, with no scratch row).
+constexpr int kHubSeg = 256;
 constexpr int kMaxThreadMasks = 24;  // waves with stride <= this: a thread per vertex (sparse rounds)
 // Dense rounds of waves with stride <= this run a team of stride/4 lanes per
 // vertex, each lane holding four masks (k_grow_team).
@@ -121,6 +124,10 @@ struct GraphDev {
   const int2* hub_chunk;   // (hub index, first CSR entry) per 32-entry chunk
   const int32_t* chunk_vtx;  // the hub vertex of each chunk
   int64_t nchunks;
+  // hub rows cut into segments of at most kHubSeg entries, relaxed by one
+  // warp each: (hub vertex, hub index, first CSR entry, segments of that hub)
+  const int4* hub_seg;
+  int64_t nsegs;
   unsigned long long* hub_min;  // per hub: hub_stride packed (cost, entry) minima
   int32_t* hub_cnt;             // per hub: chunks finished this round
   int32_t hub_stride;

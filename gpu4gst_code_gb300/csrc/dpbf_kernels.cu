@@ -868,63 +868,70 @@ __device__ __forceinline__ void hub_relax(const GraphDev& g, const LevelArgs& a,
   }
 }
 
-// Hub chunks of waves with stride 4G <= kMaxTeamStride, all 32 entries in
-// flight at once: the warp compacts the chunk's active entries (dense
-// rounds: all; sparse rounds: those whose neighbour changed) into shared
-// memory, then splits into 32/GP teams of GP lanes (GP = G rounded up to a
-// power of two; lanes G .. GP-1 of a team idle). Team t takes active
-// entries t, t + T, ... four at a time, lane q loading the 16-byte quarter
-// q of each neighbour's row, so the warp has up to 32 rows in flight where
-// a mask-per-lane walk has four. The teams' minima are combined by
-// shuffles; team 0 folds them into the hub's scratch row and the chunk
-// completes as in hub_chunk_relax (the last chunk of a hub applies the
-// row).
+// Hub rows of waves with stride 4G <= kMaxTeamStride, relaxed a segment of
+// up to kHubSeg entries per warp. The warp walks the segment 32 entries at
+// a time: it compacts the active entries (dense rounds: all; sparse rounds:
+// those whose neighbour changed) into shared memory, then splits into 32/GP
+// teams of GP lanes (GP = G rounded up to a power of two; lanes G .. GP-1
+// of a team idle); team t takes active entries t, t + T, ... four at a
+// time, lane q loading the 16-byte quarter q of each neighbour's row, so up
+// to 32 rows are in flight, and folds them into running minima held in
+// registers. At the end the teams' minima are combined by shuffles. A hub
+// of one segment (degree <= kHubSeg: almost every hub) is then applied to
+// its row directly by team 0, its only writer; the segments of a larger
+// hub fold into the hub's scratch row and the last one to finish applies
+// it, as in hub_chunk_relax.
 template <int GP>
-__device__ __forceinline__ void hub_chunk_team(const GraphDev& g, const LevelArgs& a, const RoundState& rs,
-                                               int64_t c, int4* wbuf, uint32_t (&acc)[kAccN]) {
+__device__ __forceinline__ void hub_seg_team(const GraphDev& g, const LevelArgs& a, const RoundState& rs,
+                                             int64_t sidx, int4* wbuf, uint32_t (&acc)[kAccN]) {
   constexpr int T = 32 / GP;
   const int lane = threadIdx.x & 31;
   const int team = lane / GP, glane = lane - team * GP;
   const int G = a.stride >> 2;
   const int32_t s = a.stride;
-  const int32_t u = g.chunk_vtx[c];
-  const int2 hc = g.hub_chunk[c];  // (hub index, first CSR entry of the chunk)
+  const int4 sg = g.hub_seg[sidx];  // (hub vertex, hub index, first entry, segments of the hub)
+  const int32_t u = sg.x;
   const int32_t beg = g.row_ptr[u], end = g.row_ptr[u + 1];
-  const int32_t cend = min(end, hc.y + 32);
-  const int32_t e = hc.y + lane;
-  int2 x = make_int2(0, 0);
-  bool act = false;
-  if (e < cend) {
-    x = g.adj[e];
-    act = rs.dense || rs.cur_flag[x.x] != 0;
-  }
-  const unsigned bal = __ballot_sync(0xffffffffu, act);
-  const int n = __popc(bal);
-  if (act) wbuf[__popc(bal & ((1u << lane) - 1u))] = make_int4(x.x, x.y, e, 0);
-  __syncwarp();
+  const int32_t e1 = min(end, sg.z + kHubSeg);
   int32_t best[4] = {kInf, kInf, kInf, kInf};
   int32_t code[4] = {-1, -1, -1, -1};
   const bool on = glane < G;
   const int4* tab = reinterpret_cast<const int4*>(a.cost + a.base);
-  for (int i0 = team; i0 < n; i0 += 4 * T) {
-    int4 it[4], r[4];
+  int32_t rows = 0;
+  for (int32_t e0 = sg.z; e0 < e1; e0 += 32) {
+    const int32_t e = e0 + lane;
+    int2 x = make_int2(0, 0);
+    bool act = false;
+    if (e < e1) {
+      x = g.adj[e];
+      act = rs.dense || rs.cur_flag[x.x] != 0;
+    }
+    const unsigned bal = __ballot_sync(0xffffffffu, act);
+    const int n = __popc(bal);
+    rows += n;
+    if (act) wbuf[__popc(bal & ((1u << lane) - 1u))] = make_int4(x.x, x.y, e, 0);
+    __syncwarp();
+    for (int i0 = team; i0 < n; i0 += 4 * T) {
+      int4 it[4], r[4];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) it[q] = wbuf[min(i0 + q * T, n - 1)];
+      for (int q = 0; q < 4; ++q) it[q] = wbuf[min(i0 + q * T, n - 1)];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) r[q] = on ? tab[(int64_t)it[q].x * G + glane] : make_int4(kInf, kInf, kInf, kInf);
+      for (int q = 0; q < 4; ++q) r[q] = on ? tab[(int64_t)it[q].x * G + glane] : make_int4(kInf, kInf, kInf, kInf);
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      if (i0 + q * T >= n) continue;
-      const int32_t rv[4] = {r[q].x, r[q].y, r[q].z, r[q].w};
+      for (int q = 0; q < 4; ++q) {
+        if (i0 + q * T >= n) continue;
+        const int32_t rv[4] = {r[q].x, r[q].y, r[q].z, r[q].w};
 #pragma unroll
-      for (int t = 0; t < 4; ++t) {
-        const int32_t cc = light_or_inf(rv[t], rs.ub_light) + it[q].y;  // both < 2^30: no wrap
-        if (cc < best[t]) {
-          best[t] = cc;
-          code[t] = it[q].z;
+        for (int t = 0; t < 4; ++t) {
+          const int32_t cc = light_or_inf(rv[t], rs.ub_light) + it[q].y;  // both < 2^30: no wrap
+          if (cc < best[t]) {
+            best[t] = cc;
+            code[t] = it[q].z;
+          }
         }
       }
     }
+    __syncwarp();  // wbuf is rewritten by the next 32 entries
   }
 #pragma unroll
   for (int off = GP; off < 32; off <<= 1) {
@@ -939,10 +946,36 @@ __device__ __forceinline__ void hub_chunk_team(const GraphDev& g, const LevelArg
     }
   }
   if (lane == 0) {
-    acc[kAccEnt] += cend - hc.y;
-    acc[kAccRows] += n;
+    acc[kAccEnt] += e1 - sg.z;
+    acc[kAccRows] += rows;
   }
-  unsigned long long* hm = g.hub_min + (int64_t)hc.x * g.hub_stride;
+  const int64_t rowu = a.base + (int64_t)u * s;
+  if (sg.w == 1) {
+    // the whole row in this warp: apply it directly (team 0 holds the minima)
+    bool imp = false;
+    if (team == 0 && on) {
+      const int4 own4 = tab[(int64_t)u * G + glane];
+      const int32_t own[4] = {own4.x, own4.y, own4.z, own4.w};
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        const int j = 4 * glane + t;
+        if (j >= a.m || best[t] >= own[t]) continue;
+        if (best[t] >= rs.ovf_limit) acc[kAccOverflow] = 1;
+        if (rs.ub > 0 && best[t] > cap_at(a, u, j)) continue;
+        a.cost[rowu + j] = best[t];
+        a.par[rowu + j] = code[t];
+        imp = true;
+        ++acc[kAccImproved];
+      }
+    }
+    if (lane == 0) ++acc[kAccVert];
+    if (__ballot_sync(0xffffffffu, imp) && lane == 0) {
+      rs.next_flag[u] = 1;
+      ++acc[kAccChanged];
+    }
+    return;
+  }
+  unsigned long long* hm = g.hub_min + (int64_t)sg.y * g.hub_stride;
   bool folded = false;
   if (team == 0 && on) {
 #pragma unroll
@@ -953,16 +986,14 @@ __device__ __forceinline__ void hub_chunk_team(const GraphDev& g, const LevelArg
       folded = true;
     }
   }
-  __syncwarp();  // wbuf is reused by the warp's next chunk
-  // the folded minima must be visible before the chunk counts as done; a
-  // chunk that folded nothing has nothing to order
+  // the folded minima must be visible before the segment counts as done; a
+  // segment that folded nothing has nothing to order
   if (__any_sync(0xffffffffu, folded)) __threadfence();
   int last = 0;
-  if (lane == 0) last = atomicAdd(g.hub_cnt + hc.x, 1) == (end - beg + 31) / 32 - 1;
+  if (lane == 0) last = atomicAdd(g.hub_cnt + sg.y, 1) == sg.w - 1;
   last = __shfl_sync(0xffffffffu, last, 0);
   if (!last) return;
   __threadfence();
-  const int64_t rowu = a.base + (int64_t)u * s;
   bool imp = false;
   for (int j = lane; j < s; j += 32) {
     const unsigned long long r = atomicExch(hm + j, ~0ull);  // read and clear
@@ -977,7 +1008,7 @@ __device__ __forceinline__ void hub_chunk_team(const GraphDev& g, const LevelArg
     ++acc[kAccImproved];
   }
   if (lane == 0) {
-    atomicExch(g.hub_cnt + hc.x, 0);
+    atomicExch(g.hub_cnt + sg.y, 0);
     ++acc[kAccVert];
   }
   if (__ballot_sync(0xffffffffu, imp) && lane == 0) {
@@ -986,7 +1017,9 @@ __device__ __forceinline__ void hub_chunk_team(const GraphDev& g, const LevelArg
   }
 }
 
-// hub_relax for waves with stride <= kMaxTeamStride (hub_chunk_team).
+// hub_relax for waves with stride <= kMaxTeamStride: a warp takes segments
+// warp, warp + W, ... (W warps in the grid), its lanes test 32 of them for
+// candidacy at once and the warp relaxes the candidate ones in turn.
 template <int GP>
 __device__ __forceinline__ void hub_relax_team(const GraphDev& g, const LevelArgs& a, const RoundState& rs,
                                                uint32_t (&acc)[kAccN]) {
@@ -995,14 +1028,14 @@ __device__ __forceinline__ void hub_relax_team(const GraphDev& g, const LevelArg
   const int lane = threadIdx.x & 31;
   const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t c0 = warp; c0 < g.nchunks; c0 += 32 * nwarps) {
+  for (int64_t c0 = warp; c0 < g.nsegs; c0 += 32 * nwarps) {
     const int64_t cl = c0 + lane * nwarps;
-    const bool want = cl < g.nchunks && (rs.all_cand || rs.cand_cur[g.chunk_vtx[cl]] != 0);
+    const bool want = cl < g.nsegs && (rs.all_cand || rs.cand_cur[g.hub_seg[cl].x] != 0);
     unsigned bal = __ballot_sync(0xffffffffu, want);
     while (bal) {
       const int64_t c = c0 + (int64_t)(__ffs(bal) - 1) * nwarps;
       bal &= bal - 1u;
-      hub_chunk_team<GP>(g, a, rs, c, wbuf, acc);
+      hub_seg_team<GP>(g, a, rs, c, wbuf, acc);
     }
   }
 }
@@ -1934,10 +1967,10 @@ cudaError_t hub_round(const GraphDev& g, const LevelArgs& a, int num_sms, cudaSt
 template <int GP>
 cudaError_t hub_team_round(const GraphDev& g, const LevelArgs& a, int num_sms, cudaStream_t stream,
                            int64_t* launches) {
-  if (g.nchunks == 0) return cudaSuccess;
+  if (g.nsegs == 0) return cudaSuccess;
   static const int occ = resident_blocks(k_grow_hubs_team<GP>);
   const int64_t warps_per_block = kGrowThreads / 32;
-  int64_t blocks = (g.nchunks + warps_per_block - 1) / warps_per_block;
+  int64_t blocks = (g.nsegs + warps_per_block - 1) / warps_per_block;
   if (blocks > (int64_t)num_sms * occ) blocks = (int64_t)num_sms * occ;
   k_grow_hubs_team<GP><<<(unsigned)blocks, kGrowThreads, 0, stream>>>(g, a);
   ++*launches;

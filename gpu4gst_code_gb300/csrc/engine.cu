@@ -190,6 +190,8 @@ struct gst_graph {
   int2* d_hub_chunk = nullptr;  // (hub index, first CSR entry) per 32-entry chunk of a hub row
   int32_t* d_chunk_vtx = nullptr;  // the hub vertex of each chunk
   int64_t nchunks = 0;
+  int4* d_hub_seg = nullptr;  // (hub vertex, hub index, first entry, segments of the hub) per kHubSeg-entry segment
+  int64_t nsegs = 0;
   int32_t max_w = 0;  // largest edge weight
   // Internal vertex IDs: perm[caller ID] and its inverse (see gst_graph_upload)
   std::vector<int32_t> perm, inv;
@@ -253,6 +255,8 @@ GraphDev graph_dev(const gst_graph* g) {
   d.hub_chunk = g->d_hub_chunk;
   d.chunk_vtx = g->d_chunk_vtx;
   d.nchunks = g->nchunks;
+  d.hub_seg = g->d_hub_seg;
+  d.nsegs = g->nsegs;
   d.hub_min = g->ws.hub_min;
   d.hub_cnt = g->ws.hub_cnt;
   d.hub_stride = g->ws.hub_stride;
@@ -1337,6 +1341,8 @@ gst_status ensure_lanes(gst_graph* g, int32_t n) {
     l->d_hub_chunk = g->d_hub_chunk;
     l->d_chunk_vtx = g->d_chunk_vtx;
     l->nchunks = g->nchunks;
+    l->d_hub_seg = g->d_hub_seg;
+    l->nsegs = g->nsegs;
     l->max_w = g->max_w;
     l->perm = g->perm;
     l->inv = g->inv;
@@ -1449,6 +1455,13 @@ gst_status gst_graph_upload(const int32_t* row_ptr, const int32_t* col, const in
       chunk_vtx.push_back(big[(size_t)h]);
     }
   g->nchunks = (int64_t)chunks.size();
+  std::vector<int4> segs;
+  for (int32_t h = 0; h < g->nbig; ++h) {
+    const int32_t u = big[(size_t)h], b = row_ptr[u], e = row_ptr[u + 1];
+    const int32_t n = (e - b + kHubSeg - 1) / kHubSeg;
+    for (int32_t x = b; x < e; x += kHubSeg) segs.push_back(make_int4(u, h, x, n));
+  }
+  g->nsegs = (int64_t)segs.size();
   auto cleanup = [&](gst_status s) {
     gst_graph_free(g);
     return s;
@@ -1472,6 +1485,7 @@ gst_status gst_graph_upload(const int32_t* row_ptr, const int32_t* col, const in
       (e = up((void**)&g->d_order, order.data(), order.size() * 4)) != cudaSuccess ||
       (e = up((void**)&g->d_hub_chunk, chunks.data(), chunks.size() * sizeof(int2))) != cudaSuccess ||
       (e = up((void**)&g->d_chunk_vtx, chunk_vtx.data(), chunk_vtx.size() * sizeof(int32_t))) != cudaSuccess ||
+      (e = up((void**)&g->d_hub_seg, segs.data(), segs.size() * sizeof(int4))) != cudaSuccess ||
       (e = cudaStreamSynchronize(g->stream)) != cudaSuccess)
     return cleanup(fail(e == cudaErrorMemoryAllocation ? GST_OOM : GST_CUDA_ERROR,
                         std::string("graph upload: ") + cudaGetErrorString(e)));
@@ -1500,6 +1514,7 @@ void gst_graph_free(gst_graph* g) {
     dfree(g->d_order);
     dfree(g->d_hub_chunk);
     dfree(g->d_chunk_vtx);
+    dfree(g->d_hub_seg);
   }
   if (g->stream) cudaStreamDestroy(g->stream);
   if (g->side) cudaStreamDestroy(g->side);
