@@ -396,6 +396,44 @@ def run_serving(args, wl, world, rank, local_rank, dist):
     dg.close()
 
 
+def serving_subrecord(dg, g, flush, batches=2, B=64):
+    """Batched serving on the bench's resident 1M graph (the serve256
+    workload's graph): gst_autotune on 16 sample queries, one warm-up batch,
+    then `batches` timed gst_solve_batch calls of B queries (k uniform in
+    {3..7}; serve256 query indices 0 .. batches*B-1, the first ones with
+    oracle costs), bound-refined method. Wall clock with the device
+    synchronised on both sides."""
+    import torch
+
+    from gpu4gst_code_gb300 import native as N
+
+    wl = dict(WORKLOADS["serve256"], name="serve256")
+    sample = [make_query(wl, g, 200_000 + i) for i in range(16)]
+    t = time.perf_counter()
+    lanes = dg.autotune(sample, refine_bound=True)
+    tune_s = time.perf_counter() - t
+    ids = list(range(batches * B))
+    timed_q = [make_query(wl, g, i) for i in ids]
+    dg.solve_batch([make_query(wl, g, 100_000 + i) for i in range(B)], use_graph=True, refine_bound=True)
+    walls, lat, costs = [], [], []
+    for j in range(batches):
+        flush.fill_(j & 0xFF)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res = dg.solve_batch(timed_q[j * B:(j + 1) * B], use_graph=True, refine_bound=True)
+        torch.cuda.synchronize()
+        walls.append(time.perf_counter() - t0)
+        for r in res:
+            assert r.status == N.Status.OK, r.status
+            lat.append(r.latency_ms[0])
+            costs.append(r.cost)
+    return {"workload": "serve256: " + wl["desc"].split(":", 1)[1].strip(), "batch": B, "batches": batches,
+            "lanes": lanes, "autotune_s": tune_s, "method": METHOD_DESC["bounded"],
+            "value": batches * B / sum(walls), "unit": UNIT,
+            "latency_ms_p50": float(np.percentile(lat, 50)), "latency_ms_p99": float(np.percentile(lat, 99)),
+            "parity": parity_vs_golden("serve256", ids, timed_q, costs)}
+
+
 # ------------------------------------------------------------------ ours --
 def main():
     ap = argparse.ArgumentParser()
@@ -405,6 +443,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="ba1m_k6", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-serving", action="store_true", help="skip the batched-serving sub-record")
     ap.add_argument("--methods", default="plain,learned,bounded",
                     help="comma-separated subset of plain,learned,bounded (profiling runs); value = the last of "
                          "plain, learned, bounded present")
@@ -565,6 +604,8 @@ def main():
             "proposal_over_opt_mean": float(np.mean([r.proposal_cost / r.cost for r, _ in lr if r.cost > 0])),
             "final_bound_over_opt_mean": float(np.mean([r.upper_bound / r.cost for r, _ in lr if r.cost > 0])),
         }
+    if rank == 0 and args.workload == "ba1m_k6" and not args.no_serving:
+        line["serving"] = serving_subrecord(dg, g, flush)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         import oracle
 

@@ -152,6 +152,20 @@ __device__ __forceinline__ int32_t tour_bound(const LevelArgs& a, const int32_t*
   return max(lb1, lb2);
 }
 
+// PrunedDP++'s conditional tree merging (graph_v_of_v_idealID_PrunedDPPlusPlus.h:
+// 915-921): below the last wave, a merged state costing more than 2/3 of the
+// bound is dropped. Exact for ub >= OPT: at the optimal tree's weighted
+// centroid r every branch costs at most OPT/2, and the branches split into
+// two sides of at most 2/3 OPT each, each side built from light merges
+// (parts of at most OPT/2); the last wave joins the two sides. So no merge
+// below the last wave needs a result above 2/3 OPT, and heavier merged
+// states neither grow nor serve as lower-wave parts (light rules). The
+// leaf states (cost 0) are never dropped. floor(2 ub / 3) without overflow.
+__device__ __forceinline__ int32_t merged_keep(const LevelArgs& a, int32_t ub) {
+  if (ub <= 0 || a.level >= a.k) return INT_MAX;
+  return (ub / 3) * 2 + ((ub % 3) * 2) / 3;
+}
+
 // ------------------------------------------------------------------ merge --
 // One thread per (v, slot) of the level's rows: T(v,S) = 0 when S is inside
 // groups(v), else the best split T(v,S1) + T(v,S^S1) over S1 holding the
@@ -165,6 +179,7 @@ __global__ void __launch_bounds__(kGrowThreads) k_merge(GraphDev g, LevelArgs a)
   const int32_t ub = (a.level >= 2) ? a.params->ub : 0;
   const int32_t ub_light = a.params->ub;
   const int32_t ovf_limit = a.params->ovf_limit;
+  const int32_t keep23 = merged_keep(a, ub);
   uint8_t* flag2 = a.flags + 2 * (int64_t)a.vpad;
   long long acc[3] = {0, 0, 0};  // finite states, splits, overflow
   for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += stride) {
@@ -204,7 +219,7 @@ __global__ void __launch_bounds__(kGrowThreads) k_merge(GraphDev g, LevelArgs a)
           if (sub == 0u) break;
         }
       }
-      if (best < kInf && best > cap) {
+      if (best < kInf && (best > cap || best > keep23)) {
         best = kInf;
         code = kLeaf;
       }
@@ -267,6 +282,7 @@ __global__ void __launch_bounds__(NT) k_merge_staged(GraphDev g, LevelArgs a, Me
   const int32_t ub = (a.level >= 2) ? a.params->ub : 0;
   const int32_t ub_light = a.params->ub;
   const int32_t ovf_limit = a.params->ovf_limit;
+  const int32_t keep23 = merged_keep(a, ub);
   const bool light_parts = a.level < a.k;
   uint8_t* flag2 = a.flags + 2 * (int64_t)a.vpad;
   long long acc[3] = {0, 0, 0};  // finite states, splits, overflow
@@ -371,7 +387,7 @@ __global__ void __launch_bounds__(NT) k_merge_staged(GraphDev g, LevelArgs a, Me
               }
             }
           }
-          if (best < kInf && best > cap) {
+          if (best < kInf && (best > cap || best > keep23)) {
             best = kInf;
             code = kLeaf;
           }
@@ -410,6 +426,7 @@ __global__ void __launch_bounds__(kGrowThreads) k_merge_vertex(GraphDev g, Level
   const int32_t ub = (a.level >= 2) ? a.params->ub : 0;
   const int32_t ub_light = a.params->ub;
   const int32_t ovf_limit = a.params->ovf_limit;
+  const int32_t keep23 = merged_keep(a, ub);
   const bool light_parts = a.level < a.k;
   uint8_t* flag2 = a.flags + 2 * (int64_t)a.vpad;
   long long acc[3] = {0, 0, 0};  // finite states, splits, overflow
@@ -468,7 +485,7 @@ __global__ void __launch_bounds__(kGrowThreads) k_merge_vertex(GraphDev g, Level
               code = -__ldg(ml.lmasks_all + ml.mbase[x.x >> 24] + (x.x & 0xffffff));
             }
           }
-          if (best < kInf && best > cap) {
+          if (best < kInf && (best > cap || best > keep23)) {
             best = kInf;
             code = kLeaf;
           }

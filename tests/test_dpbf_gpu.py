@@ -332,3 +332,25 @@ def test_replica_pool_matches_single():
         assert {r.replica for r in got} == {0, 1}
         for (gp, mem), r in zip(qs, got):
             _check(g.row_ptr, g.col, g.w, gp, mem, r, r.cost)
+
+
+@pytest.mark.parametrize("use_graph", MODES)
+def test_full_state_table_with_hub_segments(use_graph):
+    """The whole table of the grown waves equals the oracle's exact fixpoint
+    on a BA graph whose hubs span one and several 256-entry segments (the
+    hub rows are relaxed whole by one warp, or folded through a scratch row
+    by several), with dense, flag-checked and sparse rounds all occurring."""
+    g = native.gen_barabasi_albert(30000, 4, 1, 100, 77)
+    deg = np.diff(g.row_ptr)
+    assert (deg > 256).sum() > 0 and (deg > 64).sum() > 100
+    gp, mem = native.gen_groups_zipf_degree(g, 4, 1.2, 5, 500, 79)
+    k = len(gp) - 1
+    want = oracle.dp_table(g.row_ptr, g.col, g.w, gp, mem)
+    want = np.where(want == ORACLE_INF, native.COST_LIMIT, want)
+    with native.Graph(g.row_ptr, g.col, g.w) as dg:
+        res = dg.solve(gp, mem, use_graph=use_graph)
+        assert res.status == Status.OK
+        got = dg.debug_table(k)
+    full = (1 << k) - 1
+    assert np.array_equal(got[:, 1:full], want[:, 1:full])
+    assert got[:, full].min() == want[:, full].min() == res.cost
