@@ -334,16 +334,16 @@ __global__ void __launch_bounds__(NT) k_merge_staged(GraphDev g, LevelArgs a, Me
           int32_t lb = ub > 0 ? label_bound(dd, S) : 0;
           const uint32_t X = full ^ S;
           if (ub > 0 && a.tour && __popc(X) >= 2) {
-            // PrunedDP++'s tour bound (graph_v_of_v_idealID_PrunedDPPlusPlus.h:268-386):
-            // a tree joining v to the groups of X is at least half a walk
-            // from v through all of them, over lower bounds of every leg.
-            // The walk's first and last groups i != j are taken as
-            // unordered pairs i < j: the path table is symmetric (a path
-            // reversed), and its i = j entries are no walks
-            // PrunedDP++'s second bound lb2 (PrunedDPPlusPlus.h:454-466):
-            // the walk passes through every group i of X, so it costs at
-            // least d(v,i) + W2[i][X] (the cheapest order from i over X)
-            // + the distance back from the nearest group of X, halved
+            // PrunedDP++'s tour bounds (graph_v_of_v_idealID_PrunedDPPlusPlus.h:
+            // 268-386, 435-494): a tree joining v to the groups of X is at
+            // least half a closed walk from v through all of them, over
+            // lower bounds of every leg.
+            //  lb1: the walk's first and last groups i != j, taken as
+            //       unordered pairs i < j (the path table is symmetric, a
+            //       path reversed; its i = j entries are no walks);
+            //  lb2: the walk passes through every group i of X, so it costs
+            //       at least d(v,i) + W2[i][X] (the cheapest order from i
+            //       over X) + the distance back from the nearest group of X
             int32_t lb1 = INT_MAX, lb2 = 0, dmin = INT_MAX;
             for (uint32_t xi = X; xi; xi &= xi - 1u) dmin = min(dmin, (int32_t)min(colu[(__ffs(xi) - 1) * NT], beyond));
             const int32_t* w2 = a.tour + ((int64_t)a.k << a.k) * a.k;
