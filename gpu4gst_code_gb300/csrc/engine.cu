@@ -97,6 +97,17 @@ struct QueryGraph {
   uint64_t gen = 0;  // workspace generation it was captured against
 };
 
+// One CUDA graph for a chunk of q queries with k groups each (gst_solve_batch
+// with gst_opts.batch_graph): the whole solve of every query as parallel
+// branches, one per solve context (the graph's own workspace and its lanes').
+struct BatchGraph {
+  int32_t k = 0, q = 0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  std::vector<uint64_t> gens;         // workspace generation of every branch's context at capture
+  std::vector<cudaEvent_t> fork, join;  // capture-time fork / join points of the branches
+};
+
 struct Workspace {
   uint64_t gen = 1;           // bumped whenever a captured buffer moves
   int32_t k_cap = 0;          // cost/par sized for this many groups
@@ -212,6 +223,8 @@ struct gst_graph {
   // batch concurrency (0 = default).
   int32_t tuned_shift[GST_MAX_K + 1] = {};
   int32_t tuned_lanes = 0;
+  int32_t tuned_batch_graph = 0;  // queries per batch graph chosen by gst_autotune (0: lanes)
+  std::vector<BatchGraph*> batch_graphs;
 };
 
 struct gst_result {
@@ -812,6 +825,47 @@ gst_status run_host_loop(gst_graph* g, int32_t k, int64_t* launches, bool* timeo
   return enqueue_epilogue(g, k, s, launches);
 }
 
+// The per-query scalars of g's workspace (pinned host copy) for a solve of
+// k groups under options o.
+void fill_params(gst_graph* g, int32_t k, const gst_opts& o) {
+  Workspace& ws = g->ws;
+  ws.h_params->ub = o.upper_bound > 0 ? o.upper_bound : 0;
+  ws.h_params->max_rounds = (int32_t)std::min<int64_t>(o.max_rounds > 0 ? o.max_rounds : (int64_t)g->V + 1, INT32_MAX);
+  ws.h_params->stats_on = o.collect_stats ? 1 : 0;
+  ws.h_params->k = k;
+  ws.h_params->ovf_limit = kInf - std::max<int32_t>(g->max_w, 1);
+  const gst_graph* tg = g->parent ? g->parent : g;
+  const int32_t tuned = tg->tuned_shift[k];
+  // default threshold: V/2 unpruned; V/4 when the solve prunes (fewer rows
+  // change per round, so sparse rounds stay cheaper for longer)
+  const bool pruned = o.refine_bound != 0 || o.upper_bound > 0;
+  ws.h_params->dense_shift = o.dense_shift > 0 && o.dense_shift < 31 ? o.dense_shift
+                             : tuned > 0                              ? tuned
+                             : pruned                                 ? kDefaultDenseShiftPruned
+                                                                      : kDefaultDenseShift;
+  ws.h_params->refine = o.refine_bound ? 1 : 0;
+}
+
+// The result of a finished captured solve, from the counters, statistics and
+// tree prefix its epilogue copied to g's pinned host buffers.
+gst_status finish_solve(gst_graph* g, int32_t k, gst_result* r) {
+  Workspace& ws = g->ws;
+  const Counters& c = *ws.h_ctr;
+  r->ub = ws.h_params->ub;  // the bound as the last wave saw it (refined on the device)
+  r->launches = 1 + k + (k - 1) + std::max(k - 2, 0) + (k <= kTourMaxK ? std::max(k - 2, 0) : 0) +
+                (int64_t)c.grow_launches + 2;
+  r->states = (int64_t)c.states;
+  std::copy(ws.h_stats, ws.h_stats + kNumStats, r->stats);
+  if (c.timeout) return fail(GST_TIMEOUT, "growth did not converge within max_rounds");
+  if (c.overflow) return fail(GST_OVERFLOW, "a tree cost reached GST_COST_LIMIT");
+  if (c.best == ~0ull) {
+    r->status = GST_INFEASIBLE;
+    r->cost = -1;
+    return GST_INFEASIBLE;
+  }
+  return collect_tree(g, r, (int32_t)(c.best >> 32), (int32_t)(c.best & 0xffffffffull));
+}
+
 // One query. Caller holds g->mu and has validated the groups.
 gst_status solve_one(gst_graph* g, const int32_t* group_ptr, const int32_t* members, int32_t k,
                      const gst_opts& o, gst_result* r) {
@@ -831,21 +885,7 @@ gst_status solve_one(gst_graph* g, const int32_t* group_ptr, const int32_t* memb
     st = build_query_graph(g, k);
     if (st != GST_OK) return st;
   }
-  ws.h_params->ub = o.upper_bound > 0 ? o.upper_bound : 0;
-  ws.h_params->max_rounds = (int32_t)std::min<int64_t>(o.max_rounds > 0 ? o.max_rounds : V + 1, INT32_MAX);
-  ws.h_params->stats_on = o.collect_stats ? 1 : 0;
-  ws.h_params->k = k;
-  ws.h_params->ovf_limit = kInf - std::max<int32_t>(g->max_w, 1);
-  const gst_graph* tg = g->parent ? g->parent : g;
-  const int32_t tuned = tg->tuned_shift[k];
-  // default threshold: V/2 unpruned; V/4 when the solve prunes (fewer rows
-  // change per round, so sparse rounds stay cheaper for longer)
-  const bool pruned = o.refine_bound != 0 || o.upper_bound > 0;
-  ws.h_params->dense_shift = o.dense_shift > 0 && o.dense_shift < 31 ? o.dense_shift
-                             : tuned > 0                              ? tuned
-                             : pruned                                 ? kDefaultDenseShiftPruned
-                                                                      : kDefaultDenseShift;
-  ws.h_params->refine = o.refine_bound ? 1 : 0;
+  fill_params(g, k, o);
 
   GST_CUDA(cudaEventRecord(ws.ev[0], s));
   GST_CUDA(cudaMemcpyAsync(ws.d_params, ws.h_params, sizeof(SolveParams), cudaMemcpyHostToDevice, s));
@@ -1357,6 +1397,210 @@ gst_status ensure_lanes(gst_graph* g, int32_t n) {
   return GST_OK;
 }
 
+
+// Captures every solve context's whole query for k groups (prologue, the
+// waves with their growth while-loops, epilogue) as parallel branches of one
+// graph: ctx[0] (the graph itself) on its stream, the others forked from it
+// and joined back. The branches share nothing but the resident graph, so
+// they run concurrently and each ends on its own; one launch and one host
+// synchronisation serve the whole chunk.
+gst_status build_batch_graph(gst_graph* g, int32_t k, const std::vector<gst_graph*>& ctx, BatchGraph* bg) {
+  const size_t q = ctx.size();
+  for (cudaEvent_t e : bg->fork) cudaEventDestroy(e);
+  for (cudaEvent_t e : bg->join) cudaEventDestroy(e);
+  bg->fork.assign(q, nullptr);
+  bg->join.assign(q, nullptr);
+  for (size_t i = 0; i < q; ++i) {
+    GST_CUDA(cudaEventCreateWithFlags(&bg->fork[i], cudaEventDisableTiming));
+    GST_CUDA(cudaEventCreateWithFlags(&bg->join[i], cudaEventDisableTiming));
+  }
+  cudaStream_t s = g->stream;
+  GST_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
+  gst_status st = GST_OK;
+  auto cuda = [&](cudaError_t e, const char* what) {
+    if (st == GST_OK && e != cudaSuccess) st = fail(GST_CUDA_ERROR, std::string(what) + ": " + cudaGetErrorString(e));
+  };
+  for (size_t i = 1; i < q; ++i) {
+    cuda(cudaEventRecord(bg->fork[i], s), "batch fork");
+    cuda(cudaStreamWaitEvent(ctx[i]->stream, bg->fork[i], 0), "batch fork wait");
+  }
+  for (size_t i = 0; i < q && st == GST_OK; ++i) {
+    gst_graph* c = ctx[i];
+    cudaStream_t cs = c->stream;
+    int64_t launches = 0;
+    st = enqueue_prologue(c, k, cs, &launches);
+    for (int32_t l = 1; st == GST_OK && l <= k; ++l) {
+      const LevelArgs a = level_args(c, k, l);
+      st = enqueue_merge(c, a, cs, &launches);
+      if (st == GST_OK && l < k) st = capture_growth_loop(c, a, cs);
+      if (st == GST_OK && l < k - 1) cuda(launch_ub_refine(graph_dev(c), a, c->num_sms, cs), "bound refinement launch");
+    }
+    if (st == GST_OK) st = enqueue_epilogue(c, k, cs, &launches);
+  }
+  for (size_t i = 1; i < q; ++i) {
+    cuda(cudaEventRecord(bg->join[i], ctx[i]->stream), "batch join");
+    cuda(cudaStreamWaitEvent(s, bg->join[i], 0), "batch join wait");
+  }
+  cudaGraph_t graph = nullptr;
+  const cudaError_t ee = cudaStreamEndCapture(s, &graph);
+  if (st != GST_OK) {
+    if (graph) cudaGraphDestroy(graph);
+    return st;
+  }
+  GST_CUDA(ee);
+  cudaGraphExec_t exec = nullptr;
+  const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+  if (ie != cudaSuccess) {
+    cudaGraphDestroy(graph);
+    return fail(GST_CUDA_ERROR, std::string("cudaGraphInstantiate (batch): ") + cudaGetErrorString(ie));
+  }
+  if (bg->exec) cudaGraphExecDestroy(bg->exec);
+  if (bg->graph) cudaGraphDestroy(bg->graph);
+  bg->graph = graph;
+  bg->exec = exec;
+  bg->k = k;
+  bg->q = (int32_t)q;
+  bg->gens.clear();
+  for (gst_graph* c : ctx) bg->gens.push_back(c->ws.gen);
+  return GST_OK;
+}
+
+// Solves q queries of k groups each (query i on context ctx[i]) with one
+// launch of the chunk's batch graph. The caller holds every context's
+// mutex and has validated the groups; nmem_cap sizes every member buffer
+// alike, so one capture serves later chunks. wall_ms: the chunk's host wall
+// time; dev_ms: its device time.
+gst_status solve_chunk(gst_graph* g, int32_t k, const std::vector<gst_graph*>& ctx,
+                       const std::vector<const int32_t*>& gps, const std::vector<const int32_t*>& mems,
+                       int64_t nmem_cap, const gst_opts& o, std::vector<gst_result*>& res, double* dev_ms) {
+  const size_t q = ctx.size();
+  for (gst_graph* c : ctx) {
+    gst_status st = ensure_workspace(c, k, nmem_cap);
+    if (st != GST_OK) return st;
+    st = ensure_tables(c, k);
+    if (st != GST_OK) return st;
+  }
+  BatchGraph* bg = nullptr;
+  for (BatchGraph* b : g->batch_graphs)
+    if (b->k == k && b->q == (int32_t)q) bg = b;
+  bool fresh = bg && bg->exec && bg->gens.size() == q;
+  for (size_t i = 0; fresh && i < q; ++i) fresh = bg->gens[i] == ctx[i]->ws.gen;
+  if (!fresh) {
+    if (!bg) {
+      bg = new (std::nothrow) BatchGraph;
+      if (!bg) return fail(GST_OOM, "host allocation failed");
+      g->batch_graphs.push_back(bg);
+    }
+    const gst_status st = build_batch_graph(g, k, ctx, bg);
+    if (st != GST_OK) return st;
+  }
+  cudaStream_t s = g->stream;
+  for (size_t i = 0; i < q; ++i) {  // the queries' scalars and groups, ahead of the launch on the same stream
+    Workspace& ws = ctx[i]->ws;
+    fill_params(ctx[i], k, o);
+    const int64_t nm = gps[i][k];
+    GST_CUDA(cudaMemcpyAsync(ws.d_params, ws.h_params, sizeof(SolveParams), cudaMemcpyHostToDevice, s));
+    GST_CUDA(cudaMemcpyAsync(ws.d_group_ptr, gps[i], (size_t)(k + 1) * 4, cudaMemcpyHostToDevice, s));
+    if (nm) GST_CUDA(cudaMemcpyAsync(ws.d_members, mems[i], (size_t)nm * 4, cudaMemcpyHostToDevice, s));
+  }
+  Workspace& ws0 = g->ws;
+  GST_CUDA(cudaEventRecord(ws0.ev[0], s));
+  GST_CUDA(cudaGraphLaunch(bg->exec, s));
+  GST_CUDA(cudaEventRecord(ws0.ev[2], s));
+  GST_CUDA(cudaStreamSynchronize(s));
+  *dev_ms = elapsed(ws0.ev[0], ws0.ev[2]);
+  gst_status first = GST_OK;
+  for (size_t i = 0; i < q; ++i) {
+    g_last_error.clear();
+    const gst_status st = finish_solve(ctx[i], k, res[i]);
+    res[i]->status = st;
+    res[i]->ms[0] = *dev_ms;  // the chunk's device time (its queries ran together)
+    if (st != GST_OK && st != GST_INFEASIBLE && first == GST_OK) first = st;
+  }
+  return first;
+}
+
+// gst_solve_batch with batch graphs: the valid queries grouped by k, each
+// group in chunks of up to q queries, every chunk one launch of its batch
+// graph (solve_chunk) over the graph's context and q - 1 lanes.
+gst_status solve_batch_graphs(gst_graph* g, int32_t nq, const int32_t* ks, const std::vector<std::vector<int32_t>>& gps,
+                              const std::vector<const int32_t*>& mems, const std::vector<gst_status>& pre,
+                              const gst_opts& o, int32_t q, gst_result** out) {
+  gst_status st = ensure_lanes(g, q - 1);
+  if (st != GST_OK) return st;
+  std::vector<gst_graph*> ctx{g};
+  for (int32_t i = 0; i + 1 < q; ++i) ctx.push_back(g->lanes[(size_t)i]);
+  std::vector<std::unique_lock<std::mutex>> locks;
+  for (gst_graph* c : ctx) locks.emplace_back(c->mu);
+  int prev = -1;
+  cudaGetDevice(&prev);
+  if (prev != g->device) cudaSetDevice(g->device);
+  cudaGetLastError();
+  const auto t0 = std::chrono::steady_clock::now();
+  gst_status first = GST_OK;
+  std::string first_msg;
+  auto note = [&](gst_status s2) {
+    if (s2 != GST_OK && s2 != GST_INFEASIBLE && first == GST_OK) {
+      first = s2;
+      first_msg = g_last_error;
+    }
+  };
+  std::vector<std::vector<int32_t>> by_k(GST_MAX_K + 1);
+  for (int32_t i = 0; i < nq; ++i) {
+    auto* r = new (std::nothrow) gst_result;
+    if (!r) {
+      note(fail(GST_OOM, "host allocation failed"));
+      continue;
+    }
+    out[i] = r;
+    if (pre[(size_t)i] != GST_OK) {
+      r->status = pre[(size_t)i];
+      note(fail(pre[(size_t)i], "k out of range in batch"));
+      continue;
+    }
+    bool empty = false;
+    g_last_error.clear();
+    const gst_status v = validate_groups(g, gps[(size_t)i].data(), mems[(size_t)i], ks[i], &empty);
+    if (v != GST_OK || empty) {
+      r->status = v != GST_OK ? v : GST_INFEASIBLE;
+      note(r->status);
+      continue;
+    }
+    by_k[(size_t)ks[i]].push_back(i);
+  }
+  for (int32_t k = 1; k <= GST_MAX_K; ++k) {
+    const auto& ids = by_k[(size_t)k];
+    int64_t nmem = 0;
+    for (int32_t i : ids) nmem = std::max<int64_t>(nmem, gps[(size_t)i][(size_t)k]);
+    for (size_t c0 = 0; c0 < ids.size(); c0 += (size_t)q) {
+      const size_t n = std::min(ids.size() - c0, (size_t)q);
+      std::vector<gst_graph*> cc(ctx.begin(), ctx.begin() + (ptrdiff_t)n);
+      std::vector<const int32_t*> cg, cm;
+      std::vector<gst_result*> cr;
+      for (size_t j = 0; j < n; ++j) {
+        const int32_t i = ids[c0 + j];
+        cg.push_back(gps[(size_t)i].data());
+        cm.push_back(mems[(size_t)i]);
+        cr.push_back(out[i]);
+      }
+      const auto ts = std::chrono::steady_clock::now();
+      double dev_ms = 0;
+      g_last_error.clear();
+      const gst_status s2 = solve_chunk(g, k, cc, cg, cm, nmem, o, cr, &dev_ms);
+      const auto te = std::chrono::steady_clock::now();
+      for (gst_result* r : cr) {
+        if (s2 != GST_OK && s2 != GST_INFEASIBLE && r->status == GST_OK && r->cost < 0) r->status = s2;
+        r->lat_ms[0] = std::chrono::duration<double, std::milli>(te - ts).count();
+        r->lat_ms[1] = std::chrono::duration<double, std::milli>(te - t0).count();
+      }
+      note(s2);
+    }
+  }
+  if (prev >= 0 && prev != g->device) cudaSetDevice(prev);
+  if (first != GST_OK) g_last_error = first_msg;
+  return first;
+}
+
 }  // namespace
 
 namespace gst {
@@ -1503,6 +1747,14 @@ void gst_graph_free(gst_graph* g) {
   cudaGetDevice(&prev);
   cudaSetDevice(g->device);
   if (g->stream) cudaStreamSynchronize(g->stream);
+  for (BatchGraph* b : g->batch_graphs) {
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    for (cudaEvent_t e : b->fork) cudaEventDestroy(e);
+    for (cudaEvent_t e : b->join) cudaEventDestroy(e);
+    delete b;
+  }
+  g->batch_graphs.clear();
   free_workspace(g->ws);
   free_learn(g->lw);
   if (g->owns_device) {
@@ -1582,6 +1834,10 @@ gst_status gst_solve_batch(gst_graph* g, int32_t nq, const int32_t* ks, const in
     for (int32_t i = 0; i <= ks[q]; ++i) gp[(size_t)i] = group_ptr[b + i] - group_ptr[b];
     mems[(size_t)q] = members ? members + group_ptr[b] : nullptr;
   }
+  const int32_t bgq = o.batch_graph >= 2 ? o.batch_graph
+                      : (o.batch_graph == 0 && o.concurrency <= 0) ? g->tuned_batch_graph
+                                                                   : 0;
+  if (bgq >= 2) return solve_batch_graphs(g, nq, ks, gps, mems, pre, o, std::min(bgq, kMaxLanes), out);
   const int32_t want = o.concurrency > 0 ? o.concurrency : (g->tuned_lanes > 0 ? g->tuned_lanes : kDefaultLanes);
   const int32_t nl = std::max(1, std::min({want, nq, kMaxLanes}));
   gst_status st = ensure_lanes(g, nl - 1);
@@ -1683,14 +1939,17 @@ gst_status gst_autotune(gst_graph* g, int32_t nq, const int32_t* ks, const int32
     }
     g->tuned_shift[k] = best_shift;
   }
-  // 2. batch concurrency: the sample as one batch per candidate, wall time
+  // 2. batch execution: the sample as one batch per candidate (concurrent
+  // contexts l = 1, 2, 4, 8, or batch graphs of l = -2, -4, -8 queries),
+  // wall time
   std::vector<gst_result*> res((size_t)nq, nullptr);
   double best_s = 1e300;
   int32_t best_l = 1;
-  for (int32_t l : {1, 2, 4, 8}) {
-    if (l > kMaxLanes) break;
+  for (int32_t l : {1, 2, 4, 8, -2, -4, -8}) {
+    if (std::abs(l) > kMaxLanes) continue;
     gst_opts ob = o;
-    ob.concurrency = l;
+    ob.concurrency = l > 0 ? l : 1;
+    ob.batch_graph = l > 0 ? 1 : -l;
     for (int rep = 0; rep < 2; ++rep) {
       const auto t0 = std::chrono::steady_clock::now();
       const gst_status sb = gst_solve_batch(g, nq, ks, group_ptr, members, &ob, res.data());
@@ -1706,8 +1965,9 @@ gst_status gst_autotune(gst_graph* g, int32_t nq, const int32_t* ks, const int32
       }
     }
   }
-  g->tuned_lanes = best_l;
-  if (lanes_out) *lanes_out = best_l;
+  g->tuned_lanes = best_l > 0 ? best_l : 0;
+  g->tuned_batch_graph = best_l < 0 ? -best_l : 0;
+  if (lanes_out) *lanes_out = best_l > 0 ? best_l : -best_l;
   return GST_OK;
 }
 

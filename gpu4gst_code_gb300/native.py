@@ -56,7 +56,8 @@ class Opts(C.Structure):
         ("dense_shift", C.c_int32),
         ("refine_bound", C.c_int32),
         ("concurrency", C.c_int32),
-        ("reserved", C.c_int32 * 8),
+        ("batch_graph", C.c_int32),
+        ("reserved", C.c_int32 * 7),
     ]
 
 
@@ -244,7 +245,7 @@ def _read_result(r) -> Result:
 
 
 def make_opts(upper_bound: int = 0, max_rounds: int = 0, use_graph: bool = False, collect_stats: bool = False,
-              dense_shift: int = 0, refine_bound: bool = False, concurrency: int = 0) -> Opts:
+              dense_shift: int = 0, refine_bound: bool = False, concurrency: int = 0, batch_graph: int = 0) -> Opts:
     o = Opts()
     o.struct_size = C.sizeof(Opts)
     o.upper_bound = int(upper_bound)
@@ -254,6 +255,7 @@ def make_opts(upper_bound: int = 0, max_rounds: int = 0, use_graph: bool = False
     o.dense_shift = int(dense_shift)
     o.refine_bound = int(bool(refine_bound))
     o.concurrency = int(concurrency)
+    o.batch_graph = int(batch_graph)
     return o
 
 
@@ -378,7 +380,8 @@ class Graph:
         return _i32(ks), _i32(gptr), _i32(mem)
 
     def autotune(self, queries, *, use_graph=True, refine_bound=False) -> int:
-        """gst_autotune on a sample of queries; returns the tuned concurrency."""
+        """gst_autotune on a sample of queries; returns the tuned concurrency
+        (or the batch graph size, when batch graphs solved the sample faster)."""
         ks_a, gp_a, mem_a = self._pack_batch(queries)
         o = make_opts(0, 0, use_graph, False, 0, refine_bound)
         lanes = C.c_int32(0)
@@ -388,7 +391,7 @@ class Graph:
         return int(lanes.value)
 
     def solve_batch(self, queries, *, upper_bound=0, use_graph=False, collect_stats=False, refine_bound=False,
-                    concurrency=0, raise_on_error=True) -> list[Result]:
+                    concurrency=0, batch_graph=0, raise_on_error=True) -> list[Result]:
         """queries: list of (group_ptr, members) or list of member-list lists.
         A query that fails alone (k out of range) has its status in its own
         result; raise_on_error=False returns the results instead of raising
@@ -396,7 +399,7 @@ class Graph:
         ks_a, gp_a, mem_a = self._pack_batch(queries)
         n = len(ks_a)
         outs = (C.c_void_p * n)()
-        o = make_opts(upper_bound, 0, use_graph, collect_stats, 0, refine_bound, concurrency)
+        o = make_opts(upper_bound, 0, use_graph, collect_stats, 0, refine_bound, concurrency, batch_graph)
         st = lib().gst_solve_batch(self._h, n, _ptr(ks_a), _ptr(gp_a), _ptr(mem_a), C.byref(o), outs)
         msg = last_error()
         res = []

@@ -84,7 +84,14 @@ typedef struct gst_opts {
    * workspace and streams over the one resident graph; 0 = the tuned value
    * (gst_autotune), else 4. Capped at 8. */
   int32_t concurrency;
-  int32_t reserved[8];
+  /* gst_solve_batch: >= 2 = solve the batch in chunks of this many queries
+   * with equal k, each chunk one launch of a CUDA graph that holds every
+   * query's whole solve as a parallel branch (captured once per k and chunk
+   * size, on the graph's own context and its lanes); 1 = the concurrent
+   * solve contexts of `concurrency` instead; 0 = the tuned choice
+   * (gst_autotune), else contexts. Capped at 8. Results never depend on it. */
+  int32_t batch_graph;
+  int32_t reserved[7];
 } gst_opts;
 
 /* ---------------------------------------------------------------- graph -- */
@@ -133,10 +140,12 @@ gst_status gst_solve_batch(gst_graph *g, int32_t nq, const int32_t *ks, const in
 
 /* Tunes the graph for a sample of queries (laid out as for
  * gst_solve_batch): for every k present, the dense-round shift (1..4) that
- * solves its sample fastest; then the batch concurrency (1, 2, 4 or 8) that
- * solves the whole sample fastest. Later solves with dense_shift 0 and
- * batches with concurrency 0 use the tuned values. Results never depend on
- * tuning. No counterpart in the reference. */
+ * solves its sample fastest; then the batch execution that solves the whole
+ * sample fastest: concurrent solve contexts (1, 2, 4 or 8) or batch graphs
+ * of 2, 4 or 8 queries. Later solves with dense_shift 0 and batches with
+ * concurrency 0 and batch_graph 0 use the tuned values; *lanes_out receives
+ * the tuned concurrency (or the batch graph size when that won). Results
+ * never depend on tuning. No counterpart in the reference. */
 gst_status gst_autotune(gst_graph *g, int32_t nq, const int32_t *ks, const int32_t *group_ptr,
                         const int32_t *members, const gst_opts *opts, int32_t *lanes_out);
 

@@ -287,12 +287,33 @@ def test_concurrent_batch_matches_single(concurrency):
                 assert r.latency_ms[0] > 0 and r.latency_ms[1] >= r.latency_ms[0] * 0.999
 
 
+@pytest.mark.parametrize("batch_graph", [2, 3, 8])
+def test_batch_graphs_match_oracle(batch_graph):
+    """gst_solve_batch with batch graphs: queries grouped by k, each chunk
+    one launch of a CUDA graph whose parallel branches are the queries'
+    whole solves. Every cost equals the oracle's, every tree is valid, on
+    two batches in a row (the second reuses the captured graphs), with and
+    without bound refinement; a query with k = 17 fails alone."""
+    g, qs = _ba_queries(20_000, 13, 43)
+    want = _oracle_costs(g, qs)
+    bad = native.gen_groups_uniform(g.V, 17, 2, 44)
+    with native.Graph(g.row_ptr, g.col, g.w) as dg:
+        for refine in (False, True, True):
+            got = dg.solve_batch(qs[:6] + [bad] + qs[6:], refine_bound=refine, batch_graph=batch_graph,
+                                 raise_on_error=False)
+            assert got[6].status == Status.BAD_INPUT
+            got = got[:6] + got[7:]
+            assert [r.cost for r in got] == want
+            for (gp, mem), r in zip(qs, got):
+                _check(g.row_ptr, g.col, g.w, gp, mem, r, r.cost)
+
+
 def test_autotune_keeps_results_exact():
     g, qs = _ba_queries(20_000, 16, 37)
     want = _oracle_costs(g, qs)
     with native.Graph(g.row_ptr, g.col, g.w) as dg:
         lanes = dg.autotune(qs[:8], refine_bound=True)
-        assert lanes in (1, 2, 4, 8)
+        assert lanes in (1, 2, 4, 8)  # concurrent contexts or batch-graph size
         got = dg.solve_batch(qs, use_graph=True, refine_bound=True)
         assert [r.cost for r in got] == want
         assert [dg.solve(gp, mem, use_graph=True).cost for gp, mem in qs] == want
