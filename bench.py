@@ -429,7 +429,9 @@ def serving_subrecord(dg, g, flush, batches=2, B=64):
             lat.append(r.latency_ms[0])
             costs.append(r.cost)
     return {"workload": "serve256: " + wl["desc"].split(":", 1)[1].strip(), "batch": B, "batches": batches,
-            "lanes": lanes, "autotune_s": tune_s, "method": METHOD_DESC["bounded"],
+            "autotuned_width": lanes,
+            "autotuned_width_note": "concurrent solve contexts, or queries per batch graph when those won",
+            "autotune_s": tune_s, "method": METHOD_DESC["bounded"],
             "value": batches * B / sum(walls), "unit": UNIT,
             "latency_ms_p50": float(np.percentile(lat, 50)), "latency_ms_p99": float(np.percentile(lat, 99)),
             "parity": parity_vs_golden("serve256", ids, timed_q, costs)}
