@@ -136,20 +136,20 @@ __device__ __forceinline__ int32_t cap_at(const LevelArgs& a, int32_t v, int j) 
 // (unsigned): each is at most ub / 2 + 1 + ub + ub / 2 + 1.
 __device__ __forceinline__ int32_t tour_bound(const LevelArgs& a, const int32_t* d1, uint32_t beyond, uint32_t X) {
   const int32_t* w2 = a.tour + ((int64_t)a.k << a.k) * a.k;
-  uint32_t dmin = 0xffffffffu;
-  for (uint32_t xi = X; xi; xi &= xi - 1u) dmin = min(dmin, min((uint32_t)__ldg(d1 + __ffs(xi) - 1), beyond));
-  int32_t lb1 = INT_MAX, lb2 = 0;
+  // halving is monotone: each bound halves its extreme sum once
+  uint32_t p1 = 0xffffffffu, p2 = 0u, dmin = 0xffffffffu;
   for (uint32_t xi = X; xi; xi &= xi - 1u) {
     const int i = __ffs(xi) - 1;
     const uint32_t di = min((uint32_t)__ldg(d1 + i), beyond);
     const int32_t* fi = a.tour + (((int64_t)i << a.k) | X) * a.k;
-    lb2 = max(lb2, (int32_t)((di + (uint32_t)__ldg(w2 + ((int64_t)i << a.k) + X) + dmin) >> 1));
+    dmin = min(dmin, di);
+    p2 = max(p2, di + (uint32_t)__ldg(w2 + ((int64_t)i << a.k) + X));
     for (uint32_t xj = xi & (xi - 1u); xj; xj &= xj - 1u) {
       const int i2 = __ffs(xj) - 1;
-      lb1 = min(lb1, (int32_t)((di + (uint32_t)__ldg(fi + i2) + min((uint32_t)__ldg(d1 + i2), beyond)) >> 1));
+      p1 = min(p1, di + (uint32_t)__ldg(fi + i2) + min((uint32_t)__ldg(d1 + i2), beyond));
     }
   }
-  return max(lb1, lb2);
+  return (int32_t)max(p1 >> 1, (p2 + dmin) >> 1);
 }
 
 // PrunedDP++'s conditional tree merging (graph_v_of_v_idealID_PrunedDPPlusPlus.h:
@@ -310,11 +310,9 @@ __global__ void __launch_bounds__(NT) k_merge_staged(GraphDev g, LevelArgs a, Me
       }
     }
     const uint32_t gm = __ldg(a.gmask + v);
-    int32_t dd[16];
-    if (ub > 0) load_label_bound(a, ub, (int32_t)v, dd);
-    // the tour bound reads wave 1's distances from the staged level-1 row
-    // (words 0..k-1): light ones are exact, the others exceed ub / 2, so
-    // min(staged, ub / 2 + 1) is dd with a runtime index
+    // the bounds read wave 1's distances from the staged level-1 row (words
+    // 0..k-1): light ones are exact, the others exceed ub / 2, so
+    // min(staged, ub / 2 + 1) is the capped one-label distance
     const uint32_t beyond = (uint32_t)(ub / 2 + 1);
     const uint32_t full = (1u << a.k) - 1u;
     int4* rowc = reinterpret_cast<int4*>(a.cost + a.base + v * a.stride);
@@ -331,8 +329,12 @@ __global__ void __launch_bounds__(NT) k_merge_staged(GraphDev g, LevelArgs a, Me
         if (j < a.m) {
           const uint32_t S = (uint32_t)__ldg(a.lmasks + j);
           if ((gm & S) == S) best = 0;
-          int32_t lb = ub > 0 ? label_bound(dd, S) : 0;
           const uint32_t X = full ^ S;
+          // one-label bound: the farthest group of X (dmax)
+          uint32_t dmax = 0u;
+          if (ub > 0 && !(a.tour && __popc(X) >= 2))
+            for (uint32_t xi = X; xi; xi &= xi - 1u) dmax = max(dmax, min(colu[(__ffs(xi) - 1) * NT], beyond));
+          int32_t lb = (int32_t)dmax;
           if (ub > 0 && a.tour && __popc(X) >= 2) {
             // PrunedDP++'s tour bounds (graph_v_of_v_idealID_PrunedDPPlusPlus.h:
             // 268-386, 435-494): a tree joining v to the groups of X is at
@@ -344,21 +346,23 @@ __global__ void __launch_bounds__(NT) k_merge_staged(GraphDev g, LevelArgs a, Me
             //  lb2: the walk passes through every group i of X, so it costs
             //       at least d(v,i) + W2[i][X] (the cheapest order from i
             //       over X) + the distance back from the nearest group of X
-            int32_t lb1 = INT_MAX, lb2 = 0, dmin = INT_MAX;
-            for (uint32_t xi = X; xi; xi &= xi - 1u) dmin = min(dmin, (int32_t)min(colu[(__ffs(xi) - 1) * NT], beyond));
+            //  (halving is monotone, so each side halves its extreme sum once;
+            //  every sum is at most ub / 2 + 1 + ub + ub / 2 + 1: unsigned, no wrap)
+            uint32_t p1 = 0xffffffffu, p2 = 0u, dmin = 0xffffffffu;
             const int32_t* w2 = a.tour + ((int64_t)a.k << a.k) * a.k;
             for (uint32_t xi = X; xi; xi &= xi - 1u) {
               const int i = __ffs(xi) - 1;
-              const int32_t di = (int32_t)min(colu[i * NT], beyond);
+              const uint32_t di = min(colu[i * NT], beyond);
               const int32_t* fi = a.tour + (((int64_t)i << a.k) | X) * a.k;
-              // each sum is at most ub / 2 + 1 + ub + ub / 2 + 1: unsigned, no wrap
-              lb2 = max(lb2, (int32_t)(((uint32_t)di + (uint32_t)__ldg(w2 + ((int64_t)i << a.k) + X) + (uint32_t)dmin) >> 1));
+              dmin = min(dmin, di);
+              dmax = max(dmax, di);
+              p2 = max(p2, di + (uint32_t)__ldg(w2 + ((int64_t)i << a.k) + X));
               for (uint32_t xj = xi & (xi - 1u); xj; xj &= xj - 1u) {
                 const int i2 = __ffs(xj) - 1;
-                lb1 = min(lb1, (int32_t)(((uint32_t)di + (uint32_t)__ldg(fi + i2) + min(colu[i2 * NT], beyond)) >> 1));
+                p1 = min(p1, di + (uint32_t)__ldg(fi + i2) + min(colu[i2 * NT], beyond));
               }
             }
-            lb = max(lb, max(lb1, lb2));
+            lb = (int32_t)max(dmax, max(p1 >> 1, (p2 + dmin) >> 1));
           }
           const int32_t cap = ub > 0 ? ub - lb : kInf;
           k4[t] = cap < 0 ? -1 : cap;
@@ -908,8 +912,7 @@ __device__ __forceinline__ void hub_seg_team(const GraphDev& g, const LevelArgs&
   const int32_t s = a.stride;
   const int4 sg = g.hub_seg[sidx];  // (hub vertex, hub index, first entry, segments of the hub)
   const int32_t u = sg.x;
-  const int32_t beg = g.row_ptr[u], end = g.row_ptr[u + 1];
-  const int32_t e1 = min(end, sg.z + kHubSeg);
+  const int32_t e1 = min(g.row_ptr[u + 1], sg.z + kHubSeg);
   int32_t best[4] = {kInf, kInf, kInf, kInf};
   int32_t code[4] = {-1, -1, -1, -1};
   const bool on = glane < G;
@@ -1464,17 +1467,19 @@ __global__ void __launch_bounds__(kGrowThreads, (MP <= 16 ? 3 : 2)) k_grow_threa
 // contiguous 16G bytes) after loading the CSR entry, which every lane of
 // the team reads at the same address. UNR neighbours are in flight at a
 // time: their CSR entries are loaded unconditionally at clamped addresses,
-// then their rows, then folded. A team holds 8 best / parent registers,
+// then their rows, then folded, then the next UNR entries are loaded. The
+// caller passes the vertex's row bounds (looked up for 32 vertices at once
+// by the warp). A team holds 8 best / parent registers,
 // not the whole row, so more warps stay resident than with a thread per
 // vertex, and a neighbour costs a team one load and three integer
 // operations per mask instead of a thread's serial chain. LIGHT: the solve
 // prunes, only light neighbour states grow (light_or_inf).
 template <int G, int UNR, bool LIGHT>
 __device__ __forceinline__ void team_vertex(const GraphDev& g, const LevelArgs& a, const RoundState& rs, int32_t u,
-                                            int glane, unsigned tmask, uint32_t (&acc)[kAccN]) {
+                                            int32_t beg, int32_t end, int glane, unsigned tmask,
+                                            uint32_t (&acc)[kAccN]) {
   constexpr int S = 4 * G;
-  const int32_t beg = g.row_ptr[u], end = g.row_ptr[u + 1];
-  if (end - beg > g.deg_big) return;  // hub: relaxed in 32-entry chunks (hub_relax)
+  if (end - beg > g.deg_big) return;  // hub: relaxed in segments (hub_relax_team)
   const int64_t rowu = a.base + (int64_t)u * S;
   const int4 own4 = reinterpret_cast<const int4*>(a.cost + rowu)[glane];
   const int32_t own[4] = {own4.x, own4.y, own4.z, own4.w};
@@ -1489,10 +1494,12 @@ __device__ __forceinline__ void team_vertex(const GraphDev& g, const LevelArgs& 
   }
   if (!(__ballot_sync(tmask, live) & tmask)) return;
   const int4* tab = reinterpret_cast<const int4*>(a.cost + a.base);
-  for (int32_t e0 = beg; e0 < end; e0 += UNR) {
-    int2 x[UNR];
+  int2 x[UNR];
+  if (beg < end) {
 #pragma unroll
-    for (int i = 0; i < UNR; ++i) x[i] = g.adj[min(e0 + i, end - 1)];
+    for (int i = 0; i < UNR; ++i) x[i] = g.adj[min(beg + i, end - 1)];
+  }
+  for (int32_t e0 = beg; e0 < end; e0 += UNR) {
     int4 r[UNR];
 #pragma unroll
     for (int i = 0; i < UNR; ++i) r[i] = tab[(int64_t)x[i].x * G + glane];
@@ -1511,6 +1518,10 @@ __device__ __forceinline__ void team_vertex(const GraphDev& g, const LevelArgs& 
           }
         }
       }
+    }
+    if (e0 + UNR < end) {
+#pragma unroll
+      for (int i = 0; i < UNR; ++i) x[i] = g.adj[min(e0 + UNR + i, end - 1)];
     }
   }
   if (glane == 0) acc[kAccRows] += end - beg;
@@ -1542,10 +1553,10 @@ __device__ __forceinline__ void team_vertex(const GraphDev& g, const LevelArgs& 
 }
 
 // The dense rounds of waves whose stride is 4G (sparse rounds return at
-// once: k_grow_thread runs them). Hubs first (32-entry chunks), then the
-// other vertices in growth order: a warp takes 32 sweep positions at a time
-// from the round's counter, its 32/G teams take them in turn. Odd rounds
-// sweep backwards, as the thread kernel does.
+// once: k_grow_thread runs them). Hubs first (segments of up to kHubSeg
+// entries), then the other vertices in growth order: a warp takes 32 sweep
+// positions at a time from the round's counter, its 32/G teams take them in
+// turn. Odd rounds sweep backwards.
 template <int G, int UNR>
 __global__ void __launch_bounds__(kGrowThreads, (G <= 4 ? 4 : 3)) k_grow_team(GraphDev g, LevelArgs a) {
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&a.ctr->grow_launches, 1);
@@ -1565,23 +1576,35 @@ __global__ void __launch_bounds__(kGrowThreads, (G <= 4 ? 4 : 3)) k_grow_team(Gr
   const unsigned tmask = team < T ? (G == 32 ? 0xffffffffu : ((1u << G) - 1u) << (team * G)) : 0u;
   uint32_t* work = &a.ctl->work[rs.r % 3];
   const bool light = rs.ub_light > 0;
+  static_assert(kDenseGrab == 32, "one sweep position per lane");
   for (;;) {
     uint32_t base = 0;
     if (lane == 0) base = atomicAdd(work, (uint32_t)kDenseGrab);
     base = __shfl_sync(0xffffffffu, base, 0);
     if ((int64_t)base >= g.nsmall) break;
-    if (team < T) {
-      for (int p = team; p < kDenseGrab; p += T) {
-        const int64_t i = (int64_t)base + p;
-        if (i >= g.nsmall) break;
-        const int32_t u = g.order[(rs.r & 1) ? g.nsmall - 1 - i : i];
-        if (light)
-          team_vertex<G, UNR, true>(g, a, rs, u, glane, tmask, acc);
-        else
-          team_vertex<G, UNR, false>(g, a, rs, u, glane, tmask, acc);
-      }
+    // lane j looks up the take's j-th vertex and its row bounds (one
+    // coalesced step for the whole warp), so a team starts each of its
+    // vertices at the CSR entries
+    const int64_t ij = (int64_t)base + lane;
+    int32_t uj = -1, bj = 0, ej = 0;
+    if (ij < g.nsmall) {
+      uj = g.order[(rs.r & 1) ? g.nsmall - 1 - ij : ij];
+      bj = g.row_ptr[uj];
+      ej = g.row_ptr[uj + 1];
     }
-    __syncwarp();
+    for (int p0 = 0; p0 < kDenseGrab; p0 += T) {  // the same trip count in every lane
+      const int src = min(p0 + team, 31);
+      const int32_t u = __shfl_sync(0xffffffffu, uj, src);
+      const int32_t beg = __shfl_sync(0xffffffffu, bj, src);
+      const int32_t end = __shfl_sync(0xffffffffu, ej, src);
+      if (team < T && p0 + team < kDenseGrab && u >= 0) {
+        if (light)
+          team_vertex<G, UNR, true>(g, a, rs, u, beg, end, glane, tmask, acc);
+        else
+          team_vertex<G, UNR, false>(g, a, rs, u, beg, end, glane, tmask, acc);
+      }
+      __syncwarp();
+    }
   }
   round_end(a, rs, acc, ba);
 }
