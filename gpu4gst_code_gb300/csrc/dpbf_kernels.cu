@@ -890,9 +890,10 @@ __device__ __forceinline__ void hub_relax(const GraphDev& g, const LevelArgs& a,
 }
 
 // Hub rows of waves with stride 4G <= kMaxTeamStride, relaxed a segment of
-// up to kHubSeg entries per warp. The warp walks the segment 32 entries at
-// a time: it compacts the active entries (dense rounds: all; sparse rounds:
-// those whose neighbour changed) into shared memory, then splits into 32/GP
+// up to kHubSeg entries per warp. The warp compacts the segment's active
+// entries into shared memory 32 at a time (dense rounds: all of them, in
+// order; sparse rounds: those whose neighbour changed, found after loading
+// every entry of the segment and its change flag at once), then splits into 32/GP
 // teams of GP lanes (GP = G rounded up to a power of two; lanes G .. GP-1
 // of a team idle); team t takes active entries t, t + T, ... four at a
 // time, lane q loading the 16-byte quarter q of each neighbour's row, so up
@@ -902,7 +903,7 @@ __device__ __forceinline__ void hub_relax(const GraphDev& g, const LevelArgs& a,
 // its row directly by team 0, its only writer; the segments of a larger
 // hub fold into the hub's scratch row and the last one to finish applies
 // it, as in hub_chunk_relax.
-template <int GP>
+template <int GP, bool DENSE>
 __device__ __forceinline__ void hub_seg_team(const GraphDev& g, const LevelArgs& a, const RoundState& rs,
                                              int64_t sidx, int4* wbuf, uint32_t (&acc)[kAccN]) {
   constexpr int T = 32 / GP;
@@ -918,19 +919,8 @@ __device__ __forceinline__ void hub_seg_team(const GraphDev& g, const LevelArgs&
   const bool on = glane < G;
   const int4* tab = reinterpret_cast<const int4*>(a.cost + a.base);
   int32_t rows = 0;
-  for (int32_t e0 = sg.z; e0 < e1; e0 += 32) {
-    const int32_t e = e0 + lane;
-    int2 x = make_int2(0, 0);
-    bool act = false;
-    if (e < e1) {
-      x = g.adj[e];
-      act = rs.dense || rs.cur_flag[x.x] != 0;
-    }
-    const unsigned bal = __ballot_sync(0xffffffffu, act);
-    const int n = __popc(bal);
-    rows += n;
-    if (act) wbuf[__popc(bal & ((1u << lane) - 1u))] = make_int4(x.x, x.y, e, 0);
-    __syncwarp();
+  // folds the n entries compacted in wbuf into the teams' minima
+  auto gather = [&](int n) {
     for (int i0 = team; i0 < n; i0 += 4 * T) {
       int4 it[4], r[4];
 #pragma unroll
@@ -951,7 +941,54 @@ __device__ __forceinline__ void hub_seg_team(const GraphDev& g, const LevelArgs&
         }
       }
     }
-    __syncwarp();  // wbuf is rewritten by the next 32 entries
+    __syncwarp();  // wbuf is rewritten next
+  };
+  if (DENSE) {
+    for (int32_t e0 = sg.z; e0 < e1; e0 += 32) {
+      const int32_t e = e0 + lane;
+      if (e < e1) {
+        const int2 x = g.adj[e];
+        wbuf[lane] = make_int4(x.x, x.y, e, 0);
+      }
+      __syncwarp();
+      const int n = min(32, e1 - e0);
+      rows += n;
+      gather(n);
+    }
+  } else {
+    // a sparse round: the segment's CSR entries and their change flags are
+    // loaded for the whole segment first (lane l holds entries l, l + 32,
+    // ...), then only the changed neighbours are compacted, up to 32 at a
+    // time, and gathered: a segment with few changed neighbours costs two
+    // loads deep instead of two per 32 entries
+    constexpr int NI = kHubSeg / 32;
+    int2 xs[NI];
+#pragma unroll
+    for (int i = 0; i < NI; ++i) {
+      const int32_t e = sg.z + 32 * i + lane;
+      xs[i] = e < e1 ? g.adj[e] : make_int2(-1, 0);
+    }
+    uint32_t am = 0;
+#pragma unroll
+    for (int i = 0; i < NI; ++i)
+      if (xs[i].x >= 0 && rs.cur_flag[xs[i].x] != 0) am |= 1u << i;
+    int n = 0;
+#pragma unroll
+    for (int i = 0; i < NI; ++i) {
+      const bool act = (am >> i) & 1u;
+      const unsigned bal = __ballot_sync(0xffffffffu, act);
+      if (!bal) continue;
+      const int c = __popc(bal);
+      if (n + c > 32) {
+        gather(n);
+        n = 0;
+      }
+      if (act) wbuf[n + __popc(bal & ((1u << lane) - 1u))] = make_int4(xs[i].x, xs[i].y, sg.z + 32 * i + lane, 0);
+      __syncwarp();
+      n += c;
+      rows += c;
+    }
+    if (n) gather(n);
   }
 #pragma unroll
   for (int off = GP; off < 32; off <<= 1) {
@@ -1055,7 +1092,10 @@ __device__ __forceinline__ void hub_relax_team(const GraphDev& g, const LevelArg
     while (bal) {
       const int64_t c = c0 + (int64_t)(__ffs(bal) - 1) * nwarps;
       bal &= bal - 1u;
-      hub_seg_team<GP>(g, a, rs, c, wbuf, acc);
+      if (rs.dense)
+        hub_seg_team<GP, true>(g, a, rs, c, wbuf, acc);
+      else
+        hub_seg_team<GP, false>(g, a, rs, c, wbuf, acc);
     }
   }
 }
