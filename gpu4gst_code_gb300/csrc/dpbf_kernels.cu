@@ -1077,7 +1077,7 @@ __device__ __forceinline__ void hub_seg_team(const GraphDev& g, const LevelArgs&
 // hub_relax for waves with stride <= kMaxTeamStride: a warp takes segments
 // warp, warp + W, ... (W warps in the grid), its lanes test 32 of them for
 // candidacy at once and the warp relaxes the candidate ones in turn.
-template <int GP>
+template <int GP, bool DENSE>
 __device__ __forceinline__ void hub_relax_team(const GraphDev& g, const LevelArgs& a, const RoundState& rs,
                                                uint32_t (&acc)[kAccN]) {
   __shared__ int4 hbuf[kGrowThreads / 32][32];
@@ -1092,10 +1092,7 @@ __device__ __forceinline__ void hub_relax_team(const GraphDev& g, const LevelArg
     while (bal) {
       const int64_t c = c0 + (int64_t)(__ffs(bal) - 1) * nwarps;
       bal &= bal - 1u;
-      if (rs.dense)
-        hub_seg_team<GP, true>(g, a, rs, c, wbuf, acc);
-      else
-        hub_seg_team<GP, false>(g, a, rs, c, wbuf, acc);
+      hub_seg_team<GP, DENSE>(g, a, rs, c, wbuf, acc);
     }
   }
 }
@@ -1220,7 +1217,7 @@ __global__ void __launch_bounds__(kGrowThreads) k_grow_hubs_team(GraphDev g, Lev
   __shared__ BlockAcc ba;
   block_acc_init(ba);
   uint32_t acc[kAccN] = {0, 0, 0, 0, 0, 0, 0};
-  hub_relax_team<GP>(g, a, rs, acc);
+  hub_relax_team<GP, false>(g, a, rs, acc);
   round_flush(a, rs, acc, ba);
 }
 
@@ -1609,7 +1606,7 @@ __global__ void __launch_bounds__(kGrowThreads, (G <= 4 ? 4 : 3)) k_grow_team(Gr
   const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
   clear_flags(a, rs, t0, nthreads);
-  hub_relax_team<(G <= 1 ? 1 : G <= 2 ? 2 : G <= 4 ? 4 : 8)>(g, a, rs, acc);
+  hub_relax_team<(G <= 1 ? 1 : G <= 2 ? 2 : G <= 4 ? 4 : 8), true>(g, a, rs, acc);
   constexpr int T = 32 / G;  // teams per warp; lanes T*G .. 31 idle
   const int lane = threadIdx.x & 31;
   const int team = lane / G, glane = lane - team * G;
