@@ -582,7 +582,8 @@ def main():
         },
         "speedup_vs_plain": {m: a["qps"] / arms["plain"]["qps"] for m, a in arms.items()
                              if m != "plain" and "plain" in arms},
-        "roofline": {"kernel": "growth kernels (k_grow_thread<MP>, k_grow_hubs), plain method, per step",
+        "roofline": {"kernel": "growth kernels (k_grow_team dense rounds, k_grow_thread + k_grow_hubs_team "
+                                 "sparse rounds; k_grow_group / k_grow_hubs for wider rows), plain method, per step",
                      "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": peak_kind, "traffic": traffic_per_step(wl),
                      "traffic_note": "DRAM bytes of the growth kernels per query: an ncu capture of the 400k case "

@@ -1971,6 +1971,30 @@ gst_status gst_autotune(gst_graph* g, int32_t nq, const int32_t* ks, const int32
   return GST_OK;
 }
 
+gst_status gst_get_tuning(const gst_graph* g, gst_tuning* out) {
+  g_last_error.clear();
+  if (!g || !out) return fail(GST_BAD_INPUT, "null graph or tuning record");
+  *out = gst_tuning{};
+  for (int k = 0; k <= GST_MAX_K; ++k) out->dense_shift[k] = g->tuned_shift[k];
+  out->concurrency = g->tuned_lanes;
+  out->batch_graph = g->tuned_batch_graph;
+  return GST_OK;
+}
+
+gst_status gst_set_tuning(gst_graph* g, const gst_tuning* t) {
+  g_last_error.clear();
+  if (!g || !t) return fail(GST_BAD_INPUT, "null graph or tuning record");
+  for (int k = 0; k <= GST_MAX_K; ++k)
+    if (t->dense_shift[k] < 0 || t->dense_shift[k] > 4) return fail(GST_BAD_INPUT, "dense_shift out of range");
+  if (t->concurrency < 0 || t->concurrency > kMaxLanes) return fail(GST_BAD_INPUT, "concurrency out of range");
+  if (t->batch_graph != 0 && (t->batch_graph < 2 || t->batch_graph > kMaxLanes))
+    return fail(GST_BAD_INPUT, "batch_graph out of range");
+  for (int k = 0; k <= GST_MAX_K; ++k) g->tuned_shift[k] = t->dense_shift[k];
+  g->tuned_lanes = t->concurrency;
+  g->tuned_batch_graph = t->batch_graph;
+  return GST_OK;
+}
+
 struct gst_pool {
   std::vector<gst_graph*> replicas;
 };

@@ -61,6 +61,15 @@ class Opts(C.Structure):
     ]
 
 
+class Tuning(C.Structure):
+    _fields_ = [
+        ("dense_shift", C.c_int32 * (MAX_K + 1)),
+        ("concurrency", C.c_int32),
+        ("batch_graph", C.c_int32),
+        ("reserved", C.c_int32 * 6),
+    ]
+
+
 # name -> (restype, argtypes); every symbol include/*.h declares
 SIGNATURES = {
     "gst_graph_upload": (C.c_int, [I32P, I32P, I32P, C.c_int32, C.c_int64, C.POINTER(C.c_void_p)]),
@@ -73,6 +82,8 @@ SIGNATURES = {
         [C.c_void_p, C.c_int32, I32P, I32P, I32P, C.POINTER(Opts), C.POINTER(C.c_void_p)],
     ),
     "gst_autotune": (C.c_int, [C.c_void_p, C.c_int32, I32P, I32P, I32P, C.POINTER(Opts), I32P]),
+    "gst_get_tuning": (C.c_int, [C.c_void_p, C.POINTER(Tuning)]),
+    "gst_set_tuning": (C.c_int, [C.c_void_p, C.POINTER(Tuning)]),
     "gst_pool_create": (C.c_int, [I32P, I32P, I32P, C.c_int32, C.c_int64, I32P, C.c_int32, C.POINTER(C.c_void_p)]),
     "gst_pool_free": (None, [C.c_void_p]),
     "gst_pool_num_replicas": (C.c_int32, [C.c_void_p]),
@@ -259,6 +270,62 @@ def make_opts(upper_bound: int = 0, max_rounds: int = 0, use_graph: bool = False
     return o
 
 
+TUNING_FORMAT = "gst-tuning-1"
+
+
+def tuning_key(V: int, nnz: int, ks, refine_bound: bool, use_graph: bool) -> str:
+    """The shape a tuning record applies to: the vertex count's power-of-two
+    bucket, the rounded average degree, the set of k in the sample, the
+    method (plain or bound-refined) and the driver (CUDA graph or host)."""
+    vb = max(0, int(V) - 1).bit_length()
+    deg = round(int(nnz) / max(int(V), 1))
+    kset = ",".join(str(k) for k in sorted({int(k) for k in ks}))
+    return f"V<=2^{vb}|deg{deg}|k{kset}|{'bounded' if refine_bound else 'plain'}|{'graph' if use_graph else 'host'}"
+
+
+def load_tuning(path, key: str):
+    """The record stored under key in a tuning cache file, or None (no file,
+    no such key, or a file of another format)."""
+    import json
+
+    p = Path(path)
+    if not p.exists():
+        return None
+    try:
+        doc = json.loads(p.read_text())
+    except (OSError, ValueError):
+        return None
+    if not isinstance(doc, dict) or doc.get("format") != TUNING_FORMAT:
+        return None
+    rec = doc.get("entries", {}).get(key)
+    if not isinstance(rec, dict):
+        return None
+    return {"dense_shift": [int(x) for x in rec.get("dense_shift", [])], "concurrency": int(rec.get("concurrency", 0)),
+            "batch_graph": int(rec.get("batch_graph", 0))}
+
+
+def store_tuning(path, key: str, rec: dict) -> None:
+    """Adds (or replaces) key's record in a tuning cache file, written
+    through a temporary file and renamed into place."""
+    import json
+    import os
+
+    p = Path(path)
+    doc = {"format": TUNING_FORMAT, "entries": {}}
+    if p.exists():
+        try:
+            old = json.loads(p.read_text())
+            if isinstance(old, dict) and old.get("format") == TUNING_FORMAT:
+                doc["entries"] = dict(old.get("entries", {}))
+        except (OSError, ValueError):
+            pass
+    doc["entries"][key] = {"dense_shift": [int(x) for x in rec["dense_shift"]], "concurrency": int(rec["concurrency"]),
+                           "batch_graph": int(rec["batch_graph"])}
+    tmp = p.with_name(f".{p.name}.{os.getpid()}.tmp")
+    tmp.write_text(json.dumps(doc, indent=1, sort_keys=True) + "\n")
+    os.replace(tmp, p)
+
+
 def groups_to_csr(groups) -> tuple[np.ndarray, np.ndarray]:
     """[[members of group 0], [members of group 1], ...] -> (group_ptr, members)."""
     ptr = [0]
@@ -379,16 +446,48 @@ class Graph:
             gptr.extend(int(base + x) for x in gp[1:])
         return _i32(ks), _i32(gptr), _i32(mem)
 
-    def autotune(self, queries, *, use_graph=True, refine_bound=False) -> int:
+    def autotune(self, queries, *, use_graph=True, refine_bound=False, cache=None) -> int:
         """gst_autotune on a sample of queries; returns the tuned concurrency
-        (or the batch graph size, when batch graphs solved the sample faster)."""
+        (or the batch graph size, when batch graphs solved the sample faster).
+        cache: a JSON file of tuning records keyed by the graph's shape and
+        the sample's k (tuning_key); a record found there is applied instead
+        of tuning, a new one is added after tuning."""
         ks_a, gp_a, mem_a = self._pack_batch(queries)
+        key = tuning_key(self.V, self.nnz, ks_a, refine_bound, use_graph) if cache is not None else None
+        if key is not None:
+            rec = load_tuning(cache, key)
+            if rec is not None:
+                self.set_tuning(rec)
+                return int(rec["batch_graph"] or rec["concurrency"])
         o = make_opts(0, 0, use_graph, False, 0, refine_bound)
         lanes = C.c_int32(0)
         st = lib().gst_autotune(self._h, len(ks_a), _ptr(ks_a), _ptr(gp_a), _ptr(mem_a), C.byref(o), C.byref(lanes))
         if st != Status.OK:
             raise GSTError(st, last_error())
+        if key is not None:
+            store_tuning(cache, key, self.tuning())
         return int(lanes.value)
+
+    def tuning(self) -> dict:
+        """The graph's tuned values (gst_get_tuning) as a plain dict."""
+        t = Tuning()
+        st = lib().gst_get_tuning(self._h, C.byref(t))
+        if st != Status.OK:
+            raise GSTError(st, last_error())
+        return {"dense_shift": [int(x) for x in t.dense_shift], "concurrency": int(t.concurrency),
+                "batch_graph": int(t.batch_graph)}
+
+    def set_tuning(self, rec: dict) -> None:
+        """Applies a record of tuning() (gst_set_tuning; out-of-range values raise)."""
+        t = Tuning()
+        shifts = list(rec.get("dense_shift", []))
+        for k in range(MAX_K + 1):
+            t.dense_shift[k] = int(shifts[k]) if k < len(shifts) else 0
+        t.concurrency = int(rec.get("concurrency", 0))
+        t.batch_graph = int(rec.get("batch_graph", 0))
+        st = lib().gst_set_tuning(self._h, C.byref(t))
+        if st != Status.OK:
+            raise GSTError(st, last_error())
 
     def solve_batch(self, queries, *, upper_bound=0, use_graph=False, collect_stats=False, refine_bound=False,
                     concurrency=0, batch_graph=0, raise_on_error=True) -> list[Result]:

@@ -149,6 +149,27 @@ gst_status gst_solve_batch(gst_graph *g, int32_t nq, const int32_t *ks, const in
 gst_status gst_autotune(gst_graph *g, int32_t nq, const int32_t *ks, const int32_t *group_ptr,
                         const int32_t *members, const gst_opts *opts, int32_t *lanes_out);
 
+/* What gst_autotune chose for a graph, as a plain record that a caller can
+ * keep (for instance in a file keyed by the graph's size and the queries'
+ * k) and hand to a later graph of the same shape instead of tuning again.
+ * dense_shift[k]: the dense-round shift of k-group solves (0 = default,
+ * else 1..4); concurrency: solve contexts of a batch (0 = default, else
+ * 1..8); batch_graph: queries per batch graph (0 = contexts, else 2..8).
+ * Results never depend on it. No counterpart in the reference. */
+typedef struct gst_tuning {
+  int32_t dense_shift[GST_MAX_K + 1];
+  int32_t concurrency;
+  int32_t batch_graph;
+  int32_t reserved[6];
+} gst_tuning;
+
+/* Copies g's tuned values into *out. */
+gst_status gst_get_tuning(const gst_graph *g, gst_tuning *out);
+
+/* Sets g's tuned values from *t; GST_BAD_INPUT (g unchanged) when a value
+ * is out of its range. */
+gst_status gst_set_tuning(gst_graph *g, const gst_tuning *t);
+
 /* ---------------------------------------------------------------- pool -- */
 
 /* Replicas of one graph on several devices (query-level scaling: a query's

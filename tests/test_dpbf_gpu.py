@@ -319,6 +319,31 @@ def test_autotune_keeps_results_exact():
         assert [dg.solve(gp, mem, use_graph=True).cost for gp, mem in qs] == want
 
 
+def test_autotune_cache_applies_the_stored_record(tmp_path):
+    """autotune(cache=...) tunes once, stores the record under the graph's
+    shape key, and a second graph of the same shape takes the record from
+    the file instead of tuning; the batch results stay exact."""
+    g, qs = _ba_queries(20_000, 8, 41)
+    want = _oracle_costs(g, qs)
+    cache = tmp_path / "tuning.json"
+    with native.Graph(g.row_ptr, g.col, g.w) as dg:
+        lanes = dg.autotune(qs[:6], refine_bound=True, cache=cache)
+        rec = dg.tuning()
+    assert cache.exists()
+    key = native.tuning_key(g.V, g.nnz, [len(gp) - 1 for gp, _ in qs[:6]], True, True)
+    assert native.load_tuning(cache, key) == rec
+    assert lanes == (rec["batch_graph"] or rec["concurrency"])
+    with native.Graph(g.row_ptr, g.col, g.w) as dg2:
+        assert dg2.tuning()["concurrency"] == 0  # a fresh graph is untuned
+        assert dg2.autotune(qs[:6], refine_bound=True, cache=cache) == lanes
+        assert dg2.tuning() == rec
+        assert [r.cost for r in dg2.solve_batch(qs, use_graph=True, refine_bound=True)] == want
+        bad = dict(rec, batch_graph=99)
+        with pytest.raises(native.GSTError):
+            dg2.set_tuning(bad)
+        assert dg2.tuning() == rec  # a rejected record changes nothing
+
+
 def test_dataset_files_solve_like_the_reference_harness(tmp_path):
     """A dataset in the reference's file formats (.in/.g/.g7), read with the
     gst_io readers and solved query by query (rucgraph/test_gpu.h:115-215)."""

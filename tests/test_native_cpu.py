@@ -146,3 +146,26 @@ def test_dropin_adapter_compiles_against_reference_headers(tmp_path):
                            str(tu), str(native.LIB_PATH), "-o", str(out), "-lpthread"],
                           capture_output=True, text=True)
     assert proc.returncode == 0, proc.stderr[-2000:]
+
+
+def test_tuning_cache_file_round_trip(tmp_path):
+    """The tuning cache: records keyed by the graph's shape, merged into one
+    file, read back exactly; a missing file, key or foreign format reads as
+    no record."""
+    key = native.tuning_key(1_000_000, 7_999_980, [6, 5, 6], True, True)
+    assert key == "V<=2^20|deg8|k5,6|bounded|graph"
+    assert native.tuning_key(1_048_576, 8_388_608, [6], False, False) == "V<=2^20|deg8|k6|plain|host"
+    assert native.tuning_key(1_048_577, 8_388_608, [6], False, False).startswith("V<=2^21|")
+    f = tmp_path / "t.json"
+    assert native.load_tuning(f, key) is None
+    a = {"dense_shift": [0] * 6 + [2] + [0] * 10, "concurrency": 4, "batch_graph": 0}
+    b = {"dense_shift": [1] * 17, "concurrency": 0, "batch_graph": 8}
+    native.store_tuning(f, key, a)
+    native.store_tuning(f, "other", b)
+    assert native.load_tuning(f, key) == a and native.load_tuning(f, "other") == b
+    native.store_tuning(f, key, b)
+    assert native.load_tuning(f, key) == b
+    assert native.load_tuning(f, "missing") is None
+    f.write_text('{"format": "something-else", "entries": {}}')
+    assert native.load_tuning(f, key) is None
+    assert sorted(p.name for p in tmp_path.iterdir()) == ["t.json"]  # no temporary file left
