@@ -160,6 +160,8 @@ struct LearnWs {
   int32_t* mnb = nullptr;
   float* x = nullptr;                 // V x kFeat
   __nv_bfloat16* hb[3] = {nullptr, nullptr, nullptr};  // V x kHid each: two activations, the neighbour mean
+  CUtensorMap hb_map[3];              // their TMA descriptors (make_act_map)
+  int32_t* infer_err = nullptr;       // set by the layer GEMM when one of its waits ran out
   float* hub_sum = nullptr;           // nbig x kHid
   float* scores = nullptr;            // V
   unsigned long long* best = nullptr;
@@ -300,6 +302,7 @@ void free_learn(LearnWs& lw) {
   dfree(lw.top);
   dfree(lw.pe);
   dfree(lw.pn);
+  dfree(lw.infer_err);
   for (auto& p : lw.h) dfree(p);
   for (auto& p : lw.a) dfree(p);
   dfree(lw.dz);
@@ -1059,9 +1062,8 @@ HostTree mst_repair(gst_graph* g, std::vector<int32_t> set, int32_t root,
   return out;
 }
 
-gst_status ensure_learn_infer(gst_graph* g) {
+gst_status alloc_learn_infer(gst_graph* g) {
   LearnWs& lw = g->lw;
-  if (lw.x) return GST_OK;
   const size_t V = (size_t)g->V;
   lw.V = g->V;
   GST_CUDA(cudaMalloc(&lw.r1, V * 4));
@@ -1072,6 +1074,7 @@ gst_status ensure_learn_infer(gst_graph* g) {
   GST_CUDA(cudaMalloc(&lw.hb[0], V * kHid * sizeof(__nv_bfloat16)));
   GST_CUDA(cudaMalloc(&lw.hb[1], V * kHid * sizeof(__nv_bfloat16)));
   GST_CUDA(cudaMalloc(&lw.hb[2], V * kHid * sizeof(__nv_bfloat16)));
+  for (int i = 0; i < 3; ++i) GST_CUDA(make_act_map(lw.hb[i], g->V, &lw.hb_map[i]));
   GST_CUDA(cudaMalloc(&lw.hub_sum, std::max<size_t>(1, (size_t)g->nbig) * kHid * sizeof(float)));
   GST_CUDA(cudaMalloc(&lw.scores, V * sizeof(float)));
   GST_CUDA(cudaMalloc(&lw.best, sizeof(unsigned long long)));
@@ -1081,7 +1084,19 @@ gst_status ensure_learn_infer(gst_graph* g) {
   lw.pe_cap = (int32_t)std::min<int64_t>((int64_t)GST_MAX_K * (g->V + 1), 1 << 22);
   GST_CUDA(cudaMalloc(&lw.pe, (size_t)lw.pe_cap * sizeof(int3)));
   GST_CUDA(cudaMalloc(&lw.pn, 4 * sizeof(int32_t)));
+  GST_CUDA(cudaMalloc(&lw.infer_err, sizeof(int32_t)));
+  GST_CUDA(cudaMemset(lw.infer_err, 0, sizeof(int32_t)));
   return GST_OK;
+}
+
+// The inference workspace, allocated on first use; infer_err is the last
+// allocation, so a workspace with it is complete (a failed allocation frees
+// what it made).
+gst_status ensure_learn_infer(gst_graph* g) {
+  if (g->lw.infer_err) return GST_OK;
+  const gst_status st = alloc_learn_infer(g);
+  if (st != GST_OK) free_learn(g->lw);
+  return st;
 }
 
 gst_status ensure_learn_train(gst_graph* g, int32_t nids) {
@@ -1150,9 +1165,16 @@ gst_status infer_scores(gst_graph* g, const gst_scorer* sc) {
       GST_CUDA(launch_hub_sum_bf16(gd, hin, lw.hub_sum, s));
     }
     const bool last = l == kMpLayers;
-    GST_CUDA(launch_infer_layer(gd, g->d_hub_of, lw.hub_sum, hin, lw.hb[2],
+    GST_CUDA(launch_infer_layer(gd, g->d_hub_of, lw.hub_sum, hin, lw.hb_map[(l - 1) & 1], lw.hb[2], lw.hb_map[2],
                                 sc->wcat + (size_t)(l - 1) * kHid * 2 * kHid, sc->params, l,
-                                last ? nullptr : lw.hb[l & 1], last ? lw.scores : nullptr, s));
+                                last ? nullptr : lw.hb[l & 1], last ? lw.scores : nullptr, lw.infer_err, s));
+  }
+  int32_t err = 0;
+  GST_CUDA(cudaMemcpyAsync(&err, lw.infer_err, sizeof(err), cudaMemcpyDeviceToHost, s));
+  GST_CUDA(cudaStreamSynchronize(s));
+  if (err) {
+    GST_CUDA(cudaMemsetAsync(lw.infer_err, 0, sizeof(int32_t), s));
+    return fail(GST_INTERNAL, err == 1 ? "scorer layer: a TMA load did not complete" : "scorer layer: an MMA did not complete");
   }
   return GST_OK;
 }

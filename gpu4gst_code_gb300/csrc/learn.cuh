@@ -9,11 +9,12 @@
 //   h_l = relu(Ws_l h_{l-1} + Wn_l mean_{u in N(v)} h_{l-1}(u) + b_l)
 //   score(v) = wo . h3(v) + bo
 // Inference stores activations and weights in bf16 and accumulates in
-// fp32 (tensor-core mma over 16-vertex tiles); training runs every kernel
+// fp32 (tcgen05 GEMMs over 128-vertex tiles); training runs every kernel
 // in fp32. Parameters are one flat fp32 vector laid out as below.
 #pragma once
 #include <cstdint>
 
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -53,12 +54,18 @@ cudaError_t launch_infer_l0(int32_t V, const float* x, const float* params, __nv
 // Hub rows' neighbour sums for one layer, fp32, one 32-entry chunk per warp
 // (hub_sum[nbig][kHid], zeroed by the caller).
 cudaError_t launch_hub_sum_bf16(const GraphDev& g, const __nv_bfloat16* hin, float* hub_sum, cudaStream_t s);
+// TMA descriptor of a bf16 activation buffer (V rows of kHid values, 128
+// bytes each): 128-row boxes, 128-byte swizzle, rows past V read as zero.
+cudaError_t make_act_map(const __nv_bfloat16* buf, int32_t V, CUtensorMap* out);
 // One message-passing layer (l = 1..3): the neighbour mean into agg
-// (V x kHid bf16 scratch), then the tensor-core layer over [h | agg]. On the
-// last layer, with scores non-null, writes scores instead of activations.
+// (V x kHid bf16 scratch), then the tcgen05 layer GEMM over [h | agg]
+// (hin_map, agg_map: make_act_map of hin and agg). On the last layer, with
+// scores non-null, writes scores instead of activations. *err (device) is
+// set non-zero if a tensor-core or TMA wait of the layer ran out.
 cudaError_t launch_infer_layer(const GraphDev& g, const int32_t* hub_of, const float* hub_sum,
-                               const __nv_bfloat16* hin, __nv_bfloat16* agg, const __nv_bfloat16* wcat_l,
-                               const float* params, int l, __nv_bfloat16* hout, float* scores, cudaStream_t s);
+                               const __nv_bfloat16* hin, const CUtensorMap& hin_map, __nv_bfloat16* agg,
+                               const CUtensorMap& agg_map, const __nv_bfloat16* wcat_l, const float* params, int l,
+                               __nv_bfloat16* hout, float* scores, int32_t* err, cudaStream_t s);
 // The proposal's root without a network: most groups within 1 hop, then 2,
 // then 3, then degree (s = 1000 x3 + 100 x4 + 10 x5 + x1).
 cudaError_t launch_feature_score(int32_t V, const float* x, float* s, cudaStream_t st);

@@ -1,6 +1,6 @@
 // Kernels of the learned upper-bound proposal (declared in learn.cuh):
-// query features, bf16 inference with tensor-core mma over 16-vertex
-// tiles, fp32 forward/backward training kernels and the Adam update.
+// query features, bf16 inference with tcgen05 tensor-core GEMMs over
+// 128-vertex tiles (TMA-staged operands, tensor-memory accumulators), fp32 forward/backward training kernels and the Adam update.
 //
 // Query features x[v][0..15] (internal vertex IDs, k groups):
 //   0  1                          6  all k groups within 1 hop
@@ -10,6 +10,7 @@
 //   4  groups within 2 hops / k   10 v belongs to some group
 //   5  groups within 3 hops / k   11..15 zero
 // ("within h hops" includes v itself.)
+#include <algorithm>
 #include <cstdint>
 
 #include "learn.cuh"
@@ -211,114 +212,228 @@ __global__ void k_hub_sum_bf16(GraphDev g, const __nv_bfloat16* __restrict__ hin
 
 
 
-// D += A * B for one m16n8k16 tile (bf16 in, fp32 accumulate)
-__device__ __forceinline__ void mma_bf16(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
-                                         uint32_t b0, uint32_t b1) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-      "{%0,%1,%2,%3};\n"
-      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-      : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+// ------------------------------------------------- tcgen05 layer GEMM --
+// One message-passing layer as a tensor-core GEMM per 128-vertex tile:
+// D[128 x 64] = A[128 x 128] * B^T, A = [h(v) | mean_{u in N(v)} h(u)]
+// (bf16, both halves streamed by TMA with 128-byte swizzle), B = the
+// layer's [Ws | Wn] (64 x 128 bf16, K-major, staged once per CTA), D in
+// tensor memory (fp32, 128 lanes x 64 columns). One thread issues the TMA
+// loads and the eight K=16 MMAs of a tile; after the MMA's commit arrives,
+// each warp reads its 32 rows of D (tcgen05.ld 32x32b), adds the bias,
+// applies the ReLU and stores bf16 activations, or on the last layer
+// reduces them against wo into scores. Every wait is bounded: a wait that
+// runs out sets *err (1: TMA, 2: MMA) and the CTA leaves after freeing its
+// tensor memory.
+constexpr int kTcThreads = 128;
+constexpr int kTcRows = 128;                    // vertices per tile (MMA M)
+constexpr uint32_t kTcTileBytes = 2u * kTcRows * 128u;  // A: two 128-byte K halves of 128 rows
+constexpr int kTcSmem = 32768 + 16384 + 64 + 512 + 1024;  // A, B, barriers, bias/wo, alignment slack
+constexpr uint32_t kTcWaitLimit = 1u << 20;     // polls of 64+ ns: > 60 ms, against microseconds per tile
+constexpr uint32_t kTmemCols = 64;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
 }
 
-constexpr int kInfWarps = 4;
-constexpr int kRowPad = 2 * kHid + 8;  // bf16 per shared row: 68 words, so fragment reads hit 32 banks
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
 
-// One message-passing layer over 16-vertex tiles per warp. The warp stages
-// A = [h(v) | mean_{u in N(v)} h(u)] (16 x 128, bf16) in shared memory,
-// multiplies it by [Ws | Wn]^T (128 x 64) with 8 x 8 mma tiles, adds the
-// bias, applies the ReLU and stores bf16 activations, or on the last
-// layer reduces them against wo into scores.
-__global__ void __launch_bounds__(kInfWarps * 32) k_infer_layer(GraphDev g, const __nv_bfloat16* __restrict__ agg,
-                                                                const __nv_bfloat16* __restrict__ hin,
-                                                                const __nv_bfloat16* __restrict__ wcat,
-                                                                const float* __restrict__ bias,
-                                                                const float* __restrict__ wo,
-                                                                const float* __restrict__ bo_ptr,
-                                                                __nv_bfloat16* __restrict__ hout,
-                                                                float* __restrict__ scores) {
-  __shared__ __align__(16) __nv_bfloat16 sB[kHid][kRowPad];
-  __shared__ __align__(16) __nv_bfloat16 sA[kInfWarps][16][kRowPad];
-  __shared__ float sbias[kHid], swo[kHid];
-  for (int i = threadIdx.x; i < kHid * 2 * kHid / 2; i += blockDim.x) {
-    const int o = i / kHid, c2 = i % kHid;  // pairs of columns
-    reinterpret_cast<uint32_t*>(&sB[o][0])[c2] = reinterpret_cast<const uint32_t*>(wcat)[i];
+// Waits for the phase with the given parity to complete; false after
+// `limit` polls.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit) {
+  const uint32_t a = smem_u32(bar);
+  for (uint32_t i = 0; i < limit; ++i) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+    __nanosleep(64);
   }
-  if (threadIdx.x < kHid) {
-    sbias[threadIdx.x] = bias[threadIdx.x];
-    swo[threadIdx.x] = wo ? wo[threadIdx.x] : 0.0f;
+  return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int32_t x, int32_t y, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+      ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// Shared-memory matrix descriptor of a K-major operand with 128-byte
+// swizzle: rows of 128 bytes, 8-row groups 1024 bytes apart (the stride
+// byte offset), start address in 16-byte units, bits 46-48 = 0b001, the
+// swizzle mode (2 = 128 bytes) in bits 61-63. The leading byte offset is
+// unused for this layout (set to 1). Atoms start 1024-byte aligned, so the
+// base offset is 0; a K step of 16 elements inside the 128-byte row moves
+// the start address by 32 bytes.
+__device__ __forceinline__ uint64_t sw128_kmajor_desc(uint32_t saddr) {
+  return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+         ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+
+// Instruction descriptor of kind::f16: D fp32 (bits 4-5 = 1), A and B bf16
+// (bits 7-9, 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 in bits
+// 17-22, M >> 4 in bits 24-28.
+constexpr uint32_t kTcIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(64 >> 3) << 17) |
+                              ((uint32_t)(kTcRows >> 4) << 24);
+
+__device__ __forceinline__ void tc_mma(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+      ::"r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(kTcIdesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void tc_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// 16 consecutive fp32 columns of this thread's tensor-memory lane
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, "
+      "[%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+
+__device__ __forceinline__ void tc_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+__global__ void __launch_bounds__(kTcThreads) k_infer_layer_tc(const __grid_constant__ CUtensorMap map_h,
+                                                               const __grid_constant__ CUtensorMap map_a, int32_t V,
+                                                               const __nv_bfloat16* __restrict__ wcat,
+                                                               const float* __restrict__ bias,
+                                                               const float* __restrict__ wo,
+                                                               const float* __restrict__ bo_ptr,
+                                                               __nv_bfloat16* __restrict__ hout,
+                                                               float* __restrict__ scores, int32_t* __restrict__ err) {
+  extern __shared__ uint8_t tc_dsm[];
+  const uint32_t raw = smem_u32(tc_dsm);
+  uint8_t* sm = tc_dsm + (((raw + 1023u) & ~1023u) - raw);  // swizzle atoms are 1024-byte aligned
+  uint8_t* sA = sm;                                          // [K half][128 rows][128 B]
+  uint8_t* sB = sm + 32768;                                  // [K half][64 rows][128 B]
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + 49152);   // [0] A loaded, [1] MMAs done
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + 49168);
+  int32_t* sabort = reinterpret_cast<int32_t*>(sm + 49172);
+  float* sbias = reinterpret_cast<float*>(sm + 49216);
+  float* swo = sbias + kHid;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  // B: row o = output o, 16-byte chunk c of its 128 K values, stored in the
+  // 128-byte-swizzled K-major layout (chunk c & 7 of K half c >> 3 at
+  // position (c & 7) ^ (o & 7) of row o)
+  for (int i = tid; i < kHid * 16; i += kTcThreads) {
+    const int o = i >> 4, c = i & 15;
+    const uint4 v = reinterpret_cast<const uint4*>(wcat + (int64_t)o * 2 * kHid)[c];
+    *reinterpret_cast<uint4*>(sB + (c >> 3) * 8192 + o * 128 + (((c & 7) ^ (o & 7)) << 4)) = v;
   }
+  if (tid < kHid) {
+    sbias[tid] = bias[tid];
+    swo[tid] = wo ? wo[tid] : 0.0f;
+  }
+  if (tid == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    *sabort = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
+                 "r"(kTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // B's stores, seen by the tensor cores
+  tc_fence_before();
   __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tslot;
   const float bo = bo_ptr ? *bo_ptr : 0.0f;
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int gq = lane >> 2, tq = lane & 3;
-  const int64_t ntiles = ((int64_t)g.V + 15) / 16;
-  for (int64_t tile = (int64_t)blockIdx.x * kInfWarps + w; tile < ntiles; tile += (int64_t)gridDim.x * kInfWarps) {
-    // stage A = [h | mean]: both rows streamed (the mean comes from
-    // k_mean_bf16), a quarter warp per vertex, 16 bytes per lane
-    const int sub = lane >> 3, sl = lane & 7;
+  const uint32_t sa = smem_u32(sA), sb = smem_u32(sB);
+  const int64_t ntiles = ((int64_t)V + kTcRows - 1) / kTcRows;
+  uint32_t phase = 0;
+  bool a_in_flight = false;
+  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    if (tid == 0) {
+      mbar_expect_tx(&bar[0], kTcTileBytes);
+      tma_load_2d(sA, &map_h, 0, (int32_t)(t * kTcRows), &bar[0]);
+      tma_load_2d(sA + 16384, &map_a, 0, (int32_t)(t * kTcRows), &bar[0]);
+      if (mbar_wait(&bar[0], phase, kTcWaitLimit)) {
+        tc_fence_after();
 #pragma unroll
-    for (int i0 = 0; i0 < 16; i0 += 4) {
-      const int i = i0 + sub;
-      const int64_t v = tile * 16 + i;
-      uint4 hv = make_uint4(0, 0, 0, 0), av = make_uint4(0, 0, 0, 0);
-      if (v < g.V) {
-        hv = reinterpret_cast<const uint4*>(hin + v * kHid)[sl];
-        av = reinterpret_cast<const uint4*>(agg + v * kHid)[sl];
-      }
-      reinterpret_cast<uint4*>(&sA[w][i][0])[sl] = hv;
-      reinterpret_cast<uint4*>(&sA[w][i][kHid])[sl] = av;
-    }
-    __syncwarp();
-    float acc[kHid / 8][4];
-#pragma unroll
-    for (int nt = 0; nt < kHid / 8; ++nt) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.0f;
-#pragma unroll
-    for (int kt = 0; kt < 2 * kHid / 16; ++kt) {
-      const int c = kt * 16 + 2 * tq;
-      const uint32_t a0 = *reinterpret_cast<const uint32_t*>(&sA[w][gq][c]);
-      const uint32_t a1 = *reinterpret_cast<const uint32_t*>(&sA[w][gq + 8][c]);
-      const uint32_t a2 = *reinterpret_cast<const uint32_t*>(&sA[w][gq][c + 8]);
-      const uint32_t a3 = *reinterpret_cast<const uint32_t*>(&sA[w][gq + 8][c + 8]);
-#pragma unroll
-      for (int nt = 0; nt < kHid / 8; ++nt) {
-        const uint32_t b0 = *reinterpret_cast<const uint32_t*>(&sB[nt * 8 + gq][c]);
-        const uint32_t b1 = *reinterpret_cast<const uint32_t*>(&sB[nt * 8 + gq][c + 8]);
-        mma_bf16(acc[nt], a0, a1, a2, a3, b0, b1);
+        for (int kk = 0; kk < 2 * kHid / 16; ++kk) {
+          const uint32_t off = (uint32_t)(kk >> 2) * 16384u + (uint32_t)(kk & 3) * 32u;
+          const uint32_t boff = (uint32_t)(kk >> 2) * 8192u + (uint32_t)(kk & 3) * 32u;
+          tc_mma(tmem, sw128_kmajor_desc(sa + off), sw128_kmajor_desc(sb + boff), kk > 0 ? 1u : 0u);
+        }
+        tc_commit(&bar[1]);
+      } else {
+        a_in_flight = true;
+        *sabort = 1;
+        atomicExch(err, 1);
       }
     }
-    const int64_t v0 = tile * 16 + gq, v1 = v0 + 8;
-    if (scores) {
-      float s0 = 0.0f, s1 = 0.0f;
+    __syncthreads();
+    if (*sabort) break;
+    const bool done = mbar_wait(&bar[1], phase, kTcWaitLimit);
+    if (!done) {
+      *sabort = 1;
+      atomicExch(err, 2);
+    }
+    __syncthreads();
+    if (*sabort) break;
+    tc_fence_after();
+    uint32_t r[4][16];
+    const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
 #pragma unroll
-      for (int nt = 0; nt < kHid / 8; ++nt) {
-        const int col = nt * 8 + 2 * tq;
-        s0 += fmaxf(acc[nt][0] + sbias[col], 0.0f) * swo[col] + fmaxf(acc[nt][1] + sbias[col + 1], 0.0f) * swo[col + 1];
-        s1 += fmaxf(acc[nt][2] + sbias[col], 0.0f) * swo[col] + fmaxf(acc[nt][3] + sbias[col + 1], 0.0f) * swo[col + 1];
-      }
-      s0 += __shfl_xor_sync(0xffffffffu, s0, 1);
-      s0 += __shfl_xor_sync(0xffffffffu, s0, 2);
-      s1 += __shfl_xor_sync(0xffffffffu, s1, 1);
-      s1 += __shfl_xor_sync(0xffffffffu, s1, 2);
-      if (tq == 0) {
-        if (v0 < g.V) scores[v0] = s0 + bo;
-        if (v1 < g.V) scores[v1] = s1 + bo;
-      }
-    } else {
-      uint32_t* o2 = reinterpret_cast<uint32_t*>(hout);
+    for (int q = 0; q < 4; ++q) tc_ld16(taddr + 16 * q, r[q]);
+    tc_wait_ld();
+    const int64_t v = t * kTcRows + warp * 32 + lane;  // this thread's row of D
+    if (v < V) {
+      if (scores) {
+        float sc = bo;
 #pragma unroll
-      for (int nt = 0; nt < kHid / 8; ++nt) {
-        const int col = nt * 8 + 2 * tq;
-        if (v0 < g.V)
-          o2[(v0 * kHid + col) / 2] =
-              pack_bf16x2(fmaxf(acc[nt][0] + sbias[col], 0.0f), fmaxf(acc[nt][1] + sbias[col + 1], 0.0f));
-        if (v1 < g.V)
-          o2[(v1 * kHid + col) / 2] =
-              pack_bf16x2(fmaxf(acc[nt][2] + sbias[col], 0.0f), fmaxf(acc[nt][3] + sbias[col + 1], 0.0f));
+        for (int q = 0; q < 4; ++q)
+#pragma unroll
+          for (int j = 0; j < 16; ++j) sc += fmaxf(__uint_as_float(r[q][j]) + sbias[16 * q + j], 0.0f) * swo[16 * q + j];
+        scores[v] = sc;
+      } else {
+        uint4* out = reinterpret_cast<uint4*>(hout + v * kHid);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          uint32_t pk[8];
+#pragma unroll
+          for (int j = 0; j < 8; ++j)
+            pk[j] = pack_bf16x2(fmaxf(__uint_as_float(r[q][2 * j]) + sbias[16 * q + 2 * j], 0.0f),
+                                fmaxf(__uint_as_float(r[q][2 * j + 1]) + sbias[16 * q + 2 * j + 1], 0.0f));
+          out[2 * q] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+          out[2 * q + 1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+        }
       }
     }
-    __syncwarp();
+    tc_fence_before();
+    __syncthreads();  // D read and A consumed before the next tile's loads and MMAs
+    phase ^= 1u;
   }
+  if (tid == 0 && a_in_flight) mbar_wait(&bar[0], phase, kTcWaitLimit);  // a late A copy lands before the CTA leaves
+  // after a timed-out MMA wait the MMAs may still run: give them the same bound
+  if (*sabort && tid == 0) mbar_wait(&bar[1], phase, kTcWaitLimit);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
 }
 
 __global__ void k_feature_score(int32_t V, const float* __restrict__ x, float* __restrict__ s) {
@@ -669,16 +784,52 @@ cudaError_t launch_hub_sum_bf16(const GraphDev& g, const __nv_bfloat16* hin, flo
   return cudaGetLastError();
 }
 
+cudaError_t make_act_map(const __nv_bfloat16* buf, int32_t V, CUtensorMap* out) {
+  using EncodeFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+  static EncodeFn encode = [] {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      fn = nullptr;
+    return reinterpret_cast<EncodeFn>(fn);
+  }();
+  if (!encode) return cudaErrorNotSupported;
+  const cuuint64_t dims[2] = {(cuuint64_t)kHid, (cuuint64_t)(V > 0 ? V : 1)};
+  const cuuint64_t strides[1] = {(cuuint64_t)kHid * sizeof(__nv_bfloat16)};  // 128-byte rows
+  const cuuint32_t box[2] = {(cuuint32_t)kHid, (cuuint32_t)kTcRows};       // 128 bytes x 128 rows
+  const cuuint32_t estr[2] = {1, 1};
+  const CUresult r = encode(out, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<__nv_bfloat16*>(buf), dims, strides,
+                            box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
 cudaError_t launch_infer_layer(const GraphDev& g, const int32_t* hub_of, const float* hub_sum,
-                               const __nv_bfloat16* hin, __nv_bfloat16* agg, const __nv_bfloat16* wcat_l,
-                               const float* params, int l, __nv_bfloat16* hout, float* scores, cudaStream_t s) {
+                               const __nv_bfloat16* hin, const CUtensorMap& hin_map, __nv_bfloat16* agg,
+                               const CUtensorMap& agg_map, const __nv_bfloat16* wcat_l, const float* params, int l,
+                               __nv_bfloat16* hout, float* scores, int32_t* err, cudaStream_t s) {
   const float* bias = params + layer_off(l) + 2 * kHid * kHid;
   const float* wo = scores ? params + kOffWo : nullptr;
   const float* bo = scores ? params + kOffBo : nullptr;
   k_mean_bf16<<<grid_for((int64_t)g.V * 8, 256, 152 * 32), 256, 0, s>>>(g, hub_of, hub_sum, hin, agg);
-  const int64_t tiles = ((int64_t)g.V + 15) / 16;
-  k_infer_layer<<<grid_for(tiles, kInfWarps, 152 * 12), kInfWarps * 32, 0, s>>>(g, agg, hin, wcat_l, bias, wo, bo,
-                                                                                hout, scores);
+  static const int ctas = [] {
+    int dev = 0, sms = 152, occ = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaFuncSetAttribute(k_infer_layer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_infer_layer_tc, kTcThreads, kTcSmem) != cudaSuccess ||
+        occ < 1)
+      occ = 1;
+    return sms * occ;
+  }();
+  const cudaError_t ae = cudaFuncSetAttribute(k_infer_layer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
+  if (ae != cudaSuccess) return ae;
+  const int64_t tiles = ((int64_t)g.V + kTcRows - 1) / kTcRows;
+  const int grid = (int)std::min<int64_t>(tiles, ctas);
+  k_infer_layer_tc<<<grid, kTcThreads, kTcSmem, s>>>(hin_map, agg_map, g.V, wcat_l, bias, wo, bo, hout, scores, err);
   return cudaGetLastError();
 }
 

@@ -58,6 +58,22 @@ def test_bf16_inference_tracks_oracle(case):
     assert np.corrcoef(got, want)[0, 1] > 0.999
 
 
+@pytest.mark.parametrize("V", [60, 128, 1000])
+def test_bf16_inference_on_partial_and_whole_tiles(V):
+    """The layer GEMM works on 128-vertex tiles: one partial tile (V=60), one
+    whole tile (128) and a partial last tile (1000 = 7 x 128 + 104) score
+    like the oracle."""
+    from gpu4gst_code_gb300 import learn, native as N
+
+    g, gp, mem = ba_case(V=V, k=3, seed=V)
+    p = learn.init_params(V)
+    want, _, _ = SO.forward(p.astype(np.float64), SO.adjacency(g.row_ptr, g.col), SO.features(g.row_ptr, g.col, gp, mem))
+    with N.Graph(g.row_ptr, g.col, g.w) as dg, N.Scorer(p) as sc:
+        got = sc.scores(dg, gp, mem)
+    assert np.abs(got - want).max() <= 0.03 * (np.abs(want).max() + 1e-6)
+    assert np.corrcoef(got, want)[0, 1] > 0.999
+
+
 def test_gradients_match_oracle(case):
     from gpu4gst_code_gb300 import native as N
 
