@@ -227,7 +227,11 @@ __global__ void k_hub_sum_bf16(GraphDev g, const __nv_bfloat16* __restrict__ hin
 constexpr int kTcThreads = 128;
 constexpr int kTcRows = 128;                    // vertices per tile (MMA M)
 constexpr uint32_t kTcTileBytes = 2u * kTcRows * 128u;  // A: two 128-byte K halves of 128 rows
-constexpr int kTcSmem = 32768 + 16384 + 64 + 512 + 1024;  // A, B, barriers, bias/wo, alignment slack
+constexpr int kTcStages = 2;                    // A tiles in flight per CTA
+constexpr int kTcSmem = kTcStages * 32768 + 16384 + 64 + 512 + 1024;  // A stages, B, barriers, bias/wo, alignment
+constexpr int kTcCtasPerSm = 2;
+static_assert(kTcCtasPerSm * (kTcSmem + 1024) <= 228 * 1024, "two CTAs' shared memory (and reserve) per SM");
+static_assert(kTcCtasPerSm * 64 <= 512, "tensor memory columns per SM");
 constexpr uint32_t kTcWaitLimit = 1u << 20;     // polls of 64+ ns: > 60 ms, against microseconds per tile
 constexpr uint32_t kTmemCols = 64;
 
@@ -322,12 +326,14 @@ __global__ void __launch_bounds__(kTcThreads) k_infer_layer_tc(const __grid_cons
   extern __shared__ uint8_t tc_dsm[];
   const uint32_t raw = smem_u32(tc_dsm);
   uint8_t* sm = tc_dsm + (((raw + 1023u) & ~1023u) - raw);  // swizzle atoms are 1024-byte aligned
-  uint8_t* sA = sm;                                          // [K half][128 rows][128 B]
-  uint8_t* sB = sm + 32768;                                  // [K half][64 rows][128 B]
-  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + 49152);   // [0] A loaded, [1] MMAs done
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + 49168);
-  int32_t* sabort = reinterpret_cast<int32_t*>(sm + 49172);
-  float* sbias = reinterpret_cast<float*>(sm + 49216);
+  uint8_t* sA = sm;                                          // [stage][K half][128 rows][128 B]
+  uint8_t* sB = sm + kTcStages * 32768;                      // [K half][64 rows][128 B]
+  uint8_t* misc = sB + 16384;
+  uint64_t* full = reinterpret_cast<uint64_t*>(misc);        // [stage]: the stage's A tile landed
+  uint64_t* mma_done = full + kTcStages;                     // the tile's MMAs completed
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(mma_done + 1);
+  int32_t* sabort = reinterpret_cast<int32_t*>(tslot + 1);
+  float* sbias = reinterpret_cast<float*>(misc + 64);
   float* swo = sbias + kHid;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   // B: row o = output o, 16-byte chunk c of its 128 K values, stored in the
@@ -343,8 +349,8 @@ __global__ void __launch_bounds__(kTcThreads) k_infer_layer_tc(const __grid_cons
     swo[tid] = wo ? wo[tid] : 0.0f;
   }
   if (tid == 0) {
-    mbar_init(&bar[0], 1);
-    mbar_init(&bar[1], 1);
+    for (int st = 0; st < kTcStages; ++st) mbar_init(&full[st], 1);
+    mbar_init(mma_done, 1);
     *sabort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -362,32 +368,50 @@ __global__ void __launch_bounds__(kTcThreads) k_infer_layer_tc(const __grid_cons
   const float bo = bo_ptr ? *bo_ptr : 0.0f;
   const uint32_t sa = smem_u32(sA), sb = smem_u32(sB);
   const int64_t ntiles = ((int64_t)V + kTcRows - 1) / kTcRows;
-  uint32_t phase = 0;
-  bool a_in_flight = false;
-  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+  // stage s of A holds the CTA's tiles i = s, s + 2, ...: tile i + 1 loads
+  // while tile i is multiplied and written out (its stage was freed when
+  // tile i - 1's MMAs completed)
+  auto load_tile = [&](int64_t t, int st) {
+    mbar_expect_tx(&full[st], kTcTileBytes);
+    tma_load_2d(sA + st * 32768, &map_h, 0, (int32_t)(t * kTcRows), &full[st]);
+    tma_load_2d(sA + st * 32768 + 16384, &map_a, 0, (int32_t)(t * kTcRows), &full[st]);
+  };
+  static_assert(kTcStages == 2, "stage bits below");
+  uint32_t pending = 0u;  // thread 0: bit st = a load of stage st issued and not yet seen complete
+  uint32_t parity = 0u;   // bit st = phase parity of stage st's next completion
+  if (tid == 0 && blockIdx.x < ntiles) {
+    load_tile(blockIdx.x, 0);
+    pending |= 1u;
+  }
+  int64_t i = 0;
+  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, ++i) {
+    const int st = (int)(i & 1);
     if (tid == 0) {
-      mbar_expect_tx(&bar[0], kTcTileBytes);
-      tma_load_2d(sA, &map_h, 0, (int32_t)(t * kTcRows), &bar[0]);
-      tma_load_2d(sA + 16384, &map_a, 0, (int32_t)(t * kTcRows), &bar[0]);
-      if (mbar_wait(&bar[0], phase, kTcWaitLimit)) {
+      const int64_t tn = t + gridDim.x;
+      if (tn < ntiles) {
+        load_tile(tn, st ^ 1);
+        pending |= 1u << (st ^ 1);
+      }
+      if (mbar_wait(&full[st], (parity >> st) & 1u, kTcWaitLimit)) {
+        pending &= ~(1u << st);
+        parity ^= 1u << st;
         tc_fence_after();
+        const uint32_t a0 = sa + (uint32_t)st * 32768u;
 #pragma unroll
         for (int kk = 0; kk < 2 * kHid / 16; ++kk) {
           const uint32_t off = (uint32_t)(kk >> 2) * 16384u + (uint32_t)(kk & 3) * 32u;
           const uint32_t boff = (uint32_t)(kk >> 2) * 8192u + (uint32_t)(kk & 3) * 32u;
-          tc_mma(tmem, sw128_kmajor_desc(sa + off), sw128_kmajor_desc(sb + boff), kk > 0 ? 1u : 0u);
+          tc_mma(tmem, sw128_kmajor_desc(a0 + off), sw128_kmajor_desc(sb + boff), kk > 0 ? 1u : 0u);
         }
-        tc_commit(&bar[1]);
+        tc_commit(mma_done);
       } else {
-        a_in_flight = true;
         *sabort = 1;
         atomicExch(err, 1);
       }
     }
     __syncthreads();
     if (*sabort) break;
-    const bool done = mbar_wait(&bar[1], phase, kTcWaitLimit);
-    if (!done) {
+    if (!mbar_wait(mma_done, (uint32_t)(i & 1), kTcWaitLimit)) {
       *sabort = 1;
       atomicExch(err, 2);
     }
@@ -423,12 +447,15 @@ __global__ void __launch_bounds__(kTcThreads) k_infer_layer_tc(const __grid_cons
       }
     }
     tc_fence_before();
-    __syncthreads();  // D read and A consumed before the next tile's loads and MMAs
-    phase ^= 1u;
+    __syncthreads();  // D read before the next tile's MMAs overwrite it
   }
-  if (tid == 0 && a_in_flight) mbar_wait(&bar[0], phase, kTcWaitLimit);  // a late A copy lands before the CTA leaves
-  // after a timed-out MMA wait the MMAs may still run: give them the same bound
-  if (*sabort && tid == 0) mbar_wait(&bar[1], phase, kTcWaitLimit);
+  if (tid == 0) {
+    // after a wait ran out: loads still in flight land (bounded) before the
+    // CTA leaves, and so do MMAs that were issued
+    for (int st = 0; st < kTcStages; ++st)
+      if ((pending >> st) & 1u) mbar_wait(&full[st], (parity >> st) & 1u, kTcWaitLimit);
+    if (*sabort) mbar_wait(mma_done, (uint32_t)(i & 1), kTcWaitLimit);
+  }
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
@@ -815,15 +842,15 @@ cudaError_t launch_infer_layer(const GraphDev& g, const int32_t* hub_of, const f
   const float* wo = scores ? params + kOffWo : nullptr;
   const float* bo = scores ? params + kOffBo : nullptr;
   k_mean_bf16<<<grid_for((int64_t)g.V * 8, 256, 152 * 32), 256, 0, s>>>(g, hub_of, hub_sum, hin, agg);
+  // kTcCtasPerSm CTAs per SM (shared memory allows two; their tensor memory,
+  // 2 x 64 columns, is a quarter of an SM's), each with two tiles in flight
   static const int ctas = [] {
-    int dev = 0, sms = 152, occ = 1;
+    int dev = 0, sms = 152;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaFuncSetAttribute(k_infer_layer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_infer_layer_tc, kTcThreads, kTcSmem) != cudaSuccess ||
-        occ < 1)
-      occ = 1;
-    return sms * occ;
+    cudaFuncSetAttribute(k_infer_layer_tc, cudaFuncAttributePreferredSharedMemoryCarveout,
+                         (int)cudaSharedmemCarveoutMaxShared);
+    return sms * kTcCtasPerSm;
   }();
   const cudaError_t ae = cudaFuncSetAttribute(k_infer_layer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
   if (ae != cudaSuccess) return ae;
