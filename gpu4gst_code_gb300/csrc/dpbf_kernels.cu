@@ -548,7 +548,6 @@ namespace {
 
 constexpr int kGatherUnroll = 4;
 constexpr int kDenseGrab = 32;  // sweep positions a warp takes at a time in dense rounds (one per lane)
-constexpr int kWarpMarkMax = 16;  // changed rows of a warp up to which its lanes share each row's marking
 
 struct RoundState {
   int32_t r;
@@ -571,21 +570,30 @@ enum { kAccChanged, kAccImproved, kAccVert, kAccEnt, kAccRows, kAccMarks, kAccOv
 
 __device__ __forceinline__ bool round_begin(const GraphDev& g, const LevelArgs& a, RoundState& rs) {
   const GrowCtl* ctl = a.ctl;
+  // the round and every rotating slot load together (one step), then the
+  // previous round's slots are selected
   rs.r = ctl->round;
-  const int32_t prev = ctl->changed[(rs.r + 2) % 3];
+  const int32_t c0 = ctl->changed[0], c1 = ctl->changed[1], c2 = ctl->changed[2];
+  const int32_t d0 = ctl->dense[0], d1 = ctl->dense[1], d2 = ctl->dense[2];
+  const int32_t timeout = ctl->timeout;
+  const int32_t dense_shift = a.params->dense_shift, stats_on = a.params->stats_on, ub = a.params->ub,
+                ovf_limit = a.params->ovf_limit;
+  const int pi = (rs.r + 2) % 3;
+  const int32_t prev = pi == 0 ? c0 : pi == 1 ? c1 : c2;
+  const int32_t prev_dense = pi == 0 ? d0 : pi == 1 ? d1 : d2;
   rs.prev = prev;
   // converged (nothing changed in the previous round), or out of rounds: a
   // later kernel of the same pass must not run another round
-  if (prev == 0 || ctl->timeout) {  // nothing changed in the previous round (converged), or out of rounds
+  if ((prev == 0) | (timeout != 0)) {
     if (a.use_cond && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(a.cond, 0);
     return false;
   }
-  rs.dense = prev > (g.V >> a.params->dense_shift);
-  rs.all_cand = rs.dense || ctl->dense[(rs.r + 2) % 3] != 0;
-  rs.stats = a.params->stats_on != 0;
-  rs.ub = a.level >= 2 ? a.params->ub : 0;  // wave 1 is the bound's own input: not pruned by it
-  rs.ub_light = a.params->ub;
-  rs.ovf_limit = a.params->ovf_limit;
+  rs.dense = prev > (g.V >> dense_shift);
+  rs.all_cand = rs.dense || prev_dense != 0;
+  rs.stats = stats_on != 0;
+  rs.ub = a.level >= 2 ? ub : 0;  // wave 1 is the bound's own input: not pruned by it
+  rs.ub_light = ub;
+  rs.ovf_limit = ovf_limit;
   const int64_t P = a.vpad;  // flag arrays are padded to keep word atomics aligned
   rs.cur_flag = a.flags + (int64_t)((rs.r + 2) % 3) * P;
   rs.next_flag = a.flags + (int64_t)(rs.r % 3) * P;
@@ -630,11 +638,11 @@ __device__ __forceinline__ bool improves_row(const LevelArgs& a, int32_t ub, int
     for (int jj = 0; jj < n; ++jj) bits |= (vals(j0 + jj) + w < y(j0 + jj) ? 1u : 0u) << jj;
     if (!bits) continue;
     if (ub <= 0) return true;
-    while (bits) {
-      const int j = j0 + __ffs(bits) - 1;
-      bits &= bits - 1u;
-      if (vals(j) + w <= cap_at(a, v, j)) return true;
-    }
+    bool ok = false;  // the caps of the improved masks, loaded together
+#pragma unroll 8
+    for (int jj = 0; jj < n; ++jj)
+      if ((bits >> jj) & 1u) ok |= vals(j0 + jj) + w <= cap_at(a, v, j0 + jj);
+    if (ok) return true;
   }
   return false;
 }
@@ -1226,10 +1234,13 @@ __global__ void __launch_bounds__(kGrowThreads) k_grow_hubs_team(GraphDev g, Lev
 // warp_mark).
 template <int MP>
 __device__ __forceinline__ bool thread_vertex(const GraphDev& g, const LevelArgs& a, const RoundState& rs,
-                                              int32_t u, uint32_t (&acc)[kAccN]) {
+                                              int32_t u, int32_t& beg_out, int32_t& deg_out,
+                                              uint32_t (&acc)[kAccN]) {
   constexpr int U = MP <= 8 ? 4 : 2;
   constexpr int Q = MP / 4;
   const int32_t beg = g.row_ptr[u], end = g.row_ptr[u + 1];
+  beg_out = beg;
+  deg_out = end - beg;
   if (end - beg > g.deg_big) return false;  // hub: handled in 32-entry chunks
   int4* rowc = reinterpret_cast<int4*>(a.cost + a.base + (int64_t)u * MP);
   int32_t best[MP];
@@ -1354,59 +1365,78 @@ __device__ __forceinline__ bool thread_vertex(const GraphDev& g, const LevelArgs
 }
 
 // Marks, for every vertex of the warp whose row changed this round (chg),
-// the neighbours that the new row improves (within their bound): the
-// warp's lanes take one neighbour each, so a changed vertex costs one
-// step rather than a serial walk by its own lane. A neighbour is marked
-// only if the new row improves it for some mask: its row can only
-// decrease later, so an unmarked neighbour never needs this row. Every
-// lane of the warp must call it; dense rounds mark nothing (the next
-// round sweeps every vertex).
+// the neighbours that the new row improves (within their bound). The CSR
+// entries of the warp's changed rows are taken as one list, 32 at a time,
+// a lane per entry (the entry's row found by a binary search over the
+// lanes' entry offsets), so a step costs a few loads whatever the number
+// of changed rows: the entry, the neighbour's and the changed row's masks
+// (16 bytes at a time), and with a bound the neighbour's caps, all at
+// once. A neighbour is marked only if the new row improves it for some
+// mask: its row can only decrease later, so an unmarked neighbour never
+// needs this row. Every lane of the warp must call it; dense rounds mark
+// nothing (the next round sweeps every vertex).
 template <int MP>
 __device__ __forceinline__ void warp_mark(const GraphDev& g, const LevelArgs& a, const RoundState& rs, int32_t u,
-                                          bool chg, uint32_t (&acc)[kAccN]) {
+                                          int32_t beg, int32_t deg, bool chg, uint32_t (&acc)[kAccN]) {
   constexpr int Q = MP / 4;
   if (rs.dense) return;
-  unsigned pend = __ballot_sync(0xffffffffu, chg);
-  if (!pend) return;
+  if (!__ballot_sync(0xffffffffu, chg)) return;
   __syncwarp();  // the changed rows' stores are visible to the whole warp
   const int lane = threadIdx.x & 31;
-  // with many changed rows in the warp, each lane walks its own row's
-  // neighbours (those walks run side by side); with few, the warp's lanes
-  // share each changed row's neighbours
-  const bool own = __popc(pend) > kWarpMarkMax;
-  if (own) pend = chg ? 1u : 0u;
-  while (pend) {
-    const int src = __ffs(pend) - 1;
-    pend &= pend - 1u;
-    const int32_t w = own ? u : __shfl_sync(0xffffffffu, u, src);
-    const int32_t beg = g.row_ptr[w], end = g.row_ptr[w + 1];
-    // w's new row is read 16 bytes at a time (in the shared walk at the
-    // same address in every lane: broadcast loads, cached), light-filtered
+  const int32_t d = chg ? deg : 0;
+  int32_t incl = d;  // inclusive prefix of the changed rows' lengths over the lanes
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  const int32_t pre = incl - d;
+  const int32_t total = __shfl_sync(0xffffffffu, incl, 31);
+  for (int32_t p0 = 0; p0 < total; p0 += 32) {
+    const int32_t p = p0 + lane;
+    int src = 0;  // the last lane whose entries start at or before p
+#pragma unroll
+    for (int st = 16; st >= 1; st >>= 1) {
+      const int c = src + st;
+      const int32_t pc = __shfl_sync(0xffffffffu, pre, c & 31);
+      if (c <= 31 && pc <= p) src = c;
+    }
+    const int32_t w = __shfl_sync(0xffffffffu, u, src);
+    const int32_t wb = __shfl_sync(0xffffffffu, beg, src);
+    const int32_t wp = __shfl_sync(0xffffffffu, pre, src);
+    if (p >= total) continue;
+    const int2 x = g.adj[wb + (p - wp)];
+    // w's new row (light-filtered) against x's row
     const int4* wr = reinterpret_cast<const int4*>(a.cost + a.base + (int64_t)w * MP);
-    for (int32_t e = own ? beg : beg + lane; e < end; e += own ? 1 : 32) {
-      const int2 x = g.adj[e];
-      const int4* rv = reinterpret_cast<const int4*>(a.cost + a.base + (int64_t)x.x * MP);
-      uint32_t bits = 0;  // masks the new row improves at x
+    const int4* rv = reinterpret_cast<const int4*>(a.cost + a.base + (int64_t)x.x * MP);
+    int32_t val[MP];
+    uint32_t bits = 0;  // masks the new row improves at x
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+      const int4 t = rv[q], h = wr[q];
+      val[4 * q] = light_or_inf(h.x, rs.ub_light) + x.y;
+      val[4 * q + 1] = light_or_inf(h.y, rs.ub_light) + x.y;
+      val[4 * q + 2] = light_or_inf(h.z, rs.ub_light) + x.y;
+      val[4 * q + 3] = light_or_inf(h.w, rs.ub_light) + x.y;
+      bits |= (val[4 * q] < t.x ? 1u : 0u) << (4 * q);
+      bits |= (val[4 * q + 1] < t.y ? 1u : 0u) << (4 * q + 1);
+      bits |= (val[4 * q + 2] < t.z ? 1u : 0u) << (4 * q + 2);
+      bits |= (val[4 * q + 3] < t.w ? 1u : 0u) << (4 * q + 3);
+    }
+    bool better = bits != 0;
+    if (better && rs.ub > 0) {  // the same test under x's caps, all masks at once
+      const int4* cv = reinterpret_cast<const int4*>(a.capt + (int64_t)x.x * MP);
+      better = false;
 #pragma unroll
       for (int q = 0; q < Q; ++q) {
-        const int4 t = rv[q], h = wr[q];
-        bits |= (light_or_inf(h.x, rs.ub_light) + x.y < t.x ? 1u : 0u) << (4 * q);
-        bits |= (light_or_inf(h.y, rs.ub_light) + x.y < t.y ? 1u : 0u) << (4 * q + 1);
-        bits |= (light_or_inf(h.z, rs.ub_light) + x.y < t.z ? 1u : 0u) << (4 * q + 2);
-        bits |= (light_or_inf(h.w, rs.ub_light) + x.y < t.w ? 1u : 0u) << (4 * q + 3);
+        const int4 c = __ldg(cv + q);
+        better |= ((bits >> (4 * q)) & 1u) && val[4 * q] <= c.x;
+        better |= ((bits >> (4 * q + 1)) & 1u) && val[4 * q + 1] <= c.y;
+        better |= ((bits >> (4 * q + 2)) & 1u) && val[4 * q + 2] <= c.z;
+        better |= ((bits >> (4 * q + 3)) & 1u) && val[4 * q + 3] <= c.w;
       }
-      bool better = bits != 0;
-      if (better && rs.ub > 0) {  // the same test under x's caps
-        better = false;
-        const int32_t* wj = a.cost + a.base + (int64_t)w * MP;
-        while (bits && !better) {
-          const int j = __ffs(bits) - 1;
-          bits &= bits - 1u;
-          better = light_or_inf(wj[j], rs.ub_light) + x.y <= cap_at(a, x.x, j);
-        }
-      }
-      if (better) mark_candidate(rs.cand_next, x.x, acc);
     }
+    if (better) mark_candidate(rs.cand_next, x.x, acc);
   }
 }
 
@@ -1439,8 +1469,9 @@ __device__ __forceinline__ void thread_round_body(const GraphDev& g, const Level
       if ((int64_t)base >= g.nsmall) break;
       const int64_t i = (int64_t)base + lane;
       const int32_t u = i < g.nsmall ? g.order[(rs.r & 1) ? g.nsmall - 1 - i : i] : -1;
-      const bool chg = u >= 0 && thread_vertex<MP>(g, a, rs, u, acc);
-      warp_mark<MP>(g, a, rs, u, chg, acc);
+      int32_t beg = 0, deg = 0;
+      const bool chg = u >= 0 && thread_vertex<MP>(g, a, rs, u, beg, deg, acc);
+      warp_mark<MP>(g, a, rs, u, beg, deg, chg, acc);
     }
   } else {
     // candidates only: a warp reads kCandTile candidate bytes at a time (8
@@ -1476,8 +1507,9 @@ __device__ __forceinline__ void thread_round_body(const GraphDev& g, const Level
       __syncwarp();
       for (int i0 = 0; i0 < total; i0 += 32) {
         const int32_t u = i0 + lane < total ? tile[wib][i0 + lane] : -1;
-        const bool chg = u >= 0 && thread_vertex<MP>(g, a, rs, u, acc);
-        warp_mark<MP>(g, a, rs, u, chg, acc);
+        int32_t beg = 0, deg = 0;
+        const bool chg = u >= 0 && thread_vertex<MP>(g, a, rs, u, beg, deg, acc);
+        warp_mark<MP>(g, a, rs, u, beg, deg, chg, acc);
       }
       __syncwarp();
     }
