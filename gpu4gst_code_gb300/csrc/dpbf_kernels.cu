@@ -1516,6 +1516,10 @@ __device__ __forceinline__ void thread_round_body(const GraphDev& g, const Level
   }
 }
 
+template <int G>
+__device__ __forceinline__ void sparse_team_body(const GraphDev& g, const LevelArgs& a, const RoundState& rs,
+                                                 uint32_t (&acc)[kAccN]);
+
 template <int MP>
 __global__ void __launch_bounds__(kGrowThreads, (MP <= 16 ? 3 : 2)) k_grow_thread(GraphDev g, LevelArgs a) {
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&a.ctr->grow_launches, 1);
@@ -1525,7 +1529,16 @@ __global__ void __launch_bounds__(kGrowThreads, (MP <= 16 ? 3 : 2)) k_grow_threa
   __shared__ BlockAcc ba;
   block_acc_init(ba);
   uint32_t acc[kAccN] = {0, 0, 0, 0, 0, 0, 0};
-  thread_round_body<MP>(g, a, rs, acc);
+  // a small frontier (at most V/32 rows changed) of a wide wave: teams, whose
+  // lanes read a candidate's change flags together; otherwise a thread per
+  // candidate, which holds more candidates in flight per warp
+  bool teams = false;
+  if constexpr (MP >= 16) teams = !rs.all_cand && rs.prev <= (g.V >> 5);
+  if (teams) {
+    if constexpr (MP >= 16) sparse_team_body<MP / 4>(g, a, rs, acc);
+  } else {
+    thread_round_body<MP>(g, a, rs, acc);
+  }
   round_end(a, rs, acc, ba);
 }
 
@@ -1618,6 +1631,179 @@ __device__ __forceinline__ void team_vertex(const GraphDev& g, const LevelArgs& 
   if ((__ballot_sync(tmask, imp) & tmask) && glane == 0) {
     rs.next_flag[u] = 1;
     ++acc[kAccChanged];
+  }
+}
+
+// Sparse rounds by vertex teams (row stride 4G): a team of G lanes takes a
+// candidate, lane q holding masks 4q .. 4q+3. The team reads the change
+// flags of the candidate's CSR entries first (lane q takes entries q,
+// q+G, ..., all at once), then gathers only the changed neighbours' rows,
+// UNR at a time, each lane its 16-byte quarter. True (in every lane of the
+// team) when the candidate's row changed.
+template <int G, int UNR, bool LIGHT>
+__device__ __forceinline__ bool team_sparse_vertex(const GraphDev& g, const LevelArgs& a, const RoundState& rs,
+                                                   int32_t u, int glane, int team, unsigned tmask, int32_t& beg_out,
+                                                   int32_t& deg_out, uint32_t (&acc)[kAccN]) {
+  constexpr int S = 4 * G;
+  constexpr int NE = (kDegBigMax + G - 1) / G;  // entries per lane, enough for any non-hub row
+  const int32_t beg = g.row_ptr[u], end = g.row_ptr[u + 1];
+  beg_out = beg;
+  deg_out = end - beg;
+  if (end - beg > g.deg_big) return false;  // hub: relaxed in segments
+  const int32_t deg = end - beg;
+  const int64_t rowu = a.base + (int64_t)u * S;
+  const int4 own4 = reinterpret_cast<const int4*>(a.cost + rowu)[glane];
+  const int32_t own[4] = {own4.x, own4.y, own4.z, own4.w};
+  int32_t best[4] = {own4.x, own4.y, own4.z, own4.w};
+  int32_t code[4] = {-1, -1, -1, -1};
+  bool live = false;
+#pragma unroll
+  for (int t = 0; t < 4; ++t) live |= 4 * glane + t < a.m && own[t] != 0;  // cost-0 states cannot improve
+  if (glane == 0) {
+    ++acc[kAccVert];
+    acc[kAccEnt] += deg;
+  }
+  if (!(__ballot_sync(tmask, live) & tmask)) return false;
+  // change flags: lane q takes entries q, q + G, ...
+  int32_t nb[NE];
+#pragma unroll
+  for (int i = 0; i < NE; ++i) {
+    const int e = glane + i * G;
+    nb[i] = e < deg ? g.adj[beg + e].x : -1;
+  }
+  uint64_t chm = 0;  // bit e: entry e's neighbour changed in the previous round
+#pragma unroll
+  for (int i = 0; i < NE; ++i) {
+    const bool c = nb[i] >= 0 && rs.cur_flag[nb[i]] != 0;
+    const unsigned b = (__ballot_sync(tmask, c) >> (team * G)) & ((1u << G) - 1u);
+    chm |= (uint64_t)b << (i * G);
+    if (i * G + G >= deg) break;  // team-uniform: deg is the same in every lane of the team
+  }
+  const int4* tab = reinterpret_cast<const int4*>(a.cost + a.base);
+  int rows = 0;
+  while (chm) {
+    int rel[UNR];
+    bool ok[UNR];
+#pragma unroll
+    for (int i = 0; i < UNR; ++i) {
+      ok[i] = chm != 0ull;
+      rel[i] = ok[i] ? __ffsll((long long)chm) - 1 : 0;
+      if (ok[i]) chm &= chm - 1ull;
+    }
+    int2 x[UNR];
+#pragma unroll
+    for (int i = 0; i < UNR; ++i) x[i] = g.adj[beg + rel[i]];
+    int4 r[UNR];
+#pragma unroll
+    for (int i = 0; i < UNR; ++i) r[i] = ok[i] ? tab[(int64_t)x[i].x * G + glane] : make_int4(kInf, kInf, kInf, kInf);
+#pragma unroll
+    for (int i = 0; i < UNR; ++i) {
+      if (!ok[i]) continue;
+      ++rows;
+      const int32_t rv[4] = {r[i].x, r[i].y, r[i].z, r[i].w};
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        const int32_t c = (LIGHT ? light_or_inf(rv[t], rs.ub_light) : rv[t]) + x[i].y;
+        if (c < best[t]) {
+          best[t] = c;
+          code[t] = beg + rel[i];
+        }
+      }
+    }
+  }
+  if (glane == 0) acc[kAccRows] += rows;
+  bool imp = false;
+#pragma unroll
+  for (int t = 0; t < 4; ++t) {
+    if (code[t] < 0) continue;
+    if (best[t] >= rs.ovf_limit) acc[kAccOverflow] = 1;
+    if (rs.ub > 0 && best[t] > cap_at(a, u, 4 * glane + t)) {  // over the state's cap: keep the stored value
+      best[t] = own[t];
+      code[t] = -1;
+      continue;
+    }
+    imp = true;
+  }
+  if (imp) {
+    reinterpret_cast<int4*>(a.cost + rowu)[glane] = make_int4(best[0], best[1], best[2], best[3]);
+#pragma unroll
+    for (int t = 0; t < 4; ++t)
+      if (code[t] >= 0) {
+        a.par[rowu + 4 * glane + t] = code[t];
+        ++acc[kAccImproved];
+      }
+  }
+  const bool chg = (__ballot_sync(tmask, imp) & tmask) != 0;
+  if (chg && glane == 0) {
+    rs.next_flag[u] = 1;
+    ++acc[kAccChanged];
+  }
+  return chg;
+}
+
+// A sparse round over candidates (not the round after a dense one) of a
+// wave with row stride 4G, by vertex teams: flags cleared, the changed
+// hubs' neighbours marked, then the candidates relaxed a team each, T =
+// 32 / G per warp step, and the neighbours of the changed ones marked.
+template <int G>
+__device__ __forceinline__ void sparse_team_body(const GraphDev& g, const LevelArgs& a, const RoundState& rs,
+                                                 uint32_t (&acc)[kAccN]) {
+  constexpr int MP = 4 * G;
+  constexpr int UNR = 4;
+  const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
+  clear_flags(a, rs, t0, nthreads);
+  hub_mark(g, a, rs, acc);
+  constexpr int T = 32 / G;
+  const int lane = threadIdx.x & 31;
+  const int team = lane / G, glane = lane - team * G;
+  const unsigned tmask = team < T ? (G == 32 ? 0xffffffffu : ((1u << G) - 1u) << (team * G)) : 0u;
+  uint32_t* work = &a.ctl->work[rs.r % 3];
+  const bool light = rs.ub_light > 0;
+  // relaxes up to T candidates (list entries i0 + team) and marks the
+  // neighbours of the changed ones; every lane of the warp calls it
+  auto step = [&](const int32_t* list, int i0, int n) {
+    const int idx = i0 + team;
+    const int32_t u = (team < T && idx < n) ? list[idx] : -1;
+    int32_t beg = 0, deg = 0;
+    bool chg = false;
+    if (u >= 0)
+      chg = light ? team_sparse_vertex<G, UNR, true>(g, a, rs, u, glane, team, tmask, beg, deg, acc)
+                  : team_sparse_vertex<G, UNR, false>(g, a, rs, u, glane, team, tmask, beg, deg, acc);
+    __syncwarp();
+    warp_mark<MP>(g, a, rs, u, beg, deg, chg && glane == 0, acc);
+  };
+  // candidate tiles as in thread_round_body
+  __shared__ int32_t tile[kGrowThreads / 32][kCandTile];
+  const int wib = threadIdx.x >> 5;
+  static_assert(kCandTile == 8 * 32, "a lane reads 8 flag bytes");
+  for (;;) {
+    uint32_t ti = 0;
+    if (lane == 0) ti = atomicAdd(work, 1u);
+    ti = __shfl_sync(0xffffffffu, ti, 0);
+    const int64_t base = (int64_t)ti * kCandTile;
+    if (base >= g.V) break;
+    const int64_t v0 = base + 8 * lane;
+    uint2 f = make_uint2(0u, 0u);
+    if (v0 < g.V) f = *reinterpret_cast<const uint2*>(rs.cand_cur + v0);  // arrays padded to 16 bytes
+    const uint32_t w2[2] = {f.x, f.y};
+    int cnt = 0;
+#pragma unroll
+    for (int b = 0; b < 8; ++b) cnt += ((w2[b >> 2] >> (8 * (b & 3))) & 0xffu) != 0;
+    int pre = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, pre, o);
+      if (lane >= o) pre += t;
+    }
+    const int total = __shfl_sync(0xffffffffu, pre, 31);
+    int pos = pre - cnt;
+#pragma unroll
+    for (int b = 0; b < 8; ++b)
+      if (((w2[b >> 2] >> (8 * (b & 3))) & 0xffu) != 0) tile[wib][pos++] = (int32_t)(v0 + b);
+    __syncwarp();
+    for (int i0 = 0; i0 < total; i0 += T) step(tile[wib], i0, total);
+    __syncwarp();
   }
 }
 
