@@ -2027,7 +2027,7 @@ __global__ void __launch_bounds__(kGrowThreads) k_ub_refine(GraphDev g, LevelArg
 // clamp. The tables of PrunedDP++'s tour bound
 // (graph_v_of_v_idealID_PrunedDPPlusPlus.h:268-386) for this query's
 // groups, rebuilt before every merge because the bound may have dropped.
-__global__ void __launch_bounds__(256) k_tour_table(LevelArgs a, const int32_t* __restrict__ group_ptr,
+__global__ void __launch_bounds__(1024) k_tour_table(LevelArgs a, const int32_t* __restrict__ group_ptr,
                                                     const int32_t* __restrict__ members,
                                                     const int32_t* __restrict__ perm, int32_t* __restrict__ tour) {
   constexpr int KM = kTourMaxK;
@@ -2040,11 +2040,17 @@ __global__ void __launch_bounds__(256) k_tour_table(LevelArgs a, const int32_t* 
   for (int t = threadIdx.x; t < KM * KM; t += blockDim.x) D[t / KM][t % KM] = beyond;
   for (int t = threadIdx.x; t < k * W * k; t += blockDim.x) F[t] = ub;
   __syncthreads();
-  for (int b = 0; b < k; ++b)
-    for (int32_t i = group_ptr[b] + threadIdx.x; i < group_ptr[b + 1]; i += blockDim.x) {
-      const int32_t* d = a.cost + (int64_t)perm[members[i]] * a.stride1;  // wave 1: rank of {g} is g
-      for (int g2 = 0; g2 < k; ++g2) atomicMin(&D[g2][b], min(d[g2], beyond));
-    }
+  // every member of every group at once: member i belongs to the last group
+  // whose first member is at or before i
+  __shared__ int32_t gstart[KM + 1];
+  if (threadIdx.x <= k) gstart[threadIdx.x] = group_ptr[threadIdx.x];
+  __syncthreads();
+  for (int32_t i = gstart[0] + threadIdx.x; i < gstart[k]; i += blockDim.x) {
+    int b = 0;
+    for (int bb = 1; bb < k; ++bb) b = i >= gstart[bb] ? bb : b;
+    const int32_t* d = a.cost + (int64_t)perm[members[i]] * a.stride1;  // wave 1: rank of {g} is g
+    for (int g2 = 0; g2 < k; ++g2) atomicMin(&D[g2][b], min(d[g2], beyond));
+  }
   __syncthreads();
   int32_t sym = 0;
   if (threadIdx.x < kk) sym = max(D[threadIdx.x / k][threadIdx.x % k], D[threadIdx.x % k][threadIdx.x / k]);
@@ -2347,7 +2353,7 @@ cudaError_t launch_tour_table(const LevelArgs& a, const int32_t* group_ptr, cons
     const cudaError_t e = cudaFuncSetAttribute(k_tour_table, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
   }
-  k_tour_table<<<1, 256, smem, stream>>>(a, group_ptr, members, perm, tour);
+  k_tour_table<<<1, 1024, smem, stream>>>(a, group_ptr, members, perm, tour);
   return cudaGetLastError();
 }
 
