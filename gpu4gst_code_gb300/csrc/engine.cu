@@ -2157,7 +2157,6 @@ gst_status gst_graph_debug_table(gst_graph* g, int32_t k, int32_t* out) {
   return GST_OK;
 }
 
-
 // ------------------------------------------------------ learned proposal --
 int64_t gst_scorer_num_params(void) { return kNumParams; }
 
@@ -2299,6 +2298,27 @@ gst_status gst_scorer_train_step(gst_graph* g, gst_scorer* sc, const int32_t* gr
   GST_CUDA(cudaStreamSynchronize(s));
   if (loss) *loss = l;
   return GST_OK;
+}
+
+gst_status gst_debug_scorer_wait_timeout(gst_graph* g, const gst_scorer* sc, uint32_t extra_bytes, int32_t* flag_out) {
+  g_last_error.clear();
+  if (!g || !sc || !flag_out) return fail(GST_BAD_INPUT, "null argument");
+  if (extra_bytes > (1u << 16)) return fail(GST_BAD_INPUT, "extra_bytes above 64 KiB");
+  DeviceGuard dg(g->device);
+  std::lock_guard<std::mutex> lock(g->mu);
+  gst_status st = ensure_learn_infer(g);
+  if (st != GST_OK) return st;
+  LearnWs& lw = g->lw;
+  cudaStream_t s = g->stream;
+  GST_CUDA(launch_layer_gemm(g->V, lw.hb_map[0], lw.hb_map[2], sc->wcat, sc->params, 1, lw.hb[1], nullptr,
+                             lw.infer_err, extra_bytes, s));
+  int32_t flag = 0;
+  GST_CUDA(cudaMemcpyAsync(&flag, lw.infer_err, sizeof(flag), cudaMemcpyDeviceToHost, s));
+  GST_CUDA(cudaStreamSynchronize(s));
+  GST_CUDA(cudaMemsetAsync(lw.infer_err, 0, sizeof(int32_t), s));
+  GST_CUDA(cudaStreamSynchronize(s));
+  *flag_out = flag;
+  return flag ? fail(GST_INTERNAL, "scorer layer: a wait ran out") : GST_OK;
 }
 
 gst_status gst_propose(gst_graph* g, gst_scorer* sc, const int32_t* group_ptr, const int32_t* members, int32_t k,

@@ -66,6 +66,13 @@ cudaError_t launch_infer_layer(const GraphDev& g, const int32_t* hub_of, const f
                                const __nv_bfloat16* hin, const CUtensorMap& hin_map, __nv_bfloat16* agg,
                                const CUtensorMap& agg_map, const __nv_bfloat16* wcat_l, const float* params, int l,
                                __nv_bfloat16* hout, float* scores, int32_t* err, cudaStream_t s);
+// The layer GEMM alone (launch_infer_layer runs it after the neighbour
+// mean). extra_tx > 0 makes each CTA's first tile wait for more bytes than
+// its loads deliver, so that the wait runs out and sets *err (the test of
+// the bounded waits); 0 otherwise.
+cudaError_t launch_layer_gemm(int32_t V, const CUtensorMap& hin_map, const CUtensorMap& agg_map,
+                              const __nv_bfloat16* wcat_l, const float* params, int l, __nv_bfloat16* hout,
+                              float* scores, int32_t* err, uint32_t extra_tx, cudaStream_t s);
 // The proposal's root without a network: most groups within 1 hop, then 2,
 // then 3, then degree (s = 1000 x3 + 100 x4 + 10 x5 + x1).
 cudaError_t launch_feature_score(int32_t V, const float* x, float* s, cudaStream_t st);

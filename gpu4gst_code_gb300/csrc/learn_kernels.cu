@@ -322,7 +322,8 @@ __global__ void __launch_bounds__(kTcThreads) k_infer_layer_tc(const __grid_cons
                                                                const float* __restrict__ wo,
                                                                const float* __restrict__ bo_ptr,
                                                                __nv_bfloat16* __restrict__ hout,
-                                                               float* __restrict__ scores, int32_t* __restrict__ err) {
+                                                               float* __restrict__ scores, int32_t* __restrict__ err,
+                                                               uint32_t extra_tx) {
   extern __shared__ uint8_t tc_dsm[];
   const uint32_t raw = smem_u32(tc_dsm);
   uint8_t* sm = tc_dsm + (((raw + 1023u) & ~1023u) - raw);  // swizzle atoms are 1024-byte aligned
@@ -371,8 +372,10 @@ __global__ void __launch_bounds__(kTcThreads) k_infer_layer_tc(const __grid_cons
   // stage s of A holds the CTA's tiles i = s, s + 2, ...: tile i + 1 loads
   // while tile i is multiplied and written out (its stage was freed when
   // tile i - 1's MMAs completed)
+  // extra_tx (0 but in the bounded-wait test) raises the byte count the
+  // CTA's first tile waits for above what its loads deliver
   auto load_tile = [&](int64_t t, int st) {
-    mbar_expect_tx(&full[st], kTcTileBytes);
+    mbar_expect_tx(&full[st], kTcTileBytes + (t == blockIdx.x ? extra_tx : 0u));
     tma_load_2d(sA + st * 32768, &map_h, 0, (int32_t)(t * kTcRows), &full[st]);
     tma_load_2d(sA + st * 32768 + 16384, &map_a, 0, (int32_t)(t * kTcRows), &full[st]);
   };
@@ -838,10 +841,18 @@ cudaError_t launch_infer_layer(const GraphDev& g, const int32_t* hub_of, const f
                                const __nv_bfloat16* hin, const CUtensorMap& hin_map, __nv_bfloat16* agg,
                                const CUtensorMap& agg_map, const __nv_bfloat16* wcat_l, const float* params, int l,
                                __nv_bfloat16* hout, float* scores, int32_t* err, cudaStream_t s) {
+  k_mean_bf16<<<grid_for((int64_t)g.V * 8, 256, 152 * 32), 256, 0, s>>>(g, hub_of, hub_sum, hin, agg);
+  const cudaError_t me = cudaGetLastError();
+  if (me != cudaSuccess) return me;
+  return launch_layer_gemm(g.V, hin_map, agg_map, wcat_l, params, l, hout, scores, err, 0u, s);
+}
+
+cudaError_t launch_layer_gemm(int32_t V, const CUtensorMap& hin_map, const CUtensorMap& agg_map,
+                              const __nv_bfloat16* wcat_l, const float* params, int l, __nv_bfloat16* hout,
+                              float* scores, int32_t* err, uint32_t extra_tx, cudaStream_t s) {
   const float* bias = params + layer_off(l) + 2 * kHid * kHid;
   const float* wo = scores ? params + kOffWo : nullptr;
   const float* bo = scores ? params + kOffBo : nullptr;
-  k_mean_bf16<<<grid_for((int64_t)g.V * 8, 256, 152 * 32), 256, 0, s>>>(g, hub_of, hub_sum, hin, agg);
   // kTcCtasPerSm CTAs per SM (shared memory allows two; their tensor memory,
   // 2 x 64 columns, is a quarter of an SM's), each with two tiles in flight
   static const int ctas = [] {
@@ -854,9 +865,10 @@ cudaError_t launch_infer_layer(const GraphDev& g, const int32_t* hub_of, const f
   }();
   const cudaError_t ae = cudaFuncSetAttribute(k_infer_layer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
   if (ae != cudaSuccess) return ae;
-  const int64_t tiles = ((int64_t)g.V + kTcRows - 1) / kTcRows;
+  const int64_t tiles = ((int64_t)V + kTcRows - 1) / kTcRows;
   const int grid = (int)std::min<int64_t>(tiles, ctas);
-  k_infer_layer_tc<<<grid, kTcThreads, kTcSmem, s>>>(hin_map, agg_map, g.V, wcat_l, bias, wo, bo, hout, scores, err);
+  k_infer_layer_tc<<<grid, kTcThreads, kTcSmem, s>>>(hin_map, agg_map, V, wcat_l, bias, wo, bo, hout, scores, err,
+                                                     extra_tx);
   return cudaGetLastError();
 }
 

@@ -106,6 +106,7 @@ SIGNATURES = {
     "gst_result_times": (None, [C.c_void_p, F64P]),
     "gst_result_stats": (None, [C.c_void_p, I64P]),
     "gst_graph_debug_table": (C.c_int, [C.c_void_p, C.c_int32, I32P]),
+    "gst_debug_scorer_wait_timeout": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, I32P]),
     "gst_group_distances_noalloc": (
         C.c_int,
         [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int64, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p,

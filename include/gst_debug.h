@@ -20,6 +20,19 @@ extern "C" {
  * device and copies it only on request. */
 gst_status gst_graph_debug_table(gst_graph *g, int32_t k, int32_t *out);
 
+typedef struct gst_scorer gst_scorer;
+
+/* Test of the scorer layer's bounded waits: runs the first layer's
+ * tensor-core GEMM on g's activation buffers (whatever they hold) with the
+ * first tile of every CTA waiting for extra_bytes more than its TMA loads
+ * deliver, so that the wait runs out (after about a second at most).
+ * *flag_out receives the layer's error flag (1: a load wait ran out; 0:
+ * none did) and the status is GST_INTERNAL when it is set; the flag is
+ * cleared again and the graph stays usable. extra_bytes = 0 runs the GEMM
+ * normally (flag 0, GST_OK). */
+gst_status gst_debug_scorer_wait_timeout(gst_graph *g, const gst_scorer *sc, uint32_t extra_bytes,
+                                         int32_t *flag_out);
+
 #ifdef __cplusplus
 }
 #endif

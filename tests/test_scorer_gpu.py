@@ -156,3 +156,26 @@ def test_trained_network_gains_over_the_method_without_it():
                 ratios[name].append(res.proposal_cost / opt)
     mean = {k: float(np.mean(v)) for k, v in ratios.items()}
     assert mean["trained"] < mean["none"] and mean["trained"] < mean["untrained"], mean
+
+
+def test_layer_wait_that_runs_out_reports_and_leaves_the_device_usable(case):
+    """The layer GEMM's waits are bounded: a first tile that waits for 16
+    bytes more than its TMA loads deliver runs its wait out (about a second
+    at most), the layer reports it through its error flag (GST_INTERNAL,
+    flag 1), and the next inference on the same graph scores like the
+    oracle."""
+    import ctypes as C
+
+    from gpu4gst_code_gb300 import native as N
+
+    g, gp, mem, p, tree, A, x = case
+    want, _, _ = SO.forward(p.astype(np.float64), A, x)
+    with N.Graph(g.row_ptr, g.col, g.w) as dg, N.Scorer(p) as sc:
+        flag = C.c_int32(-1)
+        st = N.lib().gst_debug_scorer_wait_timeout(dg._h, sc._h, 0, C.byref(flag))
+        assert N.Status(st) == N.Status.OK and flag.value == 0
+        st = N.lib().gst_debug_scorer_wait_timeout(dg._h, sc._h, 16, C.byref(flag))
+        assert N.Status(st) == N.Status.INTERNAL and flag.value == 1
+        got = sc.scores(dg, gp, mem)
+    assert np.abs(got - want).max() <= 0.03 * (np.abs(want).max() + 1e-6)
+
