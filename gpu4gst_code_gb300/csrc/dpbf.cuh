@@ -170,9 +170,11 @@ struct LevelArgs {
 };
 
 // Groups up to which the merge adds PrunedDP++'s tour bounds to the one-label
-// bound (k_tour_table keeps the k x 2^k x k path table in shared memory:
-// 162 KB at k = 9).
-constexpr int kTourMaxK = 9;
+// bound. k_tour_table keeps the k x 2^k x k path table in shared memory up
+// to kTourSmemMaxK groups (162 KB at k = 9) and builds it in place in the
+// tour buffer (global memory, 400 KB at k = 10) beyond.
+constexpr int kTourMaxK = 10;
+constexpr int kTourSmemMaxK = 9;
 
 // Queries with at most kMergeTabK groups merge a vertex per thread from
 // per-level split tables (k_merge_vertex); larger k use k_merge.

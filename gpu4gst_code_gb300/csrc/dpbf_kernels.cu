@@ -2032,10 +2032,11 @@ __global__ void __launch_bounds__(1024) k_tour_table(LevelArgs a, const int32_t*
                                                     const int32_t* __restrict__ perm, int32_t* __restrict__ tour) {
   constexpr int KM = kTourMaxK;
   __shared__ int32_t D[KM][KM];
-  extern __shared__ int32_t F[];  // k x 2^k x k (64 KB at k = 8)
+  extern __shared__ int32_t Fs[];  // k x 2^k x k (64 KB at k = 8), up to kTourSmemMaxK groups
   const int32_t ub = a.params->ub;
   if (ub <= 0) return;  // no bound: the merge does not read the table
   const int k = a.k, W = 1 << k, kk = k * k;
+  int32_t* F = k <= kTourSmemMaxK ? Fs : tour;  // beyond: the path table is built in place
   const int32_t beyond = ub / 2 + 1;
   for (int t = threadIdx.x; t < KM * KM; t += blockDim.x) D[t / KM][t % KM] = beyond;
   for (int t = threadIdx.x; t < k * W * k; t += blockDim.x) F[t] = ub;
@@ -2070,7 +2071,8 @@ __global__ void __launch_bounds__(1024) k_tour_table(LevelArgs a, const int32_t*
     }
     __syncthreads();
   }
-  for (int t = threadIdx.x; t < k * W * k; t += blockDim.x) tour[t] = F[t];
+  if (F != tour)
+    for (int t = threadIdx.x; t < k * W * k; t += blockDim.x) tour[t] = F[t];
   // W2[i][X] = the cheapest order visiting X from i, ending at any group
   // j != i (0 for X = {i}): PrunedDP++'s W2 (PrunedDPPlusPlus.h:565-585)
   for (int t = threadIdx.x; t < k * W; t += blockDim.x) {
@@ -2348,7 +2350,7 @@ cudaError_t launch_grow_round(const GraphDev& g, const LevelArgs& a, int num_sms
 cudaError_t launch_tour_table(const LevelArgs& a, const int32_t* group_ptr, const int32_t* members,
                               const int32_t* perm, int32_t* tour, cudaStream_t stream) {
   if (a.k > kTourMaxK) return cudaErrorInvalidValue;
-  const size_t smem = (size_t)a.k * ((size_t)1 << a.k) * a.k * sizeof(int32_t);
+  const size_t smem = a.k <= kTourSmemMaxK ? (size_t)a.k * ((size_t)1 << a.k) * a.k * sizeof(int32_t) : 0;
   if (smem > kSmemNoOptIn) {  // k = 8 (set on the current device every time)
     const cudaError_t e = cudaFuncSetAttribute(k_tour_table, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;

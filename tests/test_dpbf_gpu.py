@@ -155,9 +155,10 @@ def test_many_group_counts(k):
         _check(g.row_ptr, g.col, g.w, gp, mem, res, want.cost)
 
 
-@pytest.mark.parametrize("k", [9, 11, 12])
+@pytest.mark.parametrize("k", [9, 10, 11, 12])
 def test_wide_masks_merge_per_state(k):
-    """k = 9 merges a vertex per thread with the tour bounds (k_merge_vertex),
+    """k = 9 and 10 merge a vertex per thread with the tour bounds
+    (k_merge_vertex; at k = 10 the path table is built in global memory),
     k > 10 a state per thread (k_merge, mask-table lookups): exact against
     the oracle unpruned, with a starting bound and with refinement."""
     g = native.gen_random_connected(300, 900, 1, 40, 60 + k)
