@@ -234,10 +234,10 @@ class ClockSampler:
 
 
 # DRAM bytes (read + write) of all growth-kernel launches of one plain
-# query from one ncu capture of the 400k-vertex case (profiles/
-# grow_dram_ba400k_k6.md), scaled by the vertex count for the 1M workload
-# (a lower bound there); None where no capture exists.
-TRAFFIC_PER_STEP = {"ba400k_k6": 2.4e9, "ba1m_k6": 6.0e9}
+# query, each from one ncu capture of that workload (profiles/
+# grow_dram_ba1m_k6.md: every growth launch of query 0 at full size, one pass
+# per launch; profiles/grow_dram_ba400k_k6.md); None where no capture exists.
+TRAFFIC_PER_STEP = {"ba400k_k6": 2.4e9, "ba1m_k6": 9.78e9}
 
 
 def table_bytes(V, k):
@@ -586,8 +586,8 @@ def main():
                                  "sparse rounds; k_grow_group / k_grow_hubs for wider rows), plain method, per step",
                      "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": peak_kind, "traffic": traffic_per_step(wl),
-                     "traffic_note": "DRAM bytes of the growth kernels per query: an ncu capture of the 400k case "
-                                     "scaled by V (profiles/grow_dram_ba400k_k6.md)",
+                     "traffic_note": "DRAM bytes of the growth kernels per query: an ncu capture of every growth "
+                                     "launch of one plain query of this workload (profiles/grow_dram_ba1m_k6.md)",
                      "algorithmic_bytes_per_step": grow_bytes / args.steps,
                      "grow_ms_per_step": grow_ms / args.steps,
                      "rounds_per_grown_wave": sum(r.stats["rounds"] for r in roof) / len(roof) / max(1, wl["k"] - 1),
