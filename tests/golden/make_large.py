@@ -15,7 +15,11 @@ The GPU machine never runs this script (it takes tens of minutes and ~10 GB of
 host memory per 2M- or 4M-vertex query); bench.py and the -m gpu tests only
 read the committed file.
 
-  python tests/golden/make_large.py [--workloads ba1m_k6,ba2m_k8,...] [--jobs N]
+  python tests/golden/make_large.py [--workloads ba1m_k6,ba2m_k8,...] [--jobs N] [--reference N]
+
+--reference N also runs the reference's own DPBF (compiled from its headers in
+this container, oracle/_ref) on the first N cases of each workload and
+records its cost (ref_cost) beside the oracle's.
 """
 from __future__ import annotations
 
@@ -75,10 +79,31 @@ def _solve(args):
             "cost": int(r.cost), "pops": int(r.pops), "oracle_s": round(sec, 3)}
 
 
+def _reference(args):
+    """The reference's own DPBF solver (graph_v_of_v_idealID_DPBF_only_ec,
+    compiled from its unmodified headers into oracle/_ref) on one case."""
+    name, i = args
+    import bench
+    import oracle
+
+    wl = dict(bench.WORKLOADS[name], name=name)
+    g = bench.make_graph(wl, oracle)
+    gp, mem = bench.make_query(wl, g, i, oracle)
+    t = time.perf_counter()
+    r = oracle.reference(g.row_ptr, g.col, g.w, gp, mem, solver="dpbf")
+    sec = time.perf_counter() - t
+    if r is None:
+        raise RuntimeError("the reference's solver library (oracle/_ref) is not available")
+    return name, i, int(r.cost), round(sec, 3)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--workloads", default=",".join(PLAN))
     ap.add_argument("--jobs", type=int, default=0, help="parallel oracle processes (0: the plan's)")
+    ap.add_argument("--reference", type=int, default=0,
+                    help="also solve the first N cases of each workload with the reference's own DPBF (ref_cost)")
+    ap.add_argument("--reference-jobs", type=int, default=2)
     args = ap.parse_args()
     import oracle
 
@@ -100,6 +125,19 @@ def main():
                 done["generator"] = ("tests/golden/make_large.py: bench.py's workloads and query seeds, oracle.gen_* "
                                      "instances, oracle.dpbf costs")
                 done["host"] = f"{platform.machine()}, {os.cpu_count()} threads"
+                OUT.write_text(json.dumps(done, indent=1) + "\n")
+    if args.reference:
+        oracle.build_ref()
+        byname = {(c["workload"], c["index"]): c for c in done["cases"]}
+        todo = [(name, i) for name in args.workloads.split(",") for i in range(args.reference)
+                if (name, i) in byname and "ref_cost" not in byname[(name, i)]]
+        ctx = mp.get_context("spawn")
+        with cf.ProcessPoolExecutor(max_workers=args.reference_jobs, mp_context=ctx) as ex:
+            for name, i, cost, sec in ex.map(_reference, todo):
+                byname[(name, i)].update(ref_cost=cost, ref_s=sec)
+                print(json.dumps(byname[(name, i)]), flush=True)
+                done["reference"] = ("ref_cost: the reference's own graph_v_of_v_idealID_DPBF_only_ec, compiled from its "
+                                     "unmodified headers (oracle/build_ref.sh), single-threaded; ref_s its time")
                 OUT.write_text(json.dumps(done, indent=1) + "\n")
 
 

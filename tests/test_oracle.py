@@ -100,3 +100,21 @@ def _edges(e):
     for u, v, w in e:
         seen[(min(int(u), int(v)), max(int(u), int(v)))] = int(w)
     return np.array([[a, b, w] for (a, b), w in seen.items()], np.int32).reshape(-1, 3)
+
+
+def test_large_golden_costs_agree_with_the_reference_solver():
+    """tests/golden/large.json: wherever the reference's own DPBF
+    (graph_v_of_v_idealID_DPBF_only_ec, compiled from its unmodified
+    headers) was run on a benchmark query (ref_cost, recorded by
+    make_large.py --reference), it returned the oracle's cost — the pin of
+    the full-size golden costs on the reference itself."""
+    import json
+    from pathlib import Path
+
+    cases = json.loads((Path(__file__).resolve().parent / "golden" / "large.json").read_text())["cases"]
+    pinned = [c for c in cases if "ref_cost" in c]
+    assert pinned, "no case carries the reference solver's cost"
+    assert {c["workload"] for c in pinned} >= {"rc1k_k3", "ba1m_k6"}
+    for c in pinned:
+        assert c["ref_cost"] == c["cost"], (c["workload"], c["index"], c["ref_cost"], c["cost"])
+
