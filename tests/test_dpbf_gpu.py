@@ -382,16 +382,19 @@ def test_replica_pool_matches_single():
 
 
 @pytest.mark.parametrize("use_graph", MODES)
-def test_full_state_table_with_hub_segments(use_graph):
+@pytest.mark.parametrize("k", [4, 6])
+def test_full_state_table_with_hub_segments(use_graph, k):
     """The whole table of the grown waves equals the oracle's exact fixpoint
     on a BA graph whose hubs span one and several 256-entry segments (the
     hub rows are relaxed whole by one warp, or folded through a scratch row
-    by several), with dense, flag-checked and sparse rounds all occurring."""
+    by several), with dense, flag-checked and sparse rounds all occurring;
+    at k = 6 the waves of 15 and 20 masks also run their small-frontier
+    sparse rounds by vertex teams."""
     g = native.gen_barabasi_albert(30000, 4, 1, 100, 77)
     deg = np.diff(g.row_ptr)
     assert (deg > 256).sum() > 0 and (deg > 64).sum() > 100
-    gp, mem = native.gen_groups_zipf_degree(g, 4, 1.2, 5, 500, 79)
-    k = len(gp) - 1
+    gp, mem = native.gen_groups_zipf_degree(g, k, 1.2, 5, 500, 79)
+    assert len(gp) - 1 == k
     want = oracle.dp_table(g.row_ptr, g.col, g.w, gp, mem)
     want = np.where(want == ORACLE_INF, native.COST_LIMIT, want)
     with native.Graph(g.row_ptr, g.col, g.w) as dg:
