@@ -1824,7 +1824,7 @@ __global__ void __launch_bounds__(kGrowThreads, (G <= 4 ? 4 : 3)) k_grow_team(Gr
   const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
   clear_flags(a, rs, t0, nthreads);
-  hub_relax_team<(G <= 1 ? 1 : G <= 2 ? 2 : G <= 4 ? 4 : 8), true>(g, a, rs, acc);
+  hub_relax_team<(G <= 1 ? 1 : G <= 2 ? 2 : G <= 4 ? 4 : G <= 8 ? 8 : G <= 16 ? 16 : 32), true>(g, a, rs, acc);
   constexpr int T = 32 / G;  // teams per warp; lanes T*G .. 31 idle
   const int lane = threadIdx.x & 31;
   const int team = lane / G, glane = lane - team * G;
@@ -1866,12 +1866,15 @@ __global__ void __launch_bounds__(kGrowThreads, (G <= 4 ? 4 : 3)) k_grow_team(Gr
 
 // G lanes per vertex for waves wider than kMaxThreadMasks. Each warp takes
 // 32 consecutive vertices at a time, finds the candidates among them with
-// one ballot, and its 32/G groups take the candidates in turn.
-template <int G, int L>
+// one ballot, and its 32/G groups take the candidates in turn. SPARSE_ONLY:
+// the wave's dense rounds run in k_grow_team (strides 28, 36, 56, 72: the
+// waves of k = 7 and 8), this kernel its sparse rounds.
+template <int G, int L, bool SPARSE_ONLY>
 __global__ void __launch_bounds__(kGrowThreads, (L >= 3 ? 3 : 4)) k_grow_group(GraphDev g, LevelArgs a) {
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&a.ctr->grow_launches, 1);
   RoundState rs;
   if (!round_begin(g, a, rs)) return;
+  if (SPARSE_ONLY && rs.dense) return;  // dense rounds of this wave run in k_grow_team
   __shared__ BlockAcc ba;
   block_acc_init(ba);
   uint32_t acc[kAccN] = {0, 0, 0, 0, 0, 0, 0};
@@ -1880,7 +1883,7 @@ __global__ void __launch_bounds__(kGrowThreads, (L >= 3 ? 3 : 4)) k_grow_group(G
     const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
     clear_flags(a, rs, t0, nthreads);
   }
-  if (rs.dense)
+  if (!SPARSE_ONLY && rs.dense)
     hub_relax<((G * L + 31) / 32 < 4 ? (G * L + 31) / 32 : 4)>(g, a, rs, acc);
   else
     hub_mark(g, a, rs, acc);
@@ -2286,10 +2289,10 @@ cudaError_t thread_round(const GraphDev& g, const LevelArgs& a, int num_sms, cud
   return launch_round(k_grow_thread<MP>, occ, g, a, num_sms, kGrowThreads, stream);
 }
 
-template <int G, int L>
+template <int G, int L, bool SPARSE_ONLY = false>
 cudaError_t group_round(const GraphDev& g, const LevelArgs& a, int num_sms, cudaStream_t stream) {
-  static const int occ = resident_blocks(k_grow_group<G, L>);
-  return launch_round(k_grow_group<G, L>, occ, g, a, num_sms, kGrowThreads / G, stream);
+  static const int occ = resident_blocks(k_grow_group<G, L, SPARSE_ONLY>);
+  return launch_round(k_grow_group<G, L, SPARSE_ONLY>, occ, g, a, num_sms, kGrowThreads / G, stream);
 }
 }  // namespace
 
@@ -2340,6 +2343,26 @@ cudaError_t launch_grow_round(const GraphDev& g, const LevelArgs& a, int num_sms
       default: te = team_round<6>(g, a, num_sms, stream); break;
     }
     return te;
+  }
+  // strides of the waves of k = 7 and 8: sparse rounds by lane groups, dense
+  // rounds by teams of stride/4 lanes (16-byte quarters of the rows)
+  cudaError_t ge = cudaErrorNotSupported;
+  switch (a.stride) {
+    case 28: ge = group_round<16, 2, true>(g, a, num_sms, stream); break;
+    case 36: ge = group_round<32, 2, true>(g, a, num_sms, stream); break;
+    case 56: ge = group_round<32, 2, true>(g, a, num_sms, stream); break;
+    case 72: ge = group_round<32, 3, true>(g, a, num_sms, stream); break;
+    default: break;
+  }
+  if (ge != cudaErrorNotSupported) {
+    if (ge != cudaSuccess) return ge;
+    ++*launches;
+    switch (a.stride) {
+      case 28: return team_round<7>(g, a, num_sms, stream);
+      case 36: return team_round<9>(g, a, num_sms, stream);
+      case 56: return team_round<14>(g, a, num_sms, stream);
+      default: return team_round<18>(g, a, num_sms, stream);
+    }
   }
   if (a.stride <= 32) return group_round<16, 2>(g, a, num_sms, stream);
   if (a.stride <= 64) return group_round<32, 2>(g, a, num_sms, stream);
