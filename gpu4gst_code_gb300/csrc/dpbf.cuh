@@ -82,7 +82,11 @@ struct SolveParams {
   int32_t ovf_limit;
   int32_t dense_shift;  // dense round when the previous one changed > V >> dense_shift
   int32_t refine;       // lower ub between waves from partial trees (k_ub_refine)
-  int32_t pad;
+  // A bound may arrive while the solve runs (launch_bound_min from another
+  // stream): every merge writes its wave's caps (kInf without a bound yet)
+  // and the tour table is built without a bound, so that a wave whose merge
+  // saw no bound can still prune by caps and tours once one arrives.
+  int32_t late_bound;
 };
 
 // Growth-loop control of the current wave (reset before each wave).
@@ -205,6 +209,8 @@ cudaError_t launch_tour_table(const LevelArgs& a, const int32_t* group_ptr, cons
 // After wave a.level's growth: with params->refine set, lowers params->ub to
 // the cheapest T(v,S) + sum of T(v,{g}) over the groups g outside S.
 cudaError_t launch_ub_refine(const GraphDev& g, const LevelArgs& a, int num_sms, cudaStream_t stream);
+// Lowers params->ub to cand (none yet: to cand) by a CAS loop on the device.
+cudaError_t launch_bound_min(SolveParams* params, int32_t cand, cudaStream_t stream);
 cudaError_t launch_argmin(const GraphDev& g, const int32_t* full_slice, int32_t stride, Counters* ctr,
                           cudaStream_t stream);
 cudaError_t launch_backtrack(const GraphDev& g, int64_t nnz, const int32_t* par, const MaskInfo* minfo,

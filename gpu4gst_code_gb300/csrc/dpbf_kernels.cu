@@ -180,6 +180,7 @@ __global__ void __launch_bounds__(kGrowThreads) k_merge(GraphDev g, LevelArgs a)
   const int32_t ub_light = a.params->ub;
   const int32_t ovf_limit = a.params->ovf_limit;
   const int32_t keep23 = merged_keep(a, ub);
+  const bool late = a.params->late_bound != 0;
   uint8_t* flag2 = a.flags + 2 * (int64_t)a.vpad;
   long long acc[3] = {0, 0, 0};  // finite states, splits, overflow
   for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += stride) {
@@ -226,7 +227,7 @@ __global__ void __launch_bounds__(kGrowThreads) k_merge(GraphDev g, LevelArgs a)
     }
     a.cost[a.base + idx] = best;
     a.par[a.base + idx] = code;
-    if (ub > 0) a.capt[idx] = cap;  // the growth of this wave prunes by it
+    if (ub > 0 || late) a.capt[idx] = cap;  // the growth of this wave prunes by it
     if (best < kInf) {
       flag2[v] = 1;
       ++acc[0];
@@ -283,6 +284,7 @@ __global__ void __launch_bounds__(NT) k_merge_staged(GraphDev g, LevelArgs a, Me
   const int32_t ub_light = a.params->ub;
   const int32_t ovf_limit = a.params->ovf_limit;
   const int32_t keep23 = merged_keep(a, ub);
+  const bool late = a.params->late_bound != 0;
   const bool light_parts = a.level < a.k;
   uint8_t* flag2 = a.flags + 2 * (int64_t)a.vpad;
   long long acc[3] = {0, 0, 0};  // finite states, splits, overflow
@@ -405,7 +407,7 @@ __global__ void __launch_bounds__(NT) k_merge_staged(GraphDev g, LevelArgs a, Me
       }
       rowc[j0 >> 2] = make_int4(b4[0], b4[1], b4[2], b4[3]);
       rowp[j0 >> 2] = make_int4(c4[0], c4[1], c4[2], c4[3]);
-      if (ub > 0) rowk[j0 >> 2] = make_int4(k4[0], k4[1], k4[2], k4[3]);  // the growth of this wave prunes by it
+      if (ub > 0 || late) rowk[j0 >> 2] = make_int4(k4[0], k4[1], k4[2], k4[3]);  // the growth of this wave prunes by it
     }
     if (any) flag2[v] = 1;
   }
@@ -431,6 +433,7 @@ __global__ void __launch_bounds__(kGrowThreads) k_merge_vertex(GraphDev g, Level
   const int32_t ub_light = a.params->ub;
   const int32_t ovf_limit = a.params->ovf_limit;
   const int32_t keep23 = merged_keep(a, ub);
+  const bool late = a.params->late_bound != 0;
   const bool light_parts = a.level < a.k;
   uint8_t* flag2 = a.flags + 2 * (int64_t)a.vpad;
   long long acc[3] = {0, 0, 0};  // finite states, splits, overflow
@@ -503,7 +506,7 @@ __global__ void __launch_bounds__(kGrowThreads) k_merge_vertex(GraphDev g, Level
       }
       rowc[j0 >> 2] = make_int4(b4[0], b4[1], b4[2], b4[3]);
       rowp[j0 >> 2] = make_int4(c4[0], c4[1], c4[2], c4[3]);
-      if (ub > 0) rowk[j0 >> 2] = make_int4(k4[0], k4[1], k4[2], k4[3]);  // the growth of this wave prunes by it
+      if (ub > 0 || late) rowk[j0 >> 2] = make_int4(k4[0], k4[1], k4[2], k4[3]);  // the growth of this wave prunes by it
     }
     if (any) flag2[v] = 1;
   }
@@ -2036,8 +2039,17 @@ __global__ void __launch_bounds__(1024) k_tour_table(LevelArgs a, const int32_t*
   constexpr int KM = kTourMaxK;
   __shared__ int32_t D[KM][KM];
   extern __shared__ int32_t Fs[];  // k x 2^k x k (64 KB at k = 8), up to kTourSmemMaxK groups
-  const int32_t ub = a.params->ub;
-  if (ub <= 0) return;  // no bound: the merge does not read the table
+  // no bound: the merge does not read the table, unless one may still
+  // arrive before it (late_bound). Then no wave has grown under a bound yet
+  // (bounds only drop), wave 1's distances are exact, and the table is
+  // built with the open clamp kTourOpen; the merge caps distances at its own
+  // bound, and the entries stay lower bounds either way.
+  constexpr int32_t kTourOpen = 1 << 28;
+  int32_t ub = a.params->ub;
+  if (ub <= 0) {
+    if (!a.params->late_bound) return;
+    ub = kTourOpen;
+  }
   const int k = a.k, W = 1 << k, kk = k * k;
   int32_t* F = k <= kTourSmemMaxK ? Fs : tour;  // beyond: the path table is built in place
   const int32_t beyond = ub / 2 + 1;
@@ -2386,6 +2398,25 @@ cudaError_t launch_seed(const GraphDev& g, const LevelArgs& a, int num_sms, cuda
   int64_t blocks = ((int64_t)g.V + kGrowThreads - 1) / kGrowThreads;  // >= one warp per 32 vertices
   if (blocks > (int64_t)num_sms * 8) blocks = (int64_t)num_sms * 8;
   k_seed<<<(unsigned)blocks, kGrowThreads, 0, stream>>>(g, a);
+  return cudaGetLastError();
+}
+
+namespace {
+// Lowers the solve's bound to cand (a bound <= 0 is none yet): the learned
+// proposal's cost, injected while the solve's graph runs.
+__global__ void k_bound_min(SolveParams* p, int32_t cand) {
+  int32_t* ub = &p->ub;
+  int32_t old = *reinterpret_cast<volatile int32_t*>(ub);
+  while (old <= 0 || cand < old) {
+    const int32_t prev = atomicCAS(ub, old, cand);
+    if (prev == old) break;
+    old = prev;
+  }
+}
+}  // namespace
+
+cudaError_t launch_bound_min(SolveParams* params, int32_t cand, cudaStream_t stream) {
+  k_bound_min<<<1, 1, 0, stream>>>(params, cand);
   return cudaGetLastError();
 }
 

@@ -192,6 +192,10 @@ struct gst_graph {
   int num_sms = 0;
   cudaStream_t stream = nullptr;
   cudaStream_t side = nullptr;  // captures conditional bodies
+  // learned overlap (gst_solve_learned): the solve's parameters are on the
+  // device; its graph has finished; the end of the lane's queued work
+  cudaEvent_t ev_params = nullptr, ev_done = nullptr, ev_side = nullptr;
+  cudaEvent_t ev_poll = nullptr;  // wait_or_stop's marker on this context's stream
   int32_t V = 0;
   int64_t nnz = 0;
   int32_t* d_row_ptr = nullptr;
@@ -244,6 +248,8 @@ struct gst_result {
   int32_t ub = 0;             // pruning bound at the last wave (0 = none)
   int32_t proposal_cost = 0;  // cost of the learned path's proposed tree
   double propose_ms = 0;      // host wall time of the proposal
+  int32_t proposal_concurrent = 0;  // the proposal ran beside the DP, on a serving lane
+  double wall_ms = 0;         // learned solves: host wall time of the whole call
 };
 
 struct gst_scorer {
@@ -847,6 +853,7 @@ void fill_params(gst_graph* g, int32_t k, const gst_opts& o) {
                              : pruned                                 ? kDefaultDenseShiftPruned
                                                                       : kDefaultDenseShift;
   ws.h_params->refine = o.refine_bound ? 1 : 0;
+  ws.h_params->late_bound = 0;
 }
 
 // The result of a finished captured solve, from the counters, statistics and
@@ -869,9 +876,35 @@ gst_status finish_solve(gst_graph* g, int32_t k, gst_result* r) {
   return collect_tree(g, r, (int32_t)(c.best >> 32), (int32_t)(c.best & 0xffffffffull));
 }
 
-// One query. Caller holds g->mu and has validated the groups.
+// Waits for the work queued so far on g->stream; with stop given, returns
+// GST_TIMEOUT as soon as (*stop)() holds instead (the queued work still
+// runs: the caller orders the context's next use after it).
+gst_status wait_or_stop(gst_graph* g, const std::function<bool()>* stop) {
+  if (!stop) {
+    GST_CUDA(cudaStreamSynchronize(g->stream));
+    return GST_OK;
+  }
+  if (!g->ev_poll) GST_CUDA(cudaEventCreateWithFlags(&g->ev_poll, cudaEventDisableTiming));
+  GST_CUDA(cudaEventRecord(g->ev_poll, g->stream));
+  for (;;) {
+    const cudaError_t e = cudaEventQuery(g->ev_poll);
+    if (e == cudaSuccess) return GST_OK;
+    if (e != cudaErrorNotReady) GST_CUDA(e);
+    if ((*stop)()) return fail(GST_TIMEOUT, "stopped: the solve it served finished first");
+    std::this_thread::yield();
+  }
+}
+
+// One query. Caller holds g->mu and has validated the groups. With a
+// captured graph, `concurrent` (if given) runs on the host right after the
+// graph's launch (g->ev_done is recorded behind it), before the wait for
+// it; it may lower the bound in the device parameters
+// (SolveParams::late_bound is set for it) once g->ev_params, recorded after
+// their upload, has completed. With `stop`, the wait for the graph gives up
+// once (*stop)() holds (wait_or_stop).
 gst_status solve_one(gst_graph* g, const int32_t* group_ptr, const int32_t* members, int32_t k,
-                     const gst_opts& o, gst_result* r) {
+                     const gst_opts& o, gst_result* r, const std::function<void()>* concurrent = nullptr,
+                     const std::function<bool()>* stop = nullptr) {
   Workspace& ws = g->ws;
   const int64_t nmembers = group_ptr[k];
   gst_status st = ensure_workspace(g, k, nmembers);
@@ -889,16 +922,22 @@ gst_status solve_one(gst_graph* g, const int32_t* group_ptr, const int32_t* memb
     if (st != GST_OK) return st;
   }
   fill_params(g, k, o);
+  if (concurrent && use_graph) ws.h_params->late_bound = 1;  // the concurrent work may lower the bound mid-solve
 
   GST_CUDA(cudaEventRecord(ws.ev[0], s));
   GST_CUDA(cudaMemcpyAsync(ws.d_params, ws.h_params, sizeof(SolveParams), cudaMemcpyHostToDevice, s));
   GST_CUDA(cudaMemcpyAsync(ws.d_group_ptr, group_ptr, (size_t)(k + 1) * 4, cudaMemcpyHostToDevice, s));
   if (nmembers)
     GST_CUDA(cudaMemcpyAsync(ws.d_members, members, (size_t)nmembers * 4, cudaMemcpyHostToDevice, s));
+  if (concurrent) GST_CUDA(cudaEventRecord(g->ev_params, s));
   int64_t launches = 0;
   bool timeout = false;
   if (use_graph) {
     GST_CUDA(cudaGraphLaunch(ws.qg[k].exec, s));
+    if (concurrent) {  // host work (and its own stream) while the graph runs
+      GST_CUDA(cudaEventRecord(g->ev_done, s));
+      (*concurrent)();
+    }
   } else {
     st = run_host_loop(g, k, &launches, &timeout);
     if (st != GST_OK) return st;
@@ -909,7 +948,8 @@ gst_status solve_one(gst_graph* g, const int32_t* group_ptr, const int32_t* memb
     }
   }
   GST_CUDA(cudaEventRecord(ws.ev[2], s));
-  GST_CUDA(cudaStreamSynchronize(s));
+  st = wait_or_stop(g, stop);
+  if (st != GST_OK) return st;
   const Counters& c = *ws.h_ctr;
   // masks, k merges, a seed per grown wave, a refinement per grown wave but
   // the last, the tour tables (k <= kTourMaxK, waves 2..k-1), the growth
@@ -983,12 +1023,13 @@ HostTree mst_repair(gst_graph* g, std::vector<int32_t> set, int32_t root,
   // slot + 1 of every set vertex in a V-sized scratch array (zero outside)
   std::vector<int32_t>& slot = g->h_slot;
   if (slot.size() != (size_t)g->V) slot.assign((size_t)g->V, 0);
+  const gst_graph* hg = g->parent ? g->parent : g;  // lanes share their graph's host CSR
   for (size_t i = 0; i < n; ++i) slot[(size_t)set[i]] = (int32_t)i + 1;
   std::vector<std::pair<int32_t, std::pair<int32_t, int32_t>>> ind;  // (w, (i, j))
   for (size_t i = 0; i < n; ++i) {
     const int32_t v = set[i];
-    for (int32_t e = g->h_row[(size_t)v]; e < g->h_row[(size_t)v + 1]; ++e) {
-      const int2 x = g->h_adj[(size_t)e];
+    for (int32_t e = hg->h_row[(size_t)v]; e < hg->h_row[(size_t)v + 1]; ++e) {
+      const int2 x = hg->h_adj[(size_t)e];
       if (x.x <= v) continue;
       const int32_t j = slot[(size_t)x.x] - 1;
       if (j >= 0) ind.push_back({x.y, {(int32_t)i, j}});
@@ -1129,7 +1170,10 @@ gst_status ensure_learn_train(gst_graph* g, int32_t nids) {
 gst_status upload_groups(gst_graph* g, const int32_t* group_ptr, const int32_t* members, int32_t k) {
   Workspace& ws = g->ws;
   const int64_t nmembers = group_ptr[k];
-  gst_status st = ensure_workspace(g, k, nmembers);
+  // the group masks and member lists; the table is only the proposal's
+  // two-group distance solve's (a serving lane proposing beside a solve of
+  // k groups holds no k-group table)
+  gst_status st = ensure_workspace(g, 2, nmembers);
   if (st != GST_OK) return st;
   cudaStream_t s = g->stream;
   GST_CUDA(cudaMemcpyAsync(ws.d_group_ptr, group_ptr, (size_t)(k + 1) * 4, cudaMemcpyHostToDevice, s));
@@ -1153,7 +1197,7 @@ gst_status compute_features(gst_graph* g, int32_t k) {
 }
 
 // bf16 inference: scores into lw.scores.
-gst_status infer_scores(gst_graph* g, const gst_scorer* sc) {
+gst_status infer_scores(gst_graph* g, const gst_scorer* sc, const std::function<bool()>* stop = nullptr) {
   LearnWs& lw = g->lw;
   const GraphDev gd = graph_dev(g);
   cudaStream_t s = g->stream;
@@ -1168,10 +1212,15 @@ gst_status infer_scores(gst_graph* g, const gst_scorer* sc) {
     GST_CUDA(launch_infer_layer(gd, g->d_hub_of, lw.hub_sum, hin, lw.hb_map[(l - 1) & 1], lw.hb[2], lw.hb_map[2],
                                 sc->wcat + (size_t)(l - 1) * kHid * 2 * kHid, sc->params, l,
                                 last ? nullptr : lw.hb[l & 1], last ? lw.scores : nullptr, lw.infer_err, s));
+    if (stop && !last) {  // beside a solve: give up between layers once it finished
+      const gst_status st = wait_or_stop(g, stop);
+      if (st != GST_OK) return st;
+    }
   }
   int32_t err = 0;
   GST_CUDA(cudaMemcpyAsync(&err, lw.infer_err, sizeof(err), cudaMemcpyDeviceToHost, s));
-  GST_CUDA(cudaStreamSynchronize(s));
+  const gst_status wst = wait_or_stop(g, stop);
+  if (wst != GST_OK) return wst;
   if (err) {
     GST_CUDA(cudaMemsetAsync(lw.infer_err, 0, sizeof(int32_t), s));
     return fail(GST_INTERNAL, err == 1 ? "scorer layer: a TMA load did not complete" : "scorer layer: an MMA did not complete");
@@ -1222,9 +1271,11 @@ gst_status train_backward(gst_graph* g, const gst_scorer* sc, int32_t n) {
 }
 
 // A feasible tree of the query rooted at the top-scored vertex (or the
-// fixed feature score with sc NULL), written into r (caller IDs).
+// fixed feature score with sc NULL), written into r (caller IDs). With
+// stop, every wait gives up (GST_TIMEOUT) once (*stop)() holds: the
+// proposal is no longer needed, and its queued work still runs.
 gst_status propose_tree(gst_graph* g, const gst_scorer* sc, const int32_t* group_ptr, const int32_t* members,
-                        int32_t k, const gst_opts& o, gst_result* r) {
+                        int32_t k, const gst_opts& o, gst_result* r, const std::function<bool()>* stop = nullptr) {
   LearnWs& lw = g->lw;
   Workspace& ws = g->ws;
   cudaStream_t s = g->stream;
@@ -1248,7 +1299,7 @@ gst_status propose_tree(gst_graph* g, const gst_scorer* sc, const int32_t* group
   phase("features");
   int64_t launches = 5;  // group masks, three reach passes, features
   if (sc) {
-    st = infer_scores(g, sc);
+    st = infer_scores(g, sc, stop);
     if (st != GST_OK) return st;
     launches += 1 + kMpLayers * (g->nbig > 0 ? 3 : 2);
   } else {
@@ -1265,7 +1316,8 @@ gst_status propose_tree(gst_graph* g, const gst_scorer* sc, const int32_t* group
   std::vector<uint32_t> hist(kScoreBins);
   GST_CUDA(cudaMemcpyAsync(&best, lw.best, sizeof(best), cudaMemcpyDeviceToHost, s));
   GST_CUDA(cudaMemcpyAsync(hist.data(), lw.hist, kScoreBins * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-  GST_CUDA(cudaStreamSynchronize(s));
+  st = wait_or_stop(g, stop);
+  if (st != GST_OK) return st;
   if (best == 0) return fail(GST_INTERNAL, "no vertex scored");
   const int32_t root = (int32_t)(0xffffffffull - (best & 0xffffffffull));
   // the kProposeTop top-scored vertices: the lowest histogram bin that
@@ -1279,10 +1331,15 @@ gst_status propose_tree(gst_graph* g, const gst_scorer* sc, const int32_t* group
   GST_CUDA(launch_score_select(g->V, lw.scores, bin_lo, lw.top, lw.pn + 3, lw.top_cap, s));
   int32_t ntop = 0;
   GST_CUDA(cudaMemcpyAsync(&ntop, lw.pn + 3, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
-  GST_CUDA(cudaStreamSynchronize(s));
+  st = wait_or_stop(g, stop);
+  if (st != GST_OK) return st;
   ntop = std::min(ntop, lw.top_cap);
   std::vector<uint2> cand((size_t)ntop);
-  if (ntop) GST_CUDA(cudaMemcpy(cand.data(), lw.top, cand.size() * sizeof(uint2), cudaMemcpyDeviceToHost));
+  if (ntop) {
+    GST_CUDA(cudaMemcpyAsync(cand.data(), lw.top, cand.size() * sizeof(uint2), cudaMemcpyDeviceToHost, s));
+    st = wait_or_stop(g, stop);
+    if (st != GST_OK) return st;
+  }
   std::sort(cand.begin(), cand.end(), [](const uint2& a, const uint2& b) { return a.x != b.x ? a.x > b.x : a.y < b.y; });
   std::vector<int32_t> top;
   for (size_t i = 0; i < cand.size() && (int)i < kProposeTop; ++i) top.push_back((int32_t)cand[i].y);
@@ -1301,7 +1358,8 @@ gst_status propose_tree(gst_graph* g, const gst_scorer* sc, const int32_t* group
   o1.refine_bound = 0;
   o1.max_rounds = kProposeRounds;
   gst_result tmp;
-  st = solve_one(g, gp1, mem1, 2, o1, &tmp);
+  st = solve_one(g, gp1, mem1, 2, o1, &tmp, nullptr, stop);
+  if (st == GST_TIMEOUT && stop && (*stop)()) return st;  // stopped, not out of rounds
   if (st == GST_TIMEOUT) {  // the capped rounds ran out: the distances so far are actual paths
     st = GST_OK;
     g_last_error.clear();
@@ -1319,11 +1377,15 @@ gst_status propose_tree(gst_graph* g, const gst_scorer* sc, const int32_t* group
                            g->d_perm, k, lw.pe, lw.pn, lw.pe_cap, s));
   int32_t pn[4];
   GST_CUDA(cudaMemcpyAsync(pn, lw.pn, sizeof(pn), cudaMemcpyDeviceToHost, s));
-  GST_CUDA(cudaStreamSynchronize(s));
+  st = wait_or_stop(g, stop);
+  if (st != GST_OK) return st;
   if (pn[2]) return fail(GST_INFEASIBLE, "a group cannot reach the proposal's root");
   if (pn[1] || pn[0] > lw.pe_cap) return fail(GST_INTERNAL, "proposal path walk failed");
   std::vector<int3> pe((size_t)pn[0]);
-  if (pn[0]) GST_CUDA(cudaMemcpy(pe.data(), lw.pe, pe.size() * sizeof(int3), cudaMemcpyDeviceToHost));
+  if (pn[0]) {
+    GST_CUDA(cudaMemcpyAsync(pe.data(), lw.pe, pe.size() * sizeof(int3), cudaMemcpyDeviceToHost, s));
+    GST_CUDA(cudaStreamSynchronize(s));
+  }
   phase("paths");
 
   // union of the paths (a subtree of the shortest-path tree)
@@ -1792,6 +1854,8 @@ void gst_graph_free(gst_graph* g) {
   }
   if (g->stream) cudaStreamDestroy(g->stream);
   if (g->side) cudaStreamDestroy(g->side);
+  for (cudaEvent_t e : {g->ev_params, g->ev_done, g->ev_side, g->ev_poll})
+    if (e) cudaEventDestroy(e);
   if (prev >= 0) cudaSetDevice(prev);
   delete g;
 }
@@ -2359,43 +2423,108 @@ gst_status gst_solve_learned(gst_graph* g, gst_scorer* sc, const int32_t* group_
     return GST_INFEASIBLE;
   }
   gst_opts o = resolve_opts(opts);
-  std::lock_guard<std::mutex> lock(g->mu);
+  o.refine_bound = 1;
+  // A captured solve runs the proposal on a serving lane while its graph
+  // runs: the proposal's cost reaches the running DP as a bound through
+  // launch_bound_min, and a proposal that the DP outran is given up at its
+  // next wait. The host loop proposes first and solves under it.
+  const bool overlap = o.use_graph != 0 && g->parent == nullptr;
+  if (overlap) {
+    st = ensure_lanes(g, 1);
+    if (st != GST_OK) return st;
+  }
+  gst_graph* lane = overlap ? g->lanes[0] : nullptr;
+  std::unique_lock<std::mutex> lock(g->mu);
+  std::unique_lock<std::mutex> lane_lock;
+  if (lane) lane_lock = std::unique_lock<std::mutex>(lane->mu);
   DeviceGuard dg(g->device);
   cudaGetLastError();
   const auto t0 = std::chrono::steady_clock::now();
   gst_result prop;
-  const gst_status pst = propose_tree(g, sc, group_ptr, members, k, o, &prop);
-  const double pms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-  o.refine_bound = 1;
-  if (pst == GST_OK && prop.cost > 0) {
-    o.upper_bound = prop.cost;
-    st = solve_one(g, group_ptr, members, k, o, r);
-    if (st == GST_OK) {
-      r->status = GST_OK;
-      r->proposal_cost = prop.cost;
-      r->propose_ms = pms;
-      r->launches += prop.launches;
-      return GST_OK;
-    }
-    if (st != GST_INFEASIBLE) {
+  gst_status pst = GST_INTERNAL;
+  double pms = 0;
+  if (overlap) {
+    for (cudaEvent_t* e : {&g->ev_params, &g->ev_done, &g->ev_side})
+      if (!*e) GST_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    bool finished = false;  // the DP's graph has completed (latched)
+    const std::function<bool()> stop = [&]() {
+      return finished = finished || cudaEventQuery(g->ev_done) == cudaSuccess;
+    };
+    bool bounded = false;
+    const std::function<void()> propose = [&]() {
+      pst = propose_tree(lane, sc, group_ptr, members, k, o, &prop, &stop);
+      if (pst == GST_OK && prop.cost > 0 && !stop()) {
+        // after the solve's parameters are on the device, so that their
+        // upload does not overwrite the bound
+        if (cudaStreamWaitEvent(lane->stream, g->ev_params, 0) != cudaSuccess ||
+            launch_bound_min(g->ws.d_params, prop.cost, lane->stream) != cudaSuccess)
+          pst = GST_INTERNAL;
+        else
+          bounded = true;
+      }
+      // the solve ends after the lane's queued work: the bound lands before
+      // the next solve uploads its parameters, and a given-up proposal's
+      // kernels finish before the lane is used again
+      if (cudaEventRecord(g->ev_side, lane->stream) != cudaSuccess ||
+          cudaStreamWaitEvent(g->stream, g->ev_side, 0) != cudaSuccess)
+        pst = GST_INTERNAL;
+      pms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    };
+    st = solve_one(g, group_ptr, members, k, o, r, &propose);
+    r->propose_ms = pms;
+    r->proposal_concurrent = 1;
+    if (bounded) r->proposal_cost = prop.cost;
+    r->launches += prop.launches + (bounded ? 1 : 0);  // + the bound's
+    // the bound the solve ended with: the proposal's may have landed after
+    // the last wave copied the parameters back
+    if (bounded && (r->ub <= 0 || prop.cost < r->ub)) r->ub = prop.cost;
+    if (st != GST_INFEASIBLE || !bounded) {
+      // a failed proposal only forgoes its bound: the DP decided alone
+      if (st == GST_OK || st == GST_INFEASIBLE) g_last_error.clear();
       r->status = st;
+      r->wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
       return st;
+    }
+    // an infeasible verdict under a proposal's bound: decided again unpruned
+    // (a feasible proposal makes it impossible; kept as a guard)
+  } else {
+    pst = propose_tree(g, sc, group_ptr, members, k, o, &prop);
+    pms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    if (pst == GST_OK && prop.cost > 0) {
+      o.upper_bound = prop.cost;
+      st = solve_one(g, group_ptr, members, k, o, r);
+      if (st == GST_OK) {
+        r->status = GST_OK;
+        r->proposal_cost = prop.cost;
+        r->propose_ms = pms;
+        r->launches += prop.launches;
+        r->wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        return GST_OK;
+      }
+      if (st != GST_INFEASIBLE) {
+        r->status = st;
+        return st;
+      }
     }
   }
   // no usable proposal (or a zero-cost one): the unpruned DP decides
   g_last_error.clear();
+  const int64_t plaunches = prop.launches;
   *r = gst_result{};
   o.upper_bound = 0;
   st = solve_one(g, group_ptr, members, k, o, r);
   r->status = st;
   r->propose_ms = pms;
-  r->launches += prop.launches;
+  r->launches += plaunches;
+  r->wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   return st;
 }
 
 int32_t gst_result_upper_bound(const gst_result* r) { return r ? r->ub : 0; }
 int32_t gst_result_proposal_cost(const gst_result* r) { return r ? r->proposal_cost : 0; }
 double gst_result_proposal_ms(const gst_result* r) { return r ? r->propose_ms : 0.0; }
+int32_t gst_result_proposal_concurrent(const gst_result* r) { return r ? r->proposal_concurrent : 0; }
+double gst_result_wall_ms(const gst_result* r) { return r ? r->wall_ms : 0.0; }
 
 const char* gst_last_error(void) { return g_last_error.c_str(); }
 const char* gst_version(void) { return "gst-gb300 0.2 (sm_103a)"; }

@@ -130,6 +130,8 @@ SIGNATURES = {
     "gst_result_upper_bound": (C.c_int32, [C.c_void_p]),
     "gst_result_proposal_cost": (C.c_int32, [C.c_void_p]),
     "gst_result_proposal_ms": (C.c_double, [C.c_void_p]),
+    "gst_result_proposal_concurrent": (C.c_int32, [C.c_void_p]),
+    "gst_result_wall_ms": (C.c_double, [C.c_void_p]),
     "gst_last_error": (C.c_char_p, []),
     "gst_version": (C.c_char_p, []),
     # generators (include/gst_gen.h)
@@ -212,6 +214,9 @@ class Result:
     upper_bound: int = 0  # pruning bound at the last wave (0: unpruned)
     proposal_cost: int = 0  # learned path: cost of the proposed tree (0: none)
     proposal_ms: float = 0.0
+    # learned path: the proposal ran beside the DP (times_ms[0] spans both)
+    proposal_concurrent: bool = False
+    wall_ms: float = 0.0  # learned path: host wall time of the call
 
     @property
     def feasible(self) -> bool:
@@ -253,6 +258,8 @@ def _read_result(r) -> Result:
         upper_bound=int(L.gst_result_upper_bound(r)),
         proposal_cost=int(L.gst_result_proposal_cost(r)),
         proposal_ms=float(L.gst_result_proposal_ms(r)),
+        proposal_concurrent=bool(L.gst_result_proposal_concurrent(r)),
+        wall_ms=float(L.gst_result_wall_ms(r)),
     )
 
 

@@ -66,18 +66,28 @@ gst_status gst_scorer_train_step(gst_graph* g, gst_scorer* s, const int32_t* gro
 gst_status gst_propose(gst_graph* g, gst_scorer* s, const int32_t* group_ptr, const int32_t* members, int32_t k,
                        gst_result** out);
 
-/* Proposal, then the exact DP pruned by the proposal's cost (opts as for
- * gst_solve; its upper_bound is replaced by the proposal's cost). With s
- * NULL the fixed feature score roots the proposal. */
+/* The exact DP pruned by the proposal's cost (opts as for gst_solve; its
+ * upper_bound is replaced by the proposal's cost). With s NULL the fixed
+ * feature score roots the proposal. With opts->use_graph the proposal runs
+ * on a serving lane of g while the captured DP runs, and its cost reaches
+ * the running DP as a bound (waves that started without it prune from the
+ * next round on); the host loop proposes first and then solves. */
 gst_status gst_solve_learned(gst_graph* g, gst_scorer* s, const int32_t* group_ptr, const int32_t* members, int32_t k,
                              const gst_opts* opts, gst_result** out);
 
 /* Pruning bound as the last DP wave saw it (after the refinements of
- * gst_opts.refine_bound; 0 = the solve ran unpruned), the cost of the
- * learned path's proposed tree (0 = no proposal, the fallback ran) and the
- * host wall time of the proposal in ms. gst_solve_learned always refines. */
+ * gst_opts.refine_bound; 0 = the solve ran unpruned; a concurrent
+ * proposal's cost when lower), the cost of the learned path's proposed
+ * tree (0 = no proposal, the fallback ran) and the host wall time of the
+ * proposal in ms. gst_solve_learned always refines. */
 int32_t gst_result_upper_bound(const gst_result* r);
 int32_t gst_result_proposal_cost(const gst_result* r);
+/* 1 when the proposal ran beside the DP (gst_solve_learned with use_graph):
+ * then times[0] spans both (the solve's stream records its end after the
+ * proposal returned), else times[0] is the DP's alone. */
+int32_t gst_result_proposal_concurrent(const gst_result* r);
+/* gst_solve_learned: host wall time of the whole call in ms. */
+double gst_result_wall_ms(const gst_result* r);
 double gst_result_proposal_ms(const gst_result* r);
 
 #ifdef __cplusplus

@@ -121,16 +121,25 @@ def test_proposal_is_feasible_and_learned_solve_exact(use_scorer):
             err = oracle.check_tree(g.row_ptr, g.col, g.w, gp, mem, prop.vertices, prop.edges, prop.cost)
             assert err is None, err
             assert prop.cost >= plain.cost
-            res = dg.solve_learned(s, gp, mem)
-            assert res.status == N.Status.OK
-            assert res.cost == plain.cost
+            # host driver: the proposal first, then the DP under its bound
+            seq = dg.solve_learned(s, gp, mem, use_graph=False)
+            assert seq.status == N.Status.OK and seq.cost == plain.cost and not seq.proposal_concurrent
             # a proposal's root distances stop after a fixed number of rounds, so two proposals of
             # one query may differ (in-place updates run in no fixed order); each is a feasible tree
-            assert res.proposal_cost >= plain.cost
+            assert seq.proposal_cost >= plain.cost
             # the refined bound: a feasible cost, or 0 (= no bound) once a zero-cost tree is seen
-            assert res.upper_bound <= res.proposal_cost and (res.upper_bound >= plain.cost or plain.cost == 0)
-            err = oracle.check_tree(g.row_ptr, g.col, g.w, gp, mem, res.vertices, res.edges, res.cost)
-            assert err is None, err
+            assert seq.upper_bound <= seq.proposal_cost and (seq.upper_bound >= plain.cost or plain.cost == 0)
+            # captured: the proposal runs beside the DP; its bound lands unless the DP finished first
+            res = dg.solve_learned(s, gp, mem)
+            assert res.status == N.Status.OK and res.cost == plain.cost and res.proposal_concurrent
+            assert res.wall_ms > 0 and res.times_ms[0] > 0
+            assert res.proposal_cost == 0 or res.proposal_cost >= plain.cost
+            if res.proposal_cost:
+                assert res.upper_bound <= res.proposal_cost
+            assert res.upper_bound >= plain.cost or res.upper_bound == 0
+            for r in (seq, res):
+                err = oracle.check_tree(g.row_ptr, g.col, g.w, gp, mem, r.vertices, r.edges, r.cost)
+                assert err is None, err
 
 
 def test_trained_network_gains_over_the_method_without_it():
@@ -150,7 +159,8 @@ def test_trained_network_gains_over_the_method_without_it():
             gp, mem = N.gen_groups_zipf_degree(g, k, 1.2, 5, 500, 90_000 + q)
             opt = dg.solve(gp, mem, use_graph=True).cost
             for name, sc in (("trained", tr), ("none", None), ("untrained", un)):
-                res = dg.solve_learned(sc, gp, mem)
+                # the host driver proposes before it solves: every proposal is complete
+                res = dg.solve_learned(sc, gp, mem, use_graph=False)
                 assert res.cost == opt
                 assert res.proposal_cost >= opt
                 ratios[name].append(res.proposal_cost / opt)
