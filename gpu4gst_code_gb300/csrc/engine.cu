@@ -146,6 +146,9 @@ struct Workspace {
   int32_t* h_out_v = nullptr;
   int3* h_out_e = nullptr;
   cudaEvent_t ev[kEvents] = {};
+  // recorded by every query graph once wave 1 has grown (an external event
+  // node): a proposal running beside the solve reads wave 1 after it
+  cudaEvent_t ev_wave1 = nullptr;
   std::vector<int32_t> h_lvl_base, h_lvl_m, h_lvl_stride;
   QueryGraph qg[GST_MAX_K + 1];
 };
@@ -362,6 +365,8 @@ void free_workspace(Workspace& ws) {
       cudaEventDestroy(e);
       e = nullptr;
     }
+  if (ws.ev_wave1) cudaEventDestroy(ws.ev_wave1);
+  ws.ev_wave1 = nullptr;
   ws.k_cap = 0;
   ws.tables_k = 0;
   ws.members_cap = 0;
@@ -401,6 +406,7 @@ gst_status ensure_workspace(gst_graph* g, int32_t k, int64_t nmembers) {
     GST_CUDA(cudaMallocHost(&ws.h_out_v, kTreePrefix * sizeof(int32_t)));
     GST_CUDA(cudaMallocHost(&ws.h_out_e, kTreePrefix * sizeof(int3)));
     for (auto& e : ws.ev) GST_CUDA(cudaEventCreate(&e));
+    GST_CUDA(cudaEventCreateWithFlags(&ws.ev_wave1, cudaEventDisableTiming));
     // backtrack capacity: states of one optimal derivation
     ws.bt_cap = (int32_t)std::min<int64_t>(4 * V + 256, 1 << 24);
     GST_CUDA(cudaMalloc(&ws.qa, (size_t)ws.bt_cap * sizeof(int2)));
@@ -674,6 +680,8 @@ gst_status build_query_graph(gst_graph* g, int32_t k) {
     if (st == GST_OK && l < k - 1 && launch_ub_refine(graph_dev(g), a, g->num_sms, s) != cudaSuccess)
       st = fail(GST_CUDA_ERROR, "bound refinement launch");
     if (st == GST_OK && cudaEventRecord(ws.ev[3 * l + 2], s) != cudaSuccess)
+      st = fail(GST_CUDA_ERROR, "event record");
+    if (st == GST_OK && l == 1 && cudaEventRecordWithFlags(ws.ev_wave1, s, cudaEventRecordExternal) != cudaSuccess)
       st = fail(GST_CUDA_ERROR, "event record");
   }
   if (st == GST_OK && cudaEventRecord(ws.ev[1], s) != cudaSuccess) st = fail(GST_CUDA_ERROR, "event record");
@@ -1273,9 +1281,13 @@ gst_status train_backward(gst_graph* g, const gst_scorer* sc, int32_t n) {
 // A feasible tree of the query rooted at the top-scored vertex (or the
 // fixed feature score with sc NULL), written into r (caller IDs). With
 // stop, every wait gives up (GST_TIMEOUT) once (*stop)() holds: the
-// proposal is no longer needed, and its queued work still runs.
+// proposal is no longer needed, and its queued work still runs. With dp,
+// the captured solve of the same query running on dp's stream, the paths
+// to the groups come from that solve's wave 1 (after its ev_wave1) instead
+// of a two-group solve of the proposal's own.
 gst_status propose_tree(gst_graph* g, const gst_scorer* sc, const int32_t* group_ptr, const int32_t* members,
-                        int32_t k, const gst_opts& o, gst_result* r, const std::function<bool()>* stop = nullptr) {
+                        int32_t k, const gst_opts& o, gst_result* r, const std::function<bool()>* stop = nullptr,
+                        const gst_graph* dp = nullptr) {
   LearnWs& lw = g->lw;
   Workspace& ws = g->ws;
   cudaStream_t s = g->stream;
@@ -1344,37 +1356,47 @@ gst_status propose_tree(gst_graph* g, const gst_scorer* sc, const int32_t* group
   std::vector<int32_t> top;
   for (size_t i = 0; i < cand.size() && (int)i < kProposeTop; ++i) top.push_back((int32_t)cand[i].y);
   phase("top");
-  // distances to the root: a two-group solve whose groups are both {root}
-  // grows wave 1 to the full shortest-path fixpoint from the root (a
-  // one-group solve would stop after its only, last, wave's merge); the
-  // row of wave 1 has stride 4 either way
-  const int32_t gp1[3] = {0, 1, 2};
-  const int32_t mem1[2] = {g->inv[(size_t)root], g->inv[(size_t)root]};
-  // The growth is capped at kProposeRounds rounds: every finite distance
-  // is the length of an actual path even before the fixpoint, so the tree
-  // stays feasible; a group still out of reach drops the proposal.
-  gst_opts o1 = o;
-  o1.upper_bound = 0;
-  o1.refine_bound = 0;
-  o1.max_rounds = kProposeRounds;
-  gst_result tmp;
-  st = solve_one(g, gp1, mem1, 2, o1, &tmp, nullptr, stop);
-  if (st == GST_TIMEOUT && stop && (*stop)()) return st;  // stopped, not out of rounds
-  if (st == GST_TIMEOUT) {  // the capped rounds ran out: the distances so far are actual paths
-    st = GST_OK;
-    g_last_error.clear();
+  if (dp) {
+    // the root's paths over the running solve's wave 1: exact distances
+    // from every vertex to every group, grown before its later waves
+    GST_CUDA(cudaStreamWaitEvent(s, dp->ws.ev_wave1, 0));
+    GST_CUDA(cudaMemsetAsync(lw.pn, 0, 4 * sizeof(int32_t), s));
+    GST_CUDA(launch_root_paths(graph_dev(g), dp->ws.cost, dp->ws.par, dp->ws.h_lvl_stride[1], ws.gmask, root, k,
+                               lw.pe, lw.pn, lw.pe_cap, s));
+    launches += 1;
+  } else {
+    // distances to the root: a two-group solve whose groups are both {root}
+    // grows wave 1 to the full shortest-path fixpoint from the root (a
+    // one-group solve would stop after its only, last, wave's merge); the
+    // row of wave 1 has stride 4 either way
+    const int32_t gp1[3] = {0, 1, 2};
+    const int32_t mem1[2] = {g->inv[(size_t)root], g->inv[(size_t)root]};
+    // The growth is capped at kProposeRounds rounds: every finite distance
+    // is the length of an actual path even before the fixpoint, so the tree
+    // stays feasible; a group still out of reach drops the proposal.
+    gst_opts o1 = o;
+    o1.upper_bound = 0;
+    o1.refine_bound = 0;
+    o1.max_rounds = kProposeRounds;
+    gst_result tmp;
+    st = solve_one(g, gp1, mem1, 2, o1, &tmp, nullptr, stop);
+    if (st == GST_TIMEOUT && stop && (*stop)()) return st;  // stopped, not out of rounds
+    if (st == GST_TIMEOUT) {  // the capped rounds ran out: the distances so far are actual paths
+      st = GST_OK;
+      g_last_error.clear();
+    }
+    if (st != GST_OK) return st;
+    launches += tmp.launches + 1;  // + the path walk
+    phase("root distances");
+    // nearest member of every group and its path to the root
+    const int64_t nmembers = group_ptr[k];
+    GST_CUDA(cudaMemcpyAsync(ws.d_group_ptr, group_ptr, (size_t)(k + 1) * 4, cudaMemcpyHostToDevice, s));
+    if (nmembers)
+      GST_CUDA(cudaMemcpyAsync(ws.d_members, members, (size_t)nmembers * 4, cudaMemcpyHostToDevice, s));
+    GST_CUDA(cudaMemsetAsync(lw.pn, 0, 4 * sizeof(int32_t), s));
+    GST_CUDA(launch_ub_paths(graph_dev(g), ws.cost, ws.par, ws.h_lvl_stride[1], ws.d_group_ptr, ws.d_members,
+                             g->d_perm, k, lw.pe, lw.pn, lw.pe_cap, s));
   }
-  if (st != GST_OK) return st;
-  launches += tmp.launches + 1;  // + the path walk
-  phase("root distances");
-  // nearest member of every group and its path to the root
-  const int64_t nmembers = group_ptr[k];
-  GST_CUDA(cudaMemcpyAsync(ws.d_group_ptr, group_ptr, (size_t)(k + 1) * 4, cudaMemcpyHostToDevice, s));
-  if (nmembers)
-    GST_CUDA(cudaMemcpyAsync(ws.d_members, members, (size_t)nmembers * 4, cudaMemcpyHostToDevice, s));
-  GST_CUDA(cudaMemsetAsync(lw.pn, 0, 4 * sizeof(int32_t), s));
-  GST_CUDA(launch_ub_paths(graph_dev(g), ws.cost, ws.par, ws.h_lvl_stride[1], ws.d_group_ptr, ws.d_members,
-                           g->d_perm, k, lw.pe, lw.pn, lw.pe_cap, s));
   int32_t pn[4];
   GST_CUDA(cudaMemcpyAsync(pn, lw.pn, sizeof(pn), cudaMemcpyDeviceToHost, s));
   st = wait_or_stop(g, stop);
@@ -2424,10 +2446,12 @@ gst_status gst_solve_learned(gst_graph* g, gst_scorer* sc, const int32_t* group_
   }
   gst_opts o = resolve_opts(opts);
   o.refine_bound = 1;
+  o.upper_bound = 0;  // the proposal's cost is the bound
   // A captured solve runs the proposal on a serving lane while its graph
-  // runs: the proposal's cost reaches the running DP as a bound through
-  // launch_bound_min, and a proposal that the DP outran is given up at its
-  // next wait. The host loop proposes first and solves under it.
+  // runs: the proposal takes its paths from the solve's own wave 1, its
+  // cost reaches the running DP as a bound through launch_bound_min, and a
+  // proposal that the DP outran is given up at its next wait. The host loop
+  // proposes first (paths from a two-group solve) and solves under it.
   const bool overlap = o.use_graph != 0 && g->parent == nullptr;
   if (overlap) {
     st = ensure_lanes(g, 1);
@@ -2452,7 +2476,7 @@ gst_status gst_solve_learned(gst_graph* g, gst_scorer* sc, const int32_t* group_
     };
     bool bounded = false;
     const std::function<void()> propose = [&]() {
-      pst = propose_tree(lane, sc, group_ptr, members, k, o, &prop, &stop);
+      pst = propose_tree(lane, sc, group_ptr, members, k, o, &prop, &stop, g);
       if (pst == GST_OK && prop.cost > 0 && !stop()) {
         // after the solve's parameters are on the device, so that their
         // upload does not overwrite the bound

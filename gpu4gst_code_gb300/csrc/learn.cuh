@@ -129,6 +129,14 @@ cudaError_t launch_ub_paths(const GraphDev& g, const int32_t* dist, const int32_
                             const int32_t* group_ptr, const int32_t* members, const int32_t* perm, int32_t k,
                             int3* out_e, int32_t* out_n, int32_t cap, cudaStream_t s);
 
+// The root's paths to the nearest member of every group over a solve's own
+// wave 1 (cost / par: the table, level 1 at its start with row stride
+// stride1; gmask: the query's group masks, internal IDs). Counters as for
+// launch_ub_paths; a walk that meets an inconsistent record stops.
+cudaError_t launch_root_paths(const GraphDev& g, const int32_t* cost, const int32_t* par, int32_t stride1,
+                              const uint32_t* gmask, int32_t root, int32_t k, int3* out_e, int32_t* out_n, int32_t cap,
+                              cudaStream_t s);
+
 // Adam step over the flat parameter vector (bias-corrected, step t >= 1).
 cudaError_t launch_adam(int64_t n, float* p, const float* g, float* m, float* v, float lr, int32_t t, cudaStream_t s);
 

@@ -780,6 +780,43 @@ __global__ void __launch_bounds__(256) k_ub_paths(GraphDev g, const int32_t* __r
   atomicExch(out_n + 1, 1);
 }
 
+// The proposal's paths over a solve's own wave 1, whose entry (v, {g}) is
+// the distance from v to group g with its growth record: one thread per
+// group walks from (root, {g}) along the records to a leaf, emitting
+// (v, next, w) edges. Every step must be a growth record of its row whose
+// cost is the next state's plus the edge weight, and the leaf a member of
+// g; anything else stops the walk (out_n[1]), so whatever the table's
+// state, the emitted paths are real paths of the graph.
+__global__ void k_root_paths(GraphDev g, const int32_t* __restrict__ cost, const int32_t* __restrict__ par,
+                             int32_t stride1, const uint32_t* __restrict__ gmask, int32_t root, int32_t k,
+                             int3* __restrict__ out_e, int32_t* out_n, int32_t cap) {
+  const int gi = blockIdx.x * blockDim.x + threadIdx.x;
+  if (gi >= k) return;
+  int32_t v = root;
+  int32_t c = cost[(int64_t)v * stride1 + gi];
+  if (c >= kInf) {
+    atomicExch(out_n + 2, 1);
+    return;
+  }
+  for (int32_t step = 0; step <= g.V; ++step) {
+    const int32_t e = par[(int64_t)v * stride1 + gi];
+    if (e == kLeaf) {
+      if (c == 0 && ((gmask[v] >> gi) & 1u)) return;
+      break;
+    }
+    if (e < g.row_ptr[v] || e >= g.row_ptr[v + 1]) break;
+    const int2 x = g.adj[e];
+    const int32_t cn = cost[(int64_t)x.x * stride1 + gi];
+    if (cn != c - x.y || cn < 0) break;
+    const int32_t i = atomicAdd(out_n, 1);
+    if (i >= cap) break;
+    out_e[i] = make_int3(v, x.x, x.y);
+    v = x.x;
+    c = cn;
+  }
+  atomicExch(out_n + 1, 1);
+}
+
 }  // namespace
 
 // -------------------------------------------------------------- launchers --
@@ -952,6 +989,13 @@ cudaError_t launch_ub_paths(const GraphDev& g, const int32_t* dist, const int32_
                             const int32_t* group_ptr, const int32_t* members, const int32_t* perm, int32_t k,
                             int3* out_e, int32_t* out_n, int32_t cap, cudaStream_t s) {
   k_ub_paths<<<k, 256, 0, s>>>(g, dist, par, stride, group_ptr, members, perm, out_e, out_n, cap);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_root_paths(const GraphDev& g, const int32_t* cost, const int32_t* par, int32_t stride1,
+                              const uint32_t* gmask, int32_t root, int32_t k, int3* out_e, int32_t* out_n, int32_t cap,
+                              cudaStream_t s) {
+  k_root_paths<<<1, 32, 0, s>>>(g, cost, par, stride1, gmask, root, k, out_e, out_n, cap);
   return cudaGetLastError();
 }
 
