@@ -180,11 +180,12 @@ struct LevelArgs {
 constexpr int kTourMaxK = 10;
 constexpr int kTourSmemMaxK = 9;
 
-// Queries with at most kMergeTabK groups merge a vertex per thread from
-// per-level split tables (k_merge_vertex); larger k use k_merge.
+// Queries with at most kMergeTabK groups merge from per-level split tables
+// (k_merge_staged: a thread per vertex; k_merge_team: a team of lanes per
+// vertex for long lower-level rows); larger k use k_merge.
 constexpr int kMergeTabK = 10;
 
-// Where each level's rows live, for k_merge_vertex.
+// Where each level's rows live, for the split-table merges.
 struct MergeLevels {
   int64_t off[kMergeTabK + 1];     // base_l * V
   int32_t stride[kMergeTabK + 1];  // row stride of level l

@@ -98,58 +98,10 @@ __global__ void k_group_masks(const int32_t* __restrict__ group_ptr, const int32
   }
 }
 
-// One-label bound of vertex v, loaded once: dd[g] = min(T(v,{g}), ub/2+1)
-// for the k groups, 0 for absent groups (wave 1 is not written while waves
-// >= 2 grow). Rows of wave 1 are 16-byte aligned.
-__device__ __forceinline__ void load_label_bound(const LevelArgs& a, int32_t ub, int32_t v, int32_t (&dd)[16]) {
-  const int4* d4 = reinterpret_cast<const int4*>(a.cost + (int64_t)v * a.stride1);
-  const int32_t beyond = ub / 2 + 1;
-#pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    int4 t = make_int4(0, 0, 0, 0);
-    if (4 * q < a.k) t = __ldg(d4 + q);
-    dd[4 * q] = 4 * q < a.k ? min(t.x, beyond) : 0;
-    dd[4 * q + 1] = 4 * q + 1 < a.k ? min(t.y, beyond) : 0;
-    dd[4 * q + 2] = 4 * q + 2 < a.k ? min(t.z, beyond) : 0;
-    dd[4 * q + 3] = 4 * q + 3 < a.k ? min(t.w, beyond) : 0;
-  }
-}
-
-// max over groups outside S of dd (the bound on completing S to the full set)
-__device__ __forceinline__ int32_t label_bound(const int32_t (&dd)[16], uint32_t S) {
-  int32_t lb = 0;
-#pragma unroll
-  for (int gg = 0; gg < 16; ++gg) lb = max(lb, ((S >> gg) & 1u) ? 0 : dd[gg]);
-  return lb;
-}
-
 // Growth under a bound (waves >= 2): the cap of state (v, mask rank j) that
 // the wave's merge wrote (read-only during the wave).
 __device__ __forceinline__ int32_t cap_at(const LevelArgs& a, int32_t v, int j) {
   return __ldg(a.capt + (int64_t)v * a.stride + j);
-}
-
-// PrunedDP++'s tour bounds of (v, X) for the merges that do not stage rows
-// (k_merge_vertex): wave-1 distances read from global memory (d1 = v's wave-1
-// row), capped at beyond = ub/2 + 1; lb1 over unordered end pairs i < j of
-// the path table, lb2 over W2 (k_tour_table). Sums stay below 2^31
-// (unsigned): each is at most ub / 2 + 1 + ub + ub / 2 + 1.
-__device__ __forceinline__ int32_t tour_bound(const LevelArgs& a, const int32_t* d1, uint32_t beyond, uint32_t X) {
-  const int32_t* w2 = a.tour + ((int64_t)a.k << a.k) * a.k;
-  // halving is monotone: each bound halves its extreme sum once
-  uint32_t p1 = 0xffffffffu, p2 = 0u, dmin = 0xffffffffu;
-  for (uint32_t xi = X; xi; xi &= xi - 1u) {
-    const int i = __ffs(xi) - 1;
-    const uint32_t di = min((uint32_t)__ldg(d1 + i), beyond);
-    const int32_t* fi = a.tour + (((int64_t)i << a.k) | X) * a.k;
-    dmin = min(dmin, di);
-    p2 = max(p2, di + (uint32_t)__ldg(w2 + ((int64_t)i << a.k) + X));
-    for (uint32_t xj = xi & (xi - 1u); xj; xj &= xj - 1u) {
-      const int i2 = __ffs(xj) - 1;
-      p1 = min(p1, di + (uint32_t)__ldg(fi + i2) + min((uint32_t)__ldg(d1 + i2), beyond));
-    }
-  }
-  return (int32_t)max(p1 >> 1, (p2 + dmin) >> 1);
 }
 
 // PrunedDP++'s conditional tree merging (graph_v_of_v_idealID_PrunedDPPlusPlus.h:
@@ -244,20 +196,17 @@ __global__ void __launch_bounds__(kGrowThreads) k_merge(GraphDev g, LevelArgs a)
   }
 }
 
-// One thread per vertex (k <= kMergeTabK): the same states as k_merge, row
-// by row. The level's split table sits in shared memory, so a split costs
-// its two row loads; the vertex's group mask and one-label bound are
-// loaded once; the row is written 16 bytes at a time.
-// Queries with at most kMergeStagedWords words of lower-level row per
-// vertex (k <= 8): a thread copies its vertex's rows of levels 1..l-1 into
-// shared memory once (light-filtered there when the merge uses light
-// parts), a column per thread, and every split then reads two shared words
-// at offsets precomputed into the block's copy of the split table, instead
-// of computing two global row addresses from the split's levels. Blocks of
-// NT threads: 128 up to kMergeStagedWords128 words, 64 beyond (at most
-// 64 KB of columns either way).
-constexpr int kMergeStagedWords128 = 136;  // k <= 7
-constexpr int kMergeStagedWords = 256;     // k = 8
+// One thread per vertex (k <= kMergeTabK, at most kMergeStagedWords128
+// words of lower-level row per vertex): the same states as k_merge, row by
+// row. A thread copies its vertex's rows of levels 1..l-1 into shared
+// memory once (light-filtered there when the merge uses light parts), a
+// column per thread, and every split then reads two shared words at
+// offsets precomputed into the block's copy of the split table (the
+// level's split table, loaded once per block); the vertex's group mask is
+// loaded once and its row written 16 bytes at a time. Blocks of NT = 128
+// threads (at most 68 KB of columns). Longer rows: k_merge_team.
+constexpr int kMergeStagedWords128 = 136;  // waves 2-6 of k = 7, 2-4 of k = 8
+constexpr int kMergeStagedWords = 256;     // the longest rows of k = 8 (teams of 4 up to here)
 
 template <int NT>
 __global__ void __launch_bounds__(NT) k_merge_staged(GraphDev g, LevelArgs a, MergeLevels ml) {
@@ -422,74 +371,142 @@ __global__ void __launch_bounds__(NT) k_merge_staged(GraphDev g, LevelArgs a, Me
   }
 }
 
-__global__ void __launch_bounds__(kGrowThreads) k_merge_vertex(GraphDev g, LevelArgs a, MergeLevels ml) {
+// A team of T lanes per vertex, for the merges whose lower-level rows are
+// too long to stage a thread per vertex at a useful occupancy: more than
+// kMergeStagedWords128 words (k_merge_staged would run blocks of 64 threads,
+// 8-10 warps per SM: waves 5-8 of k = 8, wave 7 of k = 7, and k = 9, 10),
+// or more than kMergeTeamMinWords words in a level of at least
+// kMergeTeamMinMasks masks (wave 4 of k = 8). Waves 4-6 of k = 7 stay with
+// k_merge_staged, which was faster there (ba4m_k7 bounded 22.7 against
+// 23.3 ms with teams; ba2m_k8 bounded 35.3 -> 32.9 ms with wave 4 by teams).
+// The team copies its vertex's rows of levels 1..l-1 into its own slice of
+// shared memory (consecutive words by consecutive lanes, light-filtered as
+// in k_merge_staged), then evaluates the level's states. LANE_MASKS (a
+// level of at least T masks): lane t of the team takes masks t, t + T, ...
+// and scans each mask's splits alone. Otherwise the team takes the masks
+// one by one and its lanes share each mask's splits; a minimum over
+// (cost, split index) keeps the first cheapest split, as a sequential scan
+// does. Bounds, caps, the 2/3 rule and the written rows are those of
+// k_merge_staged. T = 4 up to 256 words (k <= 8: each lane keeps a
+// quarter of the states, so lanes stay busy on levels of 7 to 70 masks,
+// and a quarter of the staging per lane quadruples the blocks per SM),
+// 32 beyond. Persistent blocks of kMergeTeamThreads threads stride over
+// the vertices.
+constexpr int kMergeTeamMinWords = 64;
+constexpr int kMergeTeamMinMasks = 64;
+constexpr int kMergeTeamThreads = 256;
+
+template <int T, bool LANE_MASKS>
+__global__ void __launch_bounds__(kMergeTeamThreads) k_merge_team(GraphDev g, LevelArgs a, MergeLevels ml,
+                                                                  int32_t words) {
+  static_assert(T >= 1 && T <= 32 && (T & (T - 1)) == 0, "teams are powers of two within a warp");
+  constexpr int kTeams = kMergeTeamThreads / T;
   extern __shared__ int32_t msm[];
-  int32_t* sp = msm;                                                // m + 1
-  int2* ss = reinterpret_cast<int2*>(msm + ((a.m + 2) & ~1));      // nsplits (8-byte aligned)
+  __shared__ int32_t loff[kMergeTabK + 1];  // level l's first word in a vertex's staged rows
+  int32_t* sp = msm;                                             // m + 1
+  int2* ss = reinterpret_cast<int2*>(msm + ((a.m + 2) & ~1));   // nsplits: staged word offsets
+  uint32_t* rows = reinterpret_cast<uint32_t*>(ss + a.nsplits);  // kTeams x words
+  if (threadIdx.x == 0) {
+    int32_t o = 0;
+    for (int l = 1; l < a.level; ++l) {
+      loff[l] = o;
+      o += ml.stride[l];
+    }
+  }
   for (int i = threadIdx.x; i <= a.m; i += blockDim.x) sp[i] = a.msplit_ptr[i];
-  for (int i = threadIdx.x; i < a.nsplits; i += blockDim.x) ss[i] = a.msplits[i];
   __syncthreads();
-  const int32_t ub = (a.level >= 2) ? a.params->ub : 0;
-  const int32_t ub_light = a.params->ub;
+  for (int i = threadIdx.x; i < a.nsplits; i += blockDim.x) {
+    const int2 x = a.msplits[i];
+    ss[i] = make_int2(loff[x.x >> 24] + (x.x & 0xffffff), loff[x.y >> 24] + (x.y & 0xffffff));
+  }
+  __syncthreads();
+  const int32_t ub = a.params->ub;  // merges are waves >= 2
   const int32_t ovf_limit = a.params->ovf_limit;
   const int32_t keep23 = merged_keep(a, ub);
   const bool late = a.params->late_bound != 0;
   const bool light_parts = a.level < a.k;
   uint8_t* flag2 = a.flags + 2 * (int64_t)a.vpad;
   long long acc[3] = {0, 0, 0};  // finite states, splits, overflow
-  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < g.V; v += (int64_t)gridDim.x * blockDim.x) {
+  constexpr uint32_t kStagedInf = 0xC0000000u;  // as in k_merge_staged
+  const int team = threadIdx.x / T, lane = threadIdx.x % T;
+  const unsigned tmask = T == 32 ? 0xffffffffu : ((1u << T) - 1u) << ((threadIdx.x & 31) & ~(T - 1));
+  uint32_t* col = rows + (int64_t)team * words;
+  const uint32_t beyond = (uint32_t)(ub / 2 + 1);
+  const uint32_t full = (1u << a.k) - 1u;
+  // the cap of state S at the staged vertex: ub minus the one-label bound
+  // (wave 1's distances, words 0..k-1 of the staged rows) or, with the
+  // tour tables, the largest of the one-label and the two tour bounds;
+  // kInf without a bound
+  auto state_cap = [&](uint32_t S) -> int32_t {
+    if (ub <= 0) return kInf;
+    const uint32_t X = full ^ S;
+    uint32_t dmax = 0u;
+    if (!(a.tour && __popc(X) >= 2)) {
+      for (uint32_t xi = X; xi; xi &= xi - 1u) dmax = max(dmax, min(col[__ffs(xi) - 1], beyond));
+      return ub - (int32_t)dmax;
+    }
+    uint32_t p1 = 0xffffffffu, p2 = 0u, dmin = 0xffffffffu;
+    const int32_t* w2 = a.tour + ((int64_t)a.k << a.k) * a.k;
+    for (uint32_t xi = X; xi; xi &= xi - 1u) {
+      const int i = __ffs(xi) - 1;
+      const uint32_t di = min(col[i], beyond);
+      const int32_t* fi = a.tour + (((int64_t)i << a.k) | X) * a.k;
+      dmin = min(dmin, di);
+      dmax = max(dmax, di);
+      p2 = max(p2, di + (uint32_t)__ldg(w2 + ((int64_t)i << a.k) + X));
+      for (uint32_t xj = xi & (xi - 1u); xj; xj &= xj - 1u) {
+        const int i2 = __ffs(xj) - 1;
+        p1 = min(p1, di + (uint32_t)__ldg(fi + i2) + min(col[i2], beyond));
+      }
+    }
+    return ub - (int32_t)max(dmax, max(p1 >> 1, (p2 + dmin) >> 1));
+  };
+  for (int64_t v = (int64_t)blockIdx.x * kTeams + team; v < g.V; v += (int64_t)gridDim.x * kTeams) {
+    for (int l = 1; l < a.level; ++l) {
+      const int32_t* src = a.cost + ml.off[l] + v * ml.stride[l];
+      uint32_t* dst = col + loff[l];
+      for (int w = lane; w < ml.stride[l]; w += T) {
+        const int32_t c = src[w];
+        dst[w] = (light_parts ? light_or_inf(c, ub) : c) >= kInf ? kStagedInf : (uint32_t)c;
+      }
+    }
+    __syncwarp(tmask);
     const uint32_t gm = __ldg(a.gmask + v);
-    int32_t dd[16];
-    if (ub > 0) load_label_bound(a, ub, (int32_t)v, dd);
-    const int32_t* d1 = a.cost + v * a.stride1;  // wave 1 (rank of {g} is g), for the tour bound
-    const uint32_t beyond = (uint32_t)(ub / 2 + 1);
-    const uint32_t full = (1u << a.k) - 1u;
-    int4* rowc = reinterpret_cast<int4*>(a.cost + a.base + v * a.stride);
-    int4* rowp = reinterpret_cast<int4*>(a.par + a.base + v * a.stride);
-    int4* rowk = reinterpret_cast<int4*>(a.capt + v * a.stride);
+    int32_t* rowc = a.cost + a.base + v * a.stride;
+    int32_t* rowp = a.par + a.base + v * a.stride;
+    int32_t* rowk = a.capt + v * a.stride;
     bool any = false;
-    for (int j0 = 0; j0 < a.stride; j0 += 4) {
-      int32_t b4[4], c4[4], k4[4];
-#pragma unroll
-      for (int t = 0; t < 4; ++t) {
-        const int j = j0 + t;
-        int32_t best = kInf, code = kLeaf;
-        k4[t] = -1;  // padding slots: nothing fits
+    if constexpr (LANE_MASKS) {
+      for (int j = lane; j < a.stride; j += T) {
+        int32_t best = kInf, code = kLeaf, capv = -1;  // padding slots: nothing fits
         if (j < a.m) {
           const uint32_t S = (uint32_t)__ldg(a.lmasks + j);
           if ((gm & S) == S) best = 0;
-          int32_t lb = ub > 0 ? label_bound(dd, S) : 0;
-          const uint32_t X = full ^ S;
-          if (ub > 0 && a.tour && __popc(X) >= 2) lb = max(lb, tour_bound(a, d1, beyond, X));
-          const int32_t cap = ub > 0 ? ub - lb : kInf;
-          k4[t] = cap < 0 ? -1 : cap;
+          const int32_t cap = state_cap(S);
+          capv = cap < 0 ? -1 : cap;
           if (cap < 0) {
             best = kInf;
           } else if (best != 0) {
+            uint32_t bu = 0xffffffffu;
             int win = -1;
-            for (int i = sp[j]; i < sp[j + 1]; ++i) {
+            const int i1 = sp[j + 1];
+            for (int i = sp[j]; i < i1; ++i) {
               const int2 x = ss[i];
-              const int l1 = x.x >> 24, l2 = x.y >> 24;
-              int32_t c1 = a.cost[ml.off[l1] + v * ml.stride[l1] + (x.x & 0xffffff)];
-              int32_t c2 = a.cost[ml.off[l2] + v * ml.stride[l2] + (x.y & 0xffffff)];
-              if (light_parts) {
-                c1 = light_or_inf(c1, ub_light);
-                c2 = light_or_inf(c2, ub_light);
-              }
-              if (c1 < kInf && c2 < kInf) {
-                const int32_t c = c1 + c2;  // both < 2^30: no wrap
-                if (c >= ovf_limit)
-                  acc[2] = 1;
-                else if (c < best) {
-                  best = c;
-                  win = i;
-                }
+              const uint32_t c = col[x.x] + col[x.y];
+              if (c < bu) {
+                bu = c;
+                win = i;
               }
             }
-            acc[1] += sp[j + 1] - sp[j];
-            if (win >= 0) {
-              const int2 x = ss[win];
-              code = -__ldg(ml.lmasks_all + ml.mbase[x.x >> 24] + (x.x & 0xffffff));
+            acc[1] += i1 - sp[j];
+            if (bu < 0x80000000u) {  // both parts finite
+              if (bu >= (uint32_t)ovf_limit) {
+                acc[2] = 1;
+              } else {
+                best = (int32_t)bu;
+                const int2 x = a.msplits[win];
+                code = -__ldg(ml.lmasks_all + ml.mbase[x.x >> 24] + (x.x & 0xffffff));
+              }
             }
           }
           if (best < kInf && (best > cap || best > keep23)) {
@@ -497,18 +514,66 @@ __global__ void __launch_bounds__(kGrowThreads) k_merge_vertex(GraphDev g, Level
             code = kLeaf;
           }
         }
-        b4[t] = best;
-        c4[t] = code;
+        rowc[j] = best;
+        rowp[j] = code;
+        if (ub > 0 || late) rowk[j] = capv;  // the growth of this wave prunes by it
         if (best < kInf) {
           any = true;
           ++acc[0];
         }
       }
-      rowc[j0 >> 2] = make_int4(b4[0], b4[1], b4[2], b4[3]);
-      rowp[j0 >> 2] = make_int4(c4[0], c4[1], c4[2], c4[3]);
-      if (ub > 0 || late) rowk[j0 >> 2] = make_int4(k4[0], k4[1], k4[2], k4[3]);  // the growth of this wave prunes by it
+    } else {
+      for (int j = 0; j < a.stride; ++j) {  // the same j on every lane of the team
+        int32_t best = kInf, code = kLeaf, capv = -1;
+        if (j < a.m) {
+          const uint32_t S = (uint32_t)__ldg(a.lmasks + j);
+          if ((gm & S) == S) best = 0;
+          const int32_t cap = state_cap(S);
+          capv = cap < 0 ? -1 : cap;
+          if (cap < 0) {
+            best = kInf;
+          } else if (best != 0) {
+            unsigned long long key = ~0ull;
+            const int i0 = sp[j], i1 = sp[j + 1];
+            for (int i = i0 + lane; i < i1; i += T) {
+              const int2 x = ss[i];
+              const unsigned long long kk = ((unsigned long long)(col[x.x] + col[x.y]) << 32) | (uint32_t)i;
+              key = kk < key ? kk : key;
+            }
+#pragma unroll
+            for (int o = T / 2; o > 0; o >>= 1) {
+              const unsigned long long y = __shfl_xor_sync(tmask, key, o);
+              key = y < key ? y : key;
+            }
+            if (lane == 0) acc[1] += i1 - i0;
+            const uint32_t bu = (uint32_t)(key >> 32);
+            if (key != ~0ull && bu < 0x80000000u) {  // both parts finite
+              if (bu >= (uint32_t)ovf_limit) {
+                acc[2] = 1;
+              } else {
+                best = (int32_t)bu;
+                const int2 x = a.msplits[(int)(key & 0xffffffffull)];
+                code = -__ldg(ml.lmasks_all + ml.mbase[x.x >> 24] + (x.x & 0xffffff));
+              }
+            }
+          }
+          if (best < kInf && (best > cap || best > keep23)) {
+            best = kInf;
+            code = kLeaf;
+          }
+        }
+        if (lane == 0) {
+          rowc[j] = best;
+          rowp[j] = code;
+          if (ub > 0 || late) rowk[j] = capv;
+          if (best < kInf) ++acc[0];
+        }
+        any = any || best < kInf;
+      }
     }
-    if (any) flag2[v] = 1;
+    any = __any_sync(tmask, any);
+    if (lane == 0 && any) flag2[v] = 1;
+    __syncwarp(tmask);  // the slice is rewritten for the next vertex
   }
   block_sum(acc);
   if (threadIdx.x == 0) {
@@ -520,6 +585,7 @@ __global__ void __launch_bounds__(kGrowThreads) k_merge_vertex(GraphDev g, Level
     if (acc[2]) atomicExch(&a.ctr->overflow, 1);
   }
 }
+
 
 // ------------------------------------------------------------------- grow --
 // One label-correcting round for every mask of the level, pull form: each
@@ -2217,30 +2283,40 @@ cudaError_t launch_merge(const GraphDev& g, const LevelArgs& a, const MergeLevel
   if (a.k <= kMergeTabK && a.msplit_ptr) {
     int32_t words = 0;  // lower-level row words per vertex
     for (int l = 1; l < a.level; ++l) words += ml.stride[l];
-    if (words <= kMergeStagedWords) {
-      const int nt = words <= kMergeStagedWords128 ? 128 : 64;
+    if (words > kMergeStagedWords128 || (words > kMergeTeamMinWords && a.m >= kMergeTeamMinMasks)) {  // a team per vertex
+      const int t = words <= kMergeStagedWords ? 4 : 32;
       const size_t smem = (size_t)((a.m + 2) & ~1) * sizeof(int32_t) + (size_t)a.nsplits * sizeof(int2) +
-                          (size_t)words * nt * sizeof(int32_t);
-      const void* fn = nt == 128 ? (const void*)k_merge_staged<128> : (const void*)k_merge_staged<64>;
-      if (smem > kSmemNoOptIn) {  // up to ~80 KB (set on the current device every time)
+                          (size_t)(kMergeTeamThreads / t) * words * sizeof(int32_t);
+      const bool lane_masks = a.m >= t;
+      const void* fn = t == 4 ? (lane_masks ? (const void*)k_merge_team<4, true> : (const void*)k_merge_team<4, false>)
+                              : (lane_masks ? (const void*)k_merge_team<32, true> : (const void*)k_merge_team<32, false>);
+      if (smem > kSmemNoOptIn) {  // up to ~75 KB (set on the current device every time)
         const cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
       }
-      const int64_t blocks = ((int64_t)g.V + nt - 1) / nt;  // a thread per vertex
-      if (nt == 128)
-        k_merge_staged<128><<<(unsigned)blocks, 128, smem, stream>>>(g, a, ml);
+      const int teams = kMergeTeamThreads / t;
+      const int64_t blocks = std::min<int64_t>(((int64_t)g.V + teams - 1) / teams, 4096);
+      const dim3 grid((unsigned)blocks), block(kMergeTeamThreads);
+      if (t == 4 && lane_masks)
+        k_merge_team<4, true><<<grid, block, smem, stream>>>(g, a, ml, words);
+      else if (t == 4)
+        k_merge_team<4, false><<<grid, block, smem, stream>>>(g, a, ml, words);
+      else if (lane_masks)
+        k_merge_team<32, true><<<grid, block, smem, stream>>>(g, a, ml, words);
       else
-        k_merge_staged<64><<<(unsigned)blocks, 64, smem, stream>>>(g, a, ml);
+        k_merge_team<32, false><<<grid, block, smem, stream>>>(g, a, ml, words);
       return cudaGetLastError();
     }
-    const size_t smem = (size_t)((a.m + 2) & ~1) * sizeof(int32_t) + (size_t)a.nsplits * sizeof(int2);
-    if (smem > kSmemNoOptIn) {  // k = 9, 10: up to ~60 KB (set on the current device every time)
-      const cudaError_t e = cudaFuncSetAttribute(k_merge_vertex, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    // a thread per vertex (at most kMergeStagedWords128 words)
+    const size_t smem = (size_t)((a.m + 2) & ~1) * sizeof(int32_t) + (size_t)a.nsplits * sizeof(int2) +
+                        (size_t)words * 128 * sizeof(int32_t);
+    if (smem > kSmemNoOptIn) {  // up to ~75 KB (set on the current device every time)
+      const cudaError_t e =
+          cudaFuncSetAttribute(k_merge_staged<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return e;
     }
-    int64_t blocks = ((int64_t)g.V + kGrowThreads - 1) / kGrowThreads;
-    if (blocks > (1 << 20)) blocks = 1 << 20;
-    k_merge_vertex<<<(unsigned)blocks, kGrowThreads, smem, stream>>>(g, a, ml);
+    const int64_t blocks = ((int64_t)g.V + 127) / 128;
+    k_merge_staged<128><<<(unsigned)blocks, 128, smem, stream>>>(g, a, ml);
     return cudaGetLastError();
   }
   const int64_t total = (int64_t)g.V * a.stride;

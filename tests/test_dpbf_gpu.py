@@ -69,7 +69,7 @@ def test_empty_group_is_infeasible():
 
 
 @pytest.mark.parametrize("use_graph", MODES)
-@pytest.mark.parametrize("idx", [0, 1, 2, 3, 200, 201, 202, 203, 204])
+@pytest.mark.parametrize("idx", [0, 1, 2, 3, 200, 201, 202, 203, 204, 206])
 def test_full_state_table_matches_oracle(golden, idx, use_graph):
     case = golden["cases"][idx]
     g, gp, mem = make_instance(case)
