@@ -196,17 +196,17 @@ __global__ void __launch_bounds__(kGrowThreads) k_merge(GraphDev g, LevelArgs a)
   }
 }
 
-// One thread per vertex (k <= kMergeTabK, at most kMergeStagedWords128
-// words of lower-level row per vertex): the same states as k_merge, row by
-// row. A thread copies its vertex's rows of levels 1..l-1 into shared
-// memory once (light-filtered there when the merge uses light parts), a
-// column per thread, and every split then reads two shared words at
-// offsets precomputed into the block's copy of the split table (the
-// level's split table, loaded once per block); the vertex's group mask is
-// loaded once and its row written 16 bytes at a time. Blocks of NT = 128
-// threads (at most 68 KB of columns). Longer rows: k_merge_team.
-constexpr int kMergeStagedWords128 = 136;  // waves 2-6 of k = 7, 2-4 of k = 8
-constexpr int kMergeStagedWords = 256;     // the longest rows of k = 8 (teams of 4 up to here)
+// One thread per vertex (k <= kMergeTabK, at most kMergeTeamMinWords words
+// of lower-level row per vertex, or a level of few masks over at most twice
+// that: every wave of k <= 6, waves 2-3 of k = 7 and 8): the same states as k_merge, row by row. A thread copies its
+// vertex's rows of levels 1..l-1 into shared memory once (light-filtered
+// there when the merge uses light parts), a column per thread, and every
+// split then reads two shared words at offsets precomputed into the block's
+// copy of the split table (the level's split table, loaded once per block);
+// the vertex's group mask is loaded once and its row written 16 bytes at a
+// time. Blocks of NT = 128 threads (at most 64 KB of columns). Longer rows:
+// k_merge_team.
+constexpr int kMergeStagedWords = 256;  // the longest rows of k = 8 (teams of 4 up to here)
 
 template <int NT>
 __global__ void __launch_bounds__(NT) k_merge_staged(GraphDev g, LevelArgs a, MergeLevels ml) {
@@ -373,12 +373,10 @@ __global__ void __launch_bounds__(NT) k_merge_staged(GraphDev g, LevelArgs a, Me
 
 // A team of T lanes per vertex, for the merges whose lower-level rows are
 // too long to stage a thread per vertex at a useful occupancy: more than
-// kMergeStagedWords128 words (k_merge_staged would run blocks of 64 threads,
-// 8-10 warps per SM: waves 5-8 of k = 8, wave 7 of k = 7, and k = 9, 10),
-// or more than kMergeTeamMinWords words in a level of at least
-// kMergeTeamMinMasks masks (wave 4 of k = 8). Waves 4-6 of k = 7 stay with
-// k_merge_staged, which was faster there (ba4m_k7 bounded 22.7 against
-// 23.3 ms with teams; ba2m_k8 bounded 35.3 -> 32.9 ms with wave 4 by teams).
+// kMergeTeamMinWords words (waves 4 and up of k = 7 and 8, and k = 9, 10),
+// where k_merge_staged keeps 8-16 warps per SM, unless the level has fewer
+// than kMergeTeamMinMasks masks and at most twice that many words (the last
+// merge of k = 6: one mask over 68 words, faster by a thread per vertex).
 // The team copies its vertex's rows of levels 1..l-1 into its own slice of
 // shared memory (consecutive words by consecutive lanes, light-filtered as
 // in k_merge_staged), then evaluates the level's states. LANE_MASKS (a
@@ -393,7 +391,7 @@ __global__ void __launch_bounds__(NT) k_merge_staged(GraphDev g, LevelArgs a, Me
 // 32 beyond. Persistent blocks of kMergeTeamThreads threads stride over
 // the vertices.
 constexpr int kMergeTeamMinWords = 64;
-constexpr int kMergeTeamMinMasks = 64;
+constexpr int kMergeTeamMinMasks = 4;
 constexpr int kMergeTeamThreads = 256;
 
 template <int T, bool LANE_MASKS>
@@ -405,7 +403,7 @@ __global__ void __launch_bounds__(kMergeTeamThreads) k_merge_team(GraphDev g, Le
   __shared__ int32_t loff[kMergeTabK + 1];  // level l's first word in a vertex's staged rows
   int32_t* sp = msm;                                             // m + 1
   int2* ss = reinterpret_cast<int2*>(msm + ((a.m + 2) & ~1));   // nsplits: staged word offsets
-  uint32_t* rows = reinterpret_cast<uint32_t*>(ss + a.nsplits);  // kTeams x words
+  uint32_t* rows = reinterpret_cast<uint32_t*>(ss + a.nsplits);  // kTeams slices of (words | 1) words
   if (threadIdx.x == 0) {
     int32_t o = 0;
     for (int l = 1; l < a.level; ++l) {
@@ -430,7 +428,8 @@ __global__ void __launch_bounds__(kMergeTeamThreads) k_merge_team(GraphDev g, Le
   constexpr uint32_t kStagedInf = 0xC0000000u;  // as in k_merge_staged
   const int team = threadIdx.x / T, lane = threadIdx.x % T;
   const unsigned tmask = T == 32 ? 0xffffffffu : ((1u << T) - 1u) << ((threadIdx.x & 31) & ~(T - 1));
-  uint32_t* col = rows + (int64_t)team * words;
+  // an odd slice length puts the same word of the warp's teams in distinct banks
+  uint32_t* col = rows + (int64_t)team * (words | 1);
   const uint32_t beyond = (uint32_t)(ub / 2 + 1);
   const uint32_t full = (1u << a.k) - 1u;
   // the cap of state S at the staged vertex: ub minus the one-label bound
@@ -2033,6 +2032,9 @@ __global__ void __launch_bounds__(kGrowThreads, (L >= 3 ? 3 : 4)) k_grow_group(G
 // states T(v,{g}) for the groups g outside S (each stored cost is that of
 // an actual tree or path, so the sum bounds the union's cost and hence the
 // optimum from above). The cheapest one lowers params->ub (0 = none yet).
+// A zero-cost tree is no bound in that encoding (0 reads as "none", and a
+// later, costlier candidate would then raise the bound): it is skipped,
+// and the bound stays what it was (still valid, only less tight).
 // The restatement, over all states of a wave at once, of PrunedDP++'s
 // update of its best solution (graph_v_of_v_idealID_PrunedDPPlusPlus.h:668-711).
 __global__ void __launch_bounds__(kGrowThreads) k_ub_refine(GraphDev g, LevelArgs a) {
@@ -2075,7 +2077,7 @@ __global__ void __launch_bounds__(kGrowThreads) k_ub_refine(GraphDev g, LevelArg
   __syncthreads();
   if (threadIdx.x != 0) return;
   for (int w = 1; w < (int)(blockDim.x >> 5); ++w) best = sbest[w] < best ? sbest[w] : best;
-  if (best >= (long long)kInf) return;
+  if (best >= (long long)kInf || best <= 0) return;
   int32_t* ub = const_cast<int32_t*>(&a.params->ub);
   const int32_t cand = (int32_t)best;
   int32_t old = *reinterpret_cast<volatile int32_t*>(ub);
@@ -2283,10 +2285,10 @@ cudaError_t launch_merge(const GraphDev& g, const LevelArgs& a, const MergeLevel
   if (a.k <= kMergeTabK && a.msplit_ptr) {
     int32_t words = 0;  // lower-level row words per vertex
     for (int l = 1; l < a.level; ++l) words += ml.stride[l];
-    if (words > kMergeStagedWords128 || (words > kMergeTeamMinWords && a.m >= kMergeTeamMinMasks)) {  // a team per vertex
+    if (words > kMergeTeamMinWords && (a.m >= kMergeTeamMinMasks || words > 2 * kMergeTeamMinWords)) {  // a team
       const int t = words <= kMergeStagedWords ? 4 : 32;
       const size_t smem = (size_t)((a.m + 2) & ~1) * sizeof(int32_t) + (size_t)a.nsplits * sizeof(int2) +
-                          (size_t)(kMergeTeamThreads / t) * words * sizeof(int32_t);
+                          (size_t)(kMergeTeamThreads / t) * (words | 1) * sizeof(int32_t);
       const bool lane_masks = a.m >= t;
       const void* fn = t == 4 ? (lane_masks ? (const void*)k_merge_team<4, true> : (const void*)k_merge_team<4, false>)
                               : (lane_masks ? (const void*)k_merge_team<32, true> : (const void*)k_merge_team<32, false>);
@@ -2307,7 +2309,7 @@ cudaError_t launch_merge(const GraphDev& g, const LevelArgs& a, const MergeLevel
         k_merge_team<32, false><<<grid, block, smem, stream>>>(g, a, ml, words);
       return cudaGetLastError();
     }
-    // a thread per vertex (at most kMergeStagedWords128 words)
+    // a thread per vertex (at most kMergeTeamMinWords words, or the short single-mask merges)
     const size_t smem = (size_t)((a.m + 2) & ~1) * sizeof(int32_t) + (size_t)a.nsplits * sizeof(int2) +
                         (size_t)words * 128 * sizeof(int32_t);
     if (smem > kSmemNoOptIn) {  // up to ~75 KB (set on the current device every time)

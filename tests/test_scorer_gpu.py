@@ -127,8 +127,9 @@ def test_proposal_is_feasible_and_learned_solve_exact(use_scorer):
             # a proposal's root distances stop after a fixed number of rounds, so two proposals of
             # one query may differ (in-place updates run in no fixed order); each is a feasible tree
             assert seq.proposal_cost >= plain.cost
-            # the refined bound: a feasible cost, or 0 (= no bound) once a zero-cost tree is seen
-            assert seq.upper_bound <= seq.proposal_cost and (seq.upper_bound >= plain.cost or plain.cost == 0)
+            # the refined bound only drops from the proposal's cost, and stays a feasible cost (a
+            # zero-cost tree leaves it unchanged: 0 would read as "no bound")
+            assert plain.cost <= seq.upper_bound <= seq.proposal_cost
             # captured: the proposal runs beside the DP; its bound lands unless the DP finished first
             res = dg.solve_learned(s, gp, mem)
             assert res.status == N.Status.OK and res.cost == plain.cost and res.proposal_concurrent
@@ -136,7 +137,7 @@ def test_proposal_is_feasible_and_learned_solve_exact(use_scorer):
             assert res.proposal_cost == 0 or res.proposal_cost >= plain.cost
             if res.proposal_cost:
                 assert res.upper_bound <= res.proposal_cost
-            assert res.upper_bound >= plain.cost or res.upper_bound == 0
+            assert res.upper_bound >= plain.cost or res.upper_bound == 0  # 0: no bound was found
             for r in (seq, res):
                 err = oracle.check_tree(g.row_ptr, g.col, g.w, gp, mem, r.vertices, r.edges, r.cost)
                 assert err is None, err
