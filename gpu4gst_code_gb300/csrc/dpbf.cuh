@@ -169,7 +169,10 @@ struct LevelArgs {
   // tour table of the PrunedDP++ tour bound (k <= kTourMaxK, 2 <= level < k;
   // null otherwise): path[(i << k | X) * k + j] = the cheapest order of
   // visiting the groups of X from group i to group j, over lower bounds of
-  // the group-to-group distances, clamped at the bound
+  // the group-to-group distances, clamped at the bound; then W2 (k x 2^k);
+  // then, at k x 2^k x (k + 1), the level's compact tables that the merges
+  // copy to shared memory: for mask rank j, the W2 values of the n = k -
+  // level groups outside S_j and the path values of their pairs i < i2
   const int32_t* tour;
 };
 
@@ -179,6 +182,9 @@ struct LevelArgs {
 // tour buffer (global memory, 400 KB at k = 10) beyond.
 constexpr int kTourMaxK = 10;
 constexpr int kTourSmemMaxK = 9;
+// Room for the largest level's compact tour tables (C(10,4) masks x (6 + 15)
+// entries = 4,410 words at k = 10).
+constexpr int kTourCompactWords = 8192;
 
 // Queries with at most kMergeTabK groups merge from per-level split tables
 // (k_merge_staged: a thread per vertex; k_merge_team: a team of lanes per

@@ -214,7 +214,9 @@ __global__ void __launch_bounds__(NT) k_merge_staged(GraphDev g, LevelArgs a, Me
   __shared__ int32_t loff[kMergeTabK + 1];  // level l's first word in a vertex's staged rows
   int32_t* sp = msm;                                            // m + 1
   int2* ss = reinterpret_cast<int2*>(msm + ((a.m + 2) & ~1));  // nsplits: staged word offsets x NT
-  int32_t* rows = reinterpret_cast<int32_t*>(ss + a.nsplits);   // staged words x NT
+  const int tn = a.k - a.level, te = tn + tn * (tn - 1) / 2;  // compact tour entries per mask
+  int32_t* sct = reinterpret_cast<int32_t*>(ss + a.nsplits);    // a.m x te when a.tour
+  int32_t* rows = sct + (a.tour ? a.m * te : 0);                // staged words x NT
   if (threadIdx.x == 0) {
     int32_t o = 0;
     for (int l = 1; l < a.level; ++l) {
@@ -224,6 +226,10 @@ __global__ void __launch_bounds__(NT) k_merge_staged(GraphDev g, LevelArgs a, Me
   }
   for (int i = threadIdx.x; i <= a.m; i += blockDim.x) sp[i] = a.msplit_ptr[i];
   __syncthreads();
+  if (a.tour) {
+    const int32_t* ct = a.tour + ((int64_t)a.k << a.k) * (a.k + 1);
+    for (int i = threadIdx.x; i < a.m * te; i += blockDim.x) sct[i] = ct[i];
+  }
   for (int i = threadIdx.x; i < a.nsplits; i += blockDim.x) {
     const int2 x = a.msplits[i];
     ss[i] = make_int2((loff[x.x >> 24] + (x.x & 0xffffff)) * NT, (loff[x.y >> 24] + (x.y & 0xffffff)) * NT);
@@ -299,18 +305,20 @@ __global__ void __launch_bounds__(NT) k_merge_staged(GraphDev g, LevelArgs a, Me
             //       over X) + the distance back from the nearest group of X
             //  (halving is monotone, so each side halves its extreme sum once;
             //  every sum is at most ub / 2 + 1 + ub + ub / 2 + 1: unsigned, no wrap)
+            // The path and W2 values of this mask come from the level's compact
+            // table in shared memory, in the order its loops visit them.
             uint32_t p1 = 0xffffffffu, p2 = 0u, dmin = 0xffffffffu;
-            const int32_t* w2 = a.tour + ((int64_t)a.k << a.k) * a.k;
-            for (uint32_t xi = X; xi; xi &= xi - 1u) {
+            const int32_t* tj = sct + j * te;
+            int ai = 0, pi = tn;
+            for (uint32_t xi = X; xi; xi &= xi - 1u, ++ai) {
               const int i = __ffs(xi) - 1;
               const uint32_t di = min(colu[i * NT], beyond);
-              const int32_t* fi = a.tour + (((int64_t)i << a.k) | X) * a.k;
               dmin = min(dmin, di);
               dmax = max(dmax, di);
-              p2 = max(p2, di + (uint32_t)__ldg(w2 + ((int64_t)i << a.k) + X));
-              for (uint32_t xj = xi & (xi - 1u); xj; xj &= xj - 1u) {
+              p2 = max(p2, di + (uint32_t)tj[ai]);
+              for (uint32_t xj = xi & (xi - 1u); xj; xj &= xj - 1u, ++pi) {
                 const int i2 = __ffs(xj) - 1;
-                p1 = min(p1, di + (uint32_t)__ldg(fi + i2) + min(colu[i2 * NT], beyond));
+                p1 = min(p1, di + (uint32_t)tj[pi] + min(colu[i2 * NT], beyond));
               }
             }
             lb = (int32_t)max(dmax, max(p1 >> 1, (p2 + dmin) >> 1));
@@ -403,7 +411,9 @@ __global__ void __launch_bounds__(kMergeTeamThreads) k_merge_team(GraphDev g, Le
   __shared__ int32_t loff[kMergeTabK + 1];  // level l's first word in a vertex's staged rows
   int32_t* sp = msm;                                             // m + 1
   int2* ss = reinterpret_cast<int2*>(msm + ((a.m + 2) & ~1));   // nsplits: staged word offsets
-  uint32_t* rows = reinterpret_cast<uint32_t*>(ss + a.nsplits);  // kTeams slices of (words | 1) words
+  const int tn = a.k - a.level, te = tn + tn * (tn - 1) / 2;  // compact tour entries per mask
+  int32_t* sct = reinterpret_cast<int32_t*>(ss + a.nsplits);    // a.m x te when a.tour
+  uint32_t* rows = reinterpret_cast<uint32_t*>(sct + (a.tour ? a.m * te : 0));  // kTeams slices of (words | 1) words
   if (threadIdx.x == 0) {
     int32_t o = 0;
     for (int l = 1; l < a.level; ++l) {
@@ -413,6 +423,10 @@ __global__ void __launch_bounds__(kMergeTeamThreads) k_merge_team(GraphDev g, Le
   }
   for (int i = threadIdx.x; i <= a.m; i += blockDim.x) sp[i] = a.msplit_ptr[i];
   __syncthreads();
+  if (a.tour) {
+    const int32_t* ct = a.tour + ((int64_t)a.k << a.k) * (a.k + 1);
+    for (int i = threadIdx.x; i < a.m * te; i += blockDim.x) sct[i] = ct[i];
+  }
   for (int i = threadIdx.x; i < a.nsplits; i += blockDim.x) {
     const int2 x = a.msplits[i];
     ss[i] = make_int2(loff[x.x >> 24] + (x.x & 0xffffff), loff[x.y >> 24] + (x.y & 0xffffff));
@@ -432,11 +446,12 @@ __global__ void __launch_bounds__(kMergeTeamThreads) k_merge_team(GraphDev g, Le
   uint32_t* col = rows + (int64_t)team * (words | 1);
   const uint32_t beyond = (uint32_t)(ub / 2 + 1);
   const uint32_t full = (1u << a.k) - 1u;
-  // the cap of state S at the staged vertex: ub minus the one-label bound
-  // (wave 1's distances, words 0..k-1 of the staged rows) or, with the
-  // tour tables, the largest of the one-label and the two tour bounds;
-  // kInf without a bound
-  auto state_cap = [&](uint32_t S) -> int32_t {
+  // the cap of state S (mask rank j) at the staged vertex: ub minus the
+  // one-label bound (wave 1's distances, words 0..k-1 of the staged rows)
+  // or, with the tour tables (the level's compact table in shared memory),
+  // the largest of the one-label and the two tour bounds; kInf without a
+  // bound
+  auto state_cap = [&](uint32_t S, int j) -> int32_t {
     if (ub <= 0) return kInf;
     const uint32_t X = full ^ S;
     uint32_t dmax = 0u;
@@ -445,17 +460,17 @@ __global__ void __launch_bounds__(kMergeTeamThreads) k_merge_team(GraphDev g, Le
       return ub - (int32_t)dmax;
     }
     uint32_t p1 = 0xffffffffu, p2 = 0u, dmin = 0xffffffffu;
-    const int32_t* w2 = a.tour + ((int64_t)a.k << a.k) * a.k;
-    for (uint32_t xi = X; xi; xi &= xi - 1u) {
+    const int32_t* tj = sct + j * te;
+    int ai = 0, pi = tn;
+    for (uint32_t xi = X; xi; xi &= xi - 1u, ++ai) {
       const int i = __ffs(xi) - 1;
       const uint32_t di = min(col[i], beyond);
-      const int32_t* fi = a.tour + (((int64_t)i << a.k) | X) * a.k;
       dmin = min(dmin, di);
       dmax = max(dmax, di);
-      p2 = max(p2, di + (uint32_t)__ldg(w2 + ((int64_t)i << a.k) + X));
-      for (uint32_t xj = xi & (xi - 1u); xj; xj &= xj - 1u) {
+      p2 = max(p2, di + (uint32_t)tj[ai]);
+      for (uint32_t xj = xi & (xi - 1u); xj; xj &= xj - 1u, ++pi) {
         const int i2 = __ffs(xj) - 1;
-        p1 = min(p1, di + (uint32_t)__ldg(fi + i2) + min(col[i2], beyond));
+        p1 = min(p1, di + (uint32_t)tj[pi] + min(col[i2], beyond));
       }
     }
     return ub - (int32_t)max(dmax, max(p1 >> 1, (p2 + dmin) >> 1));
@@ -481,7 +496,7 @@ __global__ void __launch_bounds__(kMergeTeamThreads) k_merge_team(GraphDev g, Le
         if (j < a.m) {
           const uint32_t S = (uint32_t)__ldg(a.lmasks + j);
           if ((gm & S) == S) best = 0;
-          const int32_t cap = state_cap(S);
+          const int32_t cap = state_cap(S, j);
           capv = cap < 0 ? -1 : cap;
           if (cap < 0) {
             best = kInf;
@@ -527,7 +542,7 @@ __global__ void __launch_bounds__(kMergeTeamThreads) k_merge_team(GraphDev g, Le
         if (j < a.m) {
           const uint32_t S = (uint32_t)__ldg(a.lmasks + j);
           if ((gm & S) == S) best = 0;
-          const int32_t cap = state_cap(S);
+          const int32_t cap = state_cap(S, j);
           capv = cap < 0 ? -1 : cap;
           if (cap < 0) {
             best = kInf;
@@ -2169,6 +2184,22 @@ __global__ void __launch_bounds__(1024) k_tour_table(LevelArgs a, const int32_t*
     }
     tour[k * W * k + t] = best;
   }
+  // the level's compact tables (after W2): for mask rank j, X = the groups
+  // outside S_j (n = k - level of them, in increasing order): W2[i][X] of
+  // each, then path[i][X][i2] of each pair i < i2 in order
+  __syncthreads();
+  const int n = k - a.level, E = n + n * (n - 1) / 2;
+  int32_t* ct = tour + k * W * k + k * W;
+  for (int j = threadIdx.x; j < a.m; j += blockDim.x) {
+    const uint32_t X = (uint32_t)(W - 1) ^ (uint32_t)a.lmasks[j];
+    int32_t* e = ct + j * E;
+    int ai = 0, p = n;
+    for (uint32_t xi = X; xi; xi &= xi - 1u, ++ai) {
+      const int i = __ffs(xi) - 1;
+      e[ai] = tour[k * W * k + i * W + (int)X];
+      for (uint32_t xj = xi & (xi - 1u); xj; xj &= xj - 1u, ++p) e[p] = F[((i << k) | (int)X) * k + __ffs(xj) - 1];
+    }
+  }
 }
 
 __global__ void k_argmin(int32_t V, const int32_t* __restrict__ full_slice, int32_t stride, Counters* ctr) {
@@ -2285,9 +2316,12 @@ cudaError_t launch_merge(const GraphDev& g, const LevelArgs& a, const MergeLevel
   if (a.k <= kMergeTabK && a.msplit_ptr) {
     int32_t words = 0;  // lower-level row words per vertex
     for (int l = 1; l < a.level; ++l) words += ml.stride[l];
+    const int tn = a.k - a.level;
+    const int64_t tour_words = a.tour ? (int64_t)a.m * (tn + tn * (tn - 1) / 2) : 0;  // compact tour tables
     if (words > kMergeTeamMinWords && (a.m >= kMergeTeamMinMasks || words > 2 * kMergeTeamMinWords)) {  // a team
       const int t = words <= kMergeStagedWords ? 4 : 32;
       const size_t smem = (size_t)((a.m + 2) & ~1) * sizeof(int32_t) + (size_t)a.nsplits * sizeof(int2) +
+                          (size_t)tour_words * sizeof(int32_t) +
                           (size_t)(kMergeTeamThreads / t) * (words | 1) * sizeof(int32_t);
       const bool lane_masks = a.m >= t;
       const void* fn = t == 4 ? (lane_masks ? (const void*)k_merge_team<4, true> : (const void*)k_merge_team<4, false>)
@@ -2311,7 +2345,7 @@ cudaError_t launch_merge(const GraphDev& g, const LevelArgs& a, const MergeLevel
     }
     // a thread per vertex (at most kMergeTeamMinWords words, or the short single-mask merges)
     const size_t smem = (size_t)((a.m + 2) & ~1) * sizeof(int32_t) + (size_t)a.nsplits * sizeof(int2) +
-                        (size_t)words * 128 * sizeof(int32_t);
+                        (size_t)tour_words * sizeof(int32_t) + (size_t)words * 128 * sizeof(int32_t);
     if (smem > kSmemNoOptIn) {  // up to ~75 KB (set on the current device every time)
       const cudaError_t e =
           cudaFuncSetAttribute(k_merge_staged<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

@@ -137,7 +137,9 @@ struct Workspace {
   int32_t* hub_cnt = nullptr;             // nbig chunk counters
   int32_t hub_stride = 0;
   int32_t* capt = nullptr;  // V x the widest row stride: the current wave's pruning caps
-  int32_t* tour = nullptr;  // tour-bound tables: path (k x 2^k x k), then W2 (k x 2^k), kTourMaxK sized
+  // tour-bound tables: path (k x 2^k x k), W2 (k x 2^k), then the current
+  // level's compact tables (at most 4,410 words at k = 10), kTourMaxK sized
+  int32_t* tour = nullptr;
   // pinned host mirrors
   Counters* h_ctr = nullptr;
   GrowCtl* h_ctl = nullptr;
@@ -413,7 +415,8 @@ gst_status ensure_workspace(gst_graph* g, int32_t k, int64_t nmembers) {
     GST_CUDA(cudaMalloc(&ws.qb, (size_t)ws.bt_cap * sizeof(int2)));
     GST_CUDA(cudaMalloc(&ws.out_v, (size_t)ws.bt_cap * sizeof(int32_t)));
     GST_CUDA(cudaMalloc(&ws.out_e, (size_t)ws.bt_cap * sizeof(int3)));
-    GST_CUDA(cudaMalloc(&ws.tour, (size_t)kTourMaxK * (1 << kTourMaxK) * (kTourMaxK + 1) * sizeof(int32_t)));
+    GST_CUDA(cudaMalloc(&ws.tour, ((size_t)kTourMaxK * (1 << kTourMaxK) * (kTourMaxK + 1) + kTourCompactWords) *
+                                      sizeof(int32_t)));
   }
   if (k > ws.k_cap) {
     dfree(ws.cost);
