@@ -1307,6 +1307,10 @@ gst_status propose_tree(gst_graph* g, const gst_scorer* sc, const int32_t* group
   };
   gst_status st = ensure_learn_infer(g);
   if (st != GST_OK) return st;
+  // beside a solve, the device work starts once the solve's wave 1 has
+  // grown: its dense rounds are the solve's most bandwidth-bound part, and
+  // the paths below read wave 1 anyway
+  if (dp) GST_CUDA(cudaStreamWaitEvent(s, dp->ws.ev_wave1, 0));
   st = upload_groups(g, group_ptr, members, k);
   if (st != GST_OK) return st;
   st = compute_features(g, k);
@@ -1360,9 +1364,9 @@ gst_status propose_tree(gst_graph* g, const gst_scorer* sc, const int32_t* group
   for (size_t i = 0; i < cand.size() && (int)i < kProposeTop; ++i) top.push_back((int32_t)cand[i].y);
   phase("top");
   if (dp) {
-    // the root's paths over the running solve's wave 1: exact distances
-    // from every vertex to every group, grown before its later waves
-    GST_CUDA(cudaStreamWaitEvent(s, dp->ws.ev_wave1, 0));
+    // the root's paths over the running solve's wave 1 (complete: the
+    // stream waited for it above): exact distances from every vertex to
+    // every group, grown before its later waves
     GST_CUDA(cudaMemsetAsync(lw.pn, 0, 4 * sizeof(int32_t), s));
     GST_CUDA(launch_root_paths(graph_dev(g), dp->ws.cost, dp->ws.par, dp->ws.h_lvl_stride[1], ws.gmask, root, k,
                                lw.pe, lw.pn, lw.pe_cap, s));
