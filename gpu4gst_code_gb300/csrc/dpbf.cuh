@@ -186,6 +186,22 @@ constexpr int kTourSmemMaxK = 9;
 // entries = 4,410 words at k = 10).
 constexpr int kTourCompactWords = 8192;
 
+// Words of the compact tour tables of level l at k groups: C(k, l) masks x
+// (n + n (n - 1) / 2) entries, n = k - l groups outside each.
+constexpr int64_t tour_compact_words(int k, int l) {
+  int64_t c = 1;
+  for (int i = 0; i < l; ++i) c = c * (k - i) / (i + 1);
+  const int64_t n = k - l;
+  return c * (n + n * (n - 1) / 2);
+}
+constexpr bool tour_compact_fits() {
+  for (int k = 2; k <= kTourMaxK; ++k)
+    for (int l = 2; l < k; ++l)
+      if (tour_compact_words(k, l) > kTourCompactWords) return false;
+  return true;
+}
+static_assert(tour_compact_fits(), "the compact tour tables of every level fit their room");
+
 // Queries with at most kMergeTabK groups merge from per-level split tables
 // (k_merge_staged: a thread per vertex; k_merge_team: a team of lanes per
 // vertex for long lower-level rows); larger k use k_merge.
