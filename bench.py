@@ -550,11 +550,14 @@ def main():
         d_ms, w_s = max_over_ranks([sum(dev_ms(r, method) for r, _ in res), sum(w for _, w in res)], dist)
         arms[method] = dict(results=res, dev_ms=d_ms, wall_s=w_s, qps=world * args.steps / (d_ms / 1e3),
                             e2e=world * args.steps / w_s)
-    # Roofline pass of the growth kernels: the same plain queries through the
-    # host-launched driver, whose per-wave CUDA events (on the solver's
-    # stream) bracket only growth launches; algorithmic bytes from the
-    # kernels' own counters. Not part of `value`.
-    roof = [dg.solve(*queries[i], collect_stats=True, use_graph=False) for i in range(args.warmup, n_total)]
+    # Roofline pass of the growth kernels: the same plain queries with
+    # statistics on, through the same driver. Per-wave CUDA events on the
+    # solver's stream bracket only the growth rounds (with the CUDA-graph
+    # driver they are event nodes of the query's graph, captured for solves
+    # with statistics on); algorithmic bytes from the kernels' own
+    # counters. Not part of `value`.
+    dg.solve(*queries[0], collect_stats=True, use_graph=use_graph)  # captures the timed graph
+    roof = [dg.solve(*queries[i], collect_stats=True, use_graph=use_graph) for i in range(args.warmup, n_total)]
     costs = {m: [r.cost for r, _ in a["results"]] for m, a in arms.items()}
     assert all(c == [r.cost for r in roof] for c in costs.values()), costs
     head = arms[methods[-1]]  # the metric's method: learned unless restricted

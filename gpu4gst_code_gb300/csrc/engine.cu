@@ -153,6 +153,9 @@ struct Workspace {
   cudaEvent_t ev_wave1 = nullptr;
   std::vector<int32_t> h_lvl_base, h_lvl_m, h_lvl_stride;
   QueryGraph qg[GST_MAX_K + 1];
+  // the same graphs with the per-wave timing events as external event nodes
+  // (solves with statistics on: their merge and growth times are read back)
+  QueryGraph qg_timed[GST_MAX_K + 1];
 };
 
 // Buffers of the learned proposal (allocated on first use).
@@ -290,11 +293,13 @@ GraphDev graph_dev(const gst_graph* g) {
 }
 
 void drop_graphs(Workspace& ws) {
-  for (auto& q : ws.qg) {
-    if (q.exec) cudaGraphExecDestroy(q.exec);
-    if (q.graph) cudaGraphDestroy(q.graph);
-    q = QueryGraph{};
-  }
+  for (QueryGraph* set : {ws.qg, ws.qg_timed})
+    for (int k = 0; k <= GST_MAX_K; ++k) {
+      QueryGraph& q = set[k];
+      if (q.exec) cudaGraphExecDestroy(q.exec);
+      if (q.graph) cudaGraphDestroy(q.graph);
+      q = QueryGraph{};
+    }
 }
 
 void free_learn(LearnWs& lw) {
@@ -659,35 +664,41 @@ gst_status capture_growth_loop(gst_graph* g, LevelArgs a, cudaStream_t s) {
   return GST_OK;
 }
 
-// Captures and instantiates the whole query for k (workspace generation gen).
-gst_status build_query_graph(gst_graph* g, int32_t k) {
+// Captures and instantiates the whole query for k (workspace generation
+// gen). timed: the per-wave events become external event nodes, so the
+// host reads each wave's merge and growth time after the launch (a few
+// microseconds more per query; used for solves with statistics on).
+gst_status build_query_graph(gst_graph* g, int32_t k, bool timed = false) {
   Workspace& ws = g->ws;
-  QueryGraph& q = ws.qg[k];
+  QueryGraph& q = timed ? ws.qg_timed[k] : ws.qg[k];
   if (q.exec && q.gen == ws.gen) return GST_OK;
   if (q.exec) cudaGraphExecDestroy(q.exec);
   if (q.graph) cudaGraphDestroy(q.graph);
   q = QueryGraph{};
   cudaStream_t s = g->stream;
   int64_t launches = 0;
+  auto record = [&](cudaEvent_t e) {
+    return timed ? cudaEventRecordWithFlags(e, s, cudaEventRecordExternal) : cudaEventRecord(e, s);
+  };
   GST_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
   gst_status st = enqueue_prologue(g, k, s, &launches);
   for (int32_t l = 1; st == GST_OK && l <= k; ++l) {
     const LevelArgs a = level_args(g, k, l);
-    if (cudaEventRecord(ws.ev[3 * l], s) != cudaSuccess) st = fail(GST_CUDA_ERROR, "event record");
+    if (record(ws.ev[3 * l]) != cudaSuccess) st = fail(GST_CUDA_ERROR, "event record");
     if (st == GST_OK) st = enqueue_merge(g, a, s, &launches);
-    if (st == GST_OK && cudaEventRecord(ws.ev[3 * l + 1], s) != cudaSuccess)
+    if (st == GST_OK && record(ws.ev[3 * l + 1]) != cudaSuccess)
       st = fail(GST_CUDA_ERROR, "event record");
     if (st == GST_OK && l < k) st = capture_growth_loop(g, a, s);
     // refinement after the last grown wave would only tighten the final
     // merge's cap, and the final merge evaluates every split either way
     if (st == GST_OK && l < k - 1 && launch_ub_refine(graph_dev(g), a, g->num_sms, s) != cudaSuccess)
       st = fail(GST_CUDA_ERROR, "bound refinement launch");
-    if (st == GST_OK && cudaEventRecord(ws.ev[3 * l + 2], s) != cudaSuccess)
+    if (st == GST_OK && record(ws.ev[3 * l + 2]) != cudaSuccess)
       st = fail(GST_CUDA_ERROR, "event record");
     if (st == GST_OK && l == 1 && cudaEventRecordWithFlags(ws.ev_wave1, s, cudaEventRecordExternal) != cudaSuccess)
       st = fail(GST_CUDA_ERROR, "event record");
   }
-  if (st == GST_OK && cudaEventRecord(ws.ev[1], s) != cudaSuccess) st = fail(GST_CUDA_ERROR, "event record");
+  if (st == GST_OK && record(ws.ev[1]) != cudaSuccess) st = fail(GST_CUDA_ERROR, "event record");
   if (st == GST_OK) st = enqueue_epilogue(g, k, s, &launches);
   cudaGraph_t graph = nullptr;
   const cudaError_t ee = cudaStreamEndCapture(s, &graph);
@@ -928,8 +939,9 @@ gst_status solve_one(gst_graph* g, const int32_t* group_ptr, const int32_t* memb
   // a non-sticky error left by an unrelated earlier runtime call would
   // otherwise surface at this solve's first kernel-launch check
   cudaGetLastError();
+  const bool timed = use_graph && o.collect_stats != 0;
   if (use_graph) {
-    st = build_query_graph(g, k);
+    st = build_query_graph(g, k, timed);
     if (st != GST_OK) return st;
   }
   fill_params(g, k, o);
@@ -944,7 +956,7 @@ gst_status solve_one(gst_graph* g, const int32_t* group_ptr, const int32_t* memb
   int64_t launches = 0;
   bool timeout = false;
   if (use_graph) {
-    GST_CUDA(cudaGraphLaunch(ws.qg[k].exec, s));
+    GST_CUDA(cudaGraphLaunch((timed ? ws.qg_timed[k] : ws.qg[k]).exec, s));
     if (concurrent) {  // host work (and its own stream) while the graph runs
       GST_CUDA(cudaEventRecord(g->ev_done, s));
       (*concurrent)();
@@ -974,13 +986,15 @@ gst_status solve_one(gst_graph* g, const int32_t* group_ptr, const int32_t* memb
   std::copy(ws.h_stats, ws.h_stats + kNumStats, r->stats);
   r->ms[0] = elapsed(ws.ev[0], ws.ev[2]);
   double merge_ms = 0, grow_ms = 0;
-  for (int32_t l = 1; l <= k; ++l) {
-    merge_ms += elapsed(ws.ev[3 * l], ws.ev[3 * l + 1]);
-    if (l < k) grow_ms += elapsed(ws.ev[3 * l + 1], ws.ev[3 * l + 2]);
+  if (!use_graph || timed) {  // the per-wave events ran in this solve
+    for (int32_t l = 1; l <= k; ++l) {
+      merge_ms += elapsed(ws.ev[3 * l], ws.ev[3 * l + 1]);
+      if (l < k) grow_ms += elapsed(ws.ev[3 * l + 1], ws.ev[3 * l + 2]);
+    }
+    r->ms[3] = elapsed(ws.ev[1], ws.ev[2]);
   }
   r->ms[1] = grow_ms;
   r->ms[2] = merge_ms;
-  r->ms[3] = elapsed(ws.ev[1], ws.ev[2]);
   if (c.timeout) return fail(GST_TIMEOUT, "growth did not converge within max_rounds");
   if (c.overflow) return fail(GST_OVERFLOW, "a tree cost reached GST_COST_LIMIT");
   if (c.best == ~0ull) {

@@ -211,7 +211,9 @@ int64_t gst_result_states(const gst_result *r);
 /* CUDA kernels the solve launched (no counterpart in the reference). */
 int64_t gst_result_launches(const gst_result *r);
 /* Device milliseconds: [0] whole solve, [1] growth rounds (DPBF_GPU's *rt,
- * DPQ.cu:707-709), [2] merges, [3] argmin + backtrack. */
+ * DPQ.cu:707-709), [2] merges, [3] argmin + backtrack. [1]-[3] are measured
+ * by the host-launched driver and, with the CUDA-graph driver, when
+ * collect_stats is set (a graph with per-wave event nodes); 0 otherwise. */
 void gst_result_times(const gst_result *r, double *ms4);
 /* Statistics (filled when opts.collect_stats): [0] growth rounds launched,
  * [1] vertices scanned, [2] CSR entries scanned, [3] neighbour rows
