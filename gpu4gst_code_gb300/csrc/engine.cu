@@ -934,7 +934,6 @@ gst_status solve_one(gst_graph* g, const int32_t* group_ptr, const int32_t* memb
   st = ensure_tables(g, k);
   if (st != GST_OK) return st;
   cudaStream_t s = g->stream;
-  const int64_t V = g->V;
   const bool use_graph = o.use_graph != 0;
   // a non-sticky error left by an unrelated earlier runtime call would
   // otherwise surface at this solve's first kernel-launch check
