@@ -69,9 +69,12 @@ gst_status gst_propose(gst_graph* g, gst_scorer* s, const int32_t* group_ptr, co
 /* The exact DP pruned by the proposal's cost (opts as for gst_solve; its
  * upper_bound is replaced by the proposal's cost). With s NULL the fixed
  * feature score roots the proposal. With opts->use_graph the proposal runs
- * on a serving lane of g while the captured DP runs, and its cost reaches
- * the running DP as a bound (waves that started without it prune from the
- * next round on); the host loop proposes first and then solves. */
+ * on a serving lane of g (its own stream and scorer buffers, allocated on
+ * first use and freed with g) while the captured DP runs: it starts once
+ * the DP's wave 1 has grown, takes its paths from that wave, and its cost
+ * reaches the running DP as a bound (waves that started without it prune
+ * from the next round on); a proposal the DP outruns is given up. The host
+ * loop proposes first and then solves. */
 gst_status gst_solve_learned(gst_graph* g, gst_scorer* s, const int32_t* group_ptr, const int32_t* members, int32_t k,
                              const gst_opts* opts, gst_result** out);
 
